@@ -1,0 +1,419 @@
+"""Benchmark of the real-time render path on GB300 (one JSON line on stdout).
+
+Workload: the seeded mesh / IBL scene at scale (4096 worlds x one 128x128 camera, 6 displaced
+icospheres of 5120 triangles + 10 primitives, 1024x512 HDR environment, 512x512 albedo / ORM /
+normal maps with mips, 2x2 supersampling, mirror floor of reflectance 0.3, per-world materials and
+environment rotation). A step is refit_bvh + render of one frame of every world.
+
+  value      Mpix/s from CUDA events around each step (inputs resident on the device); L2 is
+             flushed (a 256 MB write) before every timed step, outside the events.
+  e2e        the same metric through the public API with host buffers: every step copies the
+             geom / camera / light poses from pinned host memory to the device, refits, renders
+             and copies the packed RGB images back to pinned host memory.
+  roofline   the render kernel's algorithmic HBM bytes (outputs written once, world blocks and
+             tables read once) per launch over its event-timed duration, against the measured
+             copy bandwidth; the kernel is bound by FP32 issue and traversal latency, not HBM,
+             so this fraction is small by construction (see "issue").
+  cpu_baseline  the CPU oracle (scalar C restatement of the reference's real-time tier, OpenMP
+             over all host cores) on a bounded sample of the same workload.
+
+--impl reference times the reference's own CPU implementation of the path: the reference is
+Python on Warp / MuJoCo Warp (not installable here), so its CPU path is timed through the C
+restatement of the oracle, on all host threads, with the same config and metric.
+Multi-GPU (torchrun, N > 1): one replica of the workload per GPU, no collective on the data path
+(weak scaling); rank 0 prints the aggregate.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpix/s (real-time tier, 1 GB300)"
+UNIT = "Mpix/s"
+
+
+def _peaks() -> dict:
+  p = ROOT / "MEASURED_PEAKS.json"
+  if p.exists():
+    return json.loads(p.read_text())
+  return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+class ClockSampler:
+  """nvidia-smi clock / throttle samples every 200 ms while the timed region runs."""
+
+  QUERY = (
+    "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+  )
+
+  def __init__(self, index: int):
+    self.index = index
+    self.proc = None
+    self.lines: list[str] = []
+
+  def __enter__(self):
+    try:
+      self.proc = subprocess.Popen(
+        ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200"],
+        stdout=subprocess.PIPE,
+        stderr=subprocess.DEVNULL,
+        text=True,
+      )
+      self.thread = threading.Thread(target=self._read, daemon=True)
+      self.thread.start()
+    except OSError:
+      self.proc = None
+    return self
+
+  def _read(self):
+    for line in self.proc.stdout:
+      self.lines.append(line.strip())
+
+  def __exit__(self, *exc):
+    if self.proc is not None:
+      self.proc.terminate()
+      try:
+        self.proc.wait(timeout=5)
+      except subprocess.TimeoutExpired:
+        self.proc.kill()
+
+  def summary(self) -> dict:
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in self.lines:
+      parts = [p.strip() for p in line.split(",")]
+      if len(parts) < 9:
+        continue
+      try:
+        sm.append(float(parts[1]))
+        smax.append(float(parts[2]))
+      except ValueError:
+        continue
+      for name, flag in zip(names, parts[5:9], strict=False):
+        if flag.lower() == "active":
+          reasons.add(name)
+    if not sm:
+      return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _world_block_bytes(rc) -> int:
+  return int(rc.world_blocks.numel() * 4)
+
+
+def algorithmic_bytes(rc) -> int:
+  """Compulsory HBM bytes of one render launch: every output written once, the world blocks,
+  textures, environment and mesh BVHs read once."""
+  b = rc.base
+  n = rc.nworld
+  out = b.rgb_data.numel() * 4 + b.depth_data.numel() * 4 + b.seg_data.numel() * 4
+  if rc.render_hdr:
+    out += rc.hdr_data.numel() * 4
+  inputs = _world_block_bytes(rc)
+  for t in (rc.tex_data, rc.blas_nodes, rc.blas_tris):
+    if t is not None:
+      inputs += t.numel() * t.element_size()
+  if rc.env is not None:
+    inputs += rc.env.radiance_data.numel() + rc.env.prefiltered.numel() * 2
+  del n
+  return int(out + inputs)
+
+
+def _traffic(workload: str) -> float | None:
+  p = ROOT / "profiles" / "ncu_traffic.json"
+  if not p.exists():
+    return None
+  try:
+    data = json.loads(p.read_text())
+    entry = data.get(workload)
+    return float(entry["bytes_per_launch"]) if entry else None
+  except (ValueError, KeyError, TypeError):
+    return None
+
+
+def make_scene(args):
+  from mujoco_warp_pbr_gb300 import synthetic
+
+  if args.workload == "mesh_ibl":
+    return synthetic.mesh_ibl_scene(seed=args.seed, nworld=args.nworld, res=args.res)
+  return synthetic.primitive_scene(seed=args.seed, nworld=args.nworld, res=args.res)
+
+
+def cpu_baseline(sc, budget_s: float, nthreads: int = 0) -> dict:
+  """Oracle Mpix/s on a bounded sample of worlds (grown until it runs for about budget_s)."""
+  from oracle import oracle
+
+  o = oracle.OracleScene(sc.mjm, sc.mjd, sc.nworld, sc.options, sc.per_world)
+  npix = sum(w * h for w, h in o.hc.outputs["cam_res"])
+  worlds = 1
+  t0 = time.perf_counter()
+  o.render(seed=0, worlds=(0, 1), nthreads=nthreads)
+  dt = time.perf_counter() - t0
+  while dt < budget_s / 4 and worlds * 2 <= sc.nworld:
+    worlds *= 2
+    t0 = time.perf_counter()
+    o.render(seed=0, worlds=(0, worlds), nthreads=nthreads)
+    dt = time.perf_counter() - t0
+  cores = oracle.load().oracle_nthreads() if nthreads <= 0 else nthreads
+  return {
+    "value": worlds * npix / dt / 1e6,
+    "unit": UNIT,
+    "cores": int(cores),
+    "kind": "port",
+    "sample": f"{worlds} of {sc.nworld} worlds x {npix} px, {dt:.1f} s",
+  }
+
+
+def run_reference(args) -> None:
+  """--impl reference: the reference's CPU path (C restatement) on all host threads."""
+  rank = int(os.environ.get("RANK", "0"))
+  if rank != 0:
+    return
+  sc = make_scene(args)
+  from oracle import oracle
+
+  o = oracle.OracleScene(sc.mjm, sc.mjd, sc.nworld, sc.options, sc.per_world)
+  npix = sum(w * h for w, h in o.hc.outputs["cam_res"])
+  # each step renders a bounded sample of the worlds (about 2 s of CPU work)
+  t0 = time.perf_counter()
+  o.render(seed=0, worlds=(0, 1))
+  one = time.perf_counter() - t0
+  worlds = int(max(1, min(sc.nworld, 2.0 / max(one, 1e-6))))
+  for _ in range(args.warmup):
+    o.render(seed=0, worlds=(0, min(worlds, 2)))
+  times = []
+  for step in range(args.steps):
+    t0 = time.perf_counter()
+    o.render(seed=step, worlds=(0, worlds))
+    times.append(time.perf_counter() - t0)
+  total = sum(times)
+  value = worlds * npix * args.steps / total / 1e6
+  cores = oracle.load().oracle_nthreads()
+  print(
+    json.dumps(
+      {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": _config(args, sc),
+        "cpu_baseline": {
+          "value": value,
+          "unit": UNIT,
+          "cores": int(cores),
+          "kind": "port",
+          "sample": f"{worlds} of {sc.nworld} worlds per step",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference is Python on Warp/MuJoCo Warp (not installable offline); its CPU path is timed through the oracle's C restatement",
+      }
+    )
+  )
+
+
+def _config(args, sc) -> dict:
+  cfg = {
+    "workload": sc.name,
+    "nworld": sc.nworld,
+    "cam_res": [args.res, args.res],
+    "samples_per_pixel": sc.options.get("samples_per_pixel", 1) ** 2,
+    "seed": args.seed,
+    "l2": "flushed before every timed step (256 MB write)",
+  }
+  if args.workload == "mesh_ibl":
+    cfg.update({"meshes": 6, "triangles_per_mesh": 5120, "primitives": 10, "env": "1024x512", "textures": "3x512^2", "mirror_floor": 0.3})
+  else:
+    cfg.update({"primitives": 8, "lights": 2, "shadow_samples": sc.options.get("shadow_samples", 1)})
+  return cfg
+
+
+def run(args) -> None:
+  import torch
+  import torch.distributed as dist
+
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import _lib
+  from mujoco_warp_pbr_gb300 import synthetic
+
+  world_size = int(os.environ.get("WORLD_SIZE", "1"))
+  rank = int(os.environ.get("RANK", "0"))
+  local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+  sc = make_scene(args)
+  baseline = None
+  if rank == 0 and not args.no_cpu_baseline:
+    baseline = cpu_baseline(sc, args.cpu_budget)
+  torch.cuda.set_device(local_rank)
+  if world_size > 1:
+    dist.init_process_group("nccl")
+  dev = torch.device("cuda", local_rank)
+  m = mjpbr.put_model(sc.mjm, device=dev)
+  d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld, device=dev)
+  rc = mjpbr.create_render_context(sc.mjm, sc.nworld, data=sc.mjd, device=dev, **sc.options)
+  synthetic.apply_per_world(sc, m, rc)
+  stream = torch.cuda.current_stream(dev)
+  flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+  npix = sc.nworld * sum(w * h for w, h in rc.base.cam_res)
+
+  def step(seed: int) -> None:
+    mjpbr.refit_bvh(m, d, rc)
+    mjpbr.render(m, d, rc, seed=seed)
+
+  for i in range(args.warmup):
+    step(i)
+  torch.cuda.synchronize()
+  assert mjpbr.check_errors(rc) == 0, "kernels reported an error"
+
+  # ---- device-resident timing, per-step events, L2 flushed outside the events
+  starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+  mids = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+  ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+  scene = mjpbr.scene_descriptor(m, d, rc)
+  if world_size > 1:
+    dist.barrier()
+  torch.cuda.synchronize()
+  with ClockSampler(local_rank) as clocks:
+    for i in range(args.steps):
+      flush.zero_()
+      starts[i].record(stream)
+      _lib.call("mjpbr_refit_bvh", scene, stream.cuda_stream)
+      mids[i].record(stream)
+      _lib.call("mjpbr_render", scene, 1000 + i, stream.cuda_stream)
+      ends[i].record(stream)
+    torch.cuda.synchronize()
+  if world_size > 1:
+    dist.barrier()
+  step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends, strict=True)]
+  render_ms = [s.elapsed_time(e) for s, e in zip(mids, ends, strict=True)]
+  total_ms = sum(step_ms)
+  if world_size > 1:
+    t = torch.tensor([total_ms], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+  value = npix * args.steps * world_size / (total_ms / 1000.0) / 1e6
+  assert mjpbr.check_errors(rc) == 0
+
+  # ---- end to end through the public API with host buffers
+  host = {name: getattr(d, name).cpu().pin_memory() for name in ("geom_xpos", "geom_xmat", "cam_xpos", "cam_xmat", "light_xpos", "light_xdir")}
+  out_host = torch.empty(rc.base.rgb_data.shape, dtype=rc.base.rgb_data.dtype).pin_memory()
+  h2d = sum(t.numel() * t.element_size() for t in host.values())
+  d2h = out_host.numel() * out_host.element_size()
+  e2e_steps = max(3, args.steps // 2)
+  for i in range(2):
+    for name, t in host.items():
+      getattr(d, name).copy_(t, non_blocking=True)
+    step(i)
+    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+  torch.cuda.synchronize()
+  if world_size > 1:
+    dist.barrier()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  for i in range(e2e_steps):
+    for name, t in host.items():
+      getattr(d, name).copy_(t, non_blocking=True)
+    step(2000 + i)
+    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+  e1.record(stream)
+  torch.cuda.synchronize()
+  e2e_ms = e0.elapsed_time(e1)
+  if world_size > 1:
+    t = torch.tensor([e2e_ms], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_ms = float(t.item())
+  e2e_value = npix * e2e_steps * world_size / (e2e_ms / 1000.0) / 1e6
+
+  if rank == 0:
+    peaks = _peaks()
+    render_avg = sum(render_ms) / len(render_ms)
+    alg = algorithmic_bytes(rc)
+    achieved = alg / (render_avg / 1000.0) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = _traffic(sc.name)
+    line = {
+      "metric": METRIC,
+      "value": value,
+      "unit": UNIT,
+      "n_gpus": world_size,
+      "steps": args.steps,
+      "warmup": args.warmup,
+      "ms_per_step": total_ms / args.steps,
+      "higher_is_better": True,
+      "scaling": "weak",
+      "vs_baseline": None,
+      "dtype": "f32",
+      "data": "synthetic (seeded scenes; no dataset)",
+      "config": _config(args, sc),
+      "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+      "roofline": {
+        "bound": "hbm",
+        "kernel": "rt_kernel",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": traffic,
+        "algorithmic_bytes_per_launch": alg,
+        "peak_source": "measured" if "fallback" not in peaks else "fallback",
+      },
+      "render_ms": render_avg,
+      "refit_ms": (total_ms / args.steps) - render_avg,
+      "rays_note": "primary rays = pixels x supersamples; shadow and mirror rays extra",
+      "gpu_launches": 2 * args.steps,
+      "clocks": clocks.summary(),
+      "cpu_baseline": baseline,
+    }
+    print(json.dumps(line))
+  if world_size > 1:
+    dist.destroy_process_group()
+
+
+def main() -> None:
+  p = argparse.ArgumentParser()
+  p.add_argument("--gpus", type=int, default=1)
+  p.add_argument("--steps", type=int, default=20)
+  p.add_argument("--warmup", type=int, default=3)
+  p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+  p.add_argument("--workload", choices=["mesh_ibl", "primitives"], default="mesh_ibl")
+  p.add_argument("--nworld", type=int, default=None)
+  p.add_argument("--res", type=int, default=None)
+  p.add_argument("--seed", type=int, default=0)
+  p.add_argument("--cpu-budget", type=float, default=15.0)
+  p.add_argument("--no-cpu-baseline", action="store_true")
+  args = p.parse_args()
+  if args.nworld is None:
+    args.nworld = 4096 if args.workload == "mesh_ibl" else 16
+  if args.res is None:
+    args.res = 128 if args.workload == "mesh_ibl" else 64
+  args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+  if args.impl == "reference":
+    run_reference(args)
+  else:
+    run(args)
+
+
+if __name__ == "__main__":
+  main()

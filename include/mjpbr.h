@@ -1,0 +1,377 @@
+/*
+ * mjpbr.h — C ABI of the GB300-native batched PBR render path (libmjpbr.so).
+ *
+ * The library renders thousands of MuJoCo worlds per launch on one sm_103a GPU. Every entry
+ * point takes a plain-old-data scene descriptor (MjpbrScene) that holds device pointers to the
+ * model, data and render-context arrays plus the render settings, and a CUDA stream
+ * (cudaStream_t passed as void*). Entry points return an int status (MJPBR_OK = 0); on failure
+ * mjpbr_last_error() returns a message for the calling thread. No C++ exception crosses the ABI,
+ * no entry point allocates device memory unless its comment says so, and none synchronises the
+ * stream, so calls can be captured into a CUDA graph.
+ *
+ * Arrays follow MuJoCo Warp's batching convention: a table whose leading dimension is a batch
+ * dimension (an mjpbr_f32b / mjpbr_i32b) is indexed with worldid % nbatch, so nbatch is 1 (one
+ * value shared by every world) or nworld (one per world). Matrices are row-major 3x3 (MuJoCo's
+ * xmat). Vectors are packed float triples.
+ *
+ * Reference interfaces replaced (julien-blanchon/mujoco_warp_pbr, paths inside that project):
+ *   mjpbr_refit_bvh        mujoco_warp.refit_bvh(m, d, rc.base)          (called at tests/conftest.py:44,
+ *                                                                          benchmarks/bench.py:184-186)
+ *   mjpbr_render           mujoco_warp_pbr.render(m, d, rc, seed)        (mujoco_warp_pbr/_src/render.py:431-460)
+ *   mjpbr_get_rgb          mujoco_warp_pbr.get_rgb(rc, cam, out)         (mujoco_warp_pbr/_src/output.py:34-38)
+ *   mjpbr_get_depth        mujoco_warp_pbr.get_depth(rc, cam, s, out)    (mujoco_warp_pbr/_src/output.py:41-45)
+ *   mjpbr_get_segmentation mujoco_warp_pbr.get_segmentation(...)         (mujoco_warp_pbr/_src/output.py:48-52)
+ *   mjpbr_get_image        get_hdr / get_albedo / get_normal             (mujoco_warp_pbr/_src/output.py:55-152)
+ *   mjpbr_dfg_lut          ibl.dfg_lut_array                              (mujoco_warp_pbr/_src/ibl.py:62-101)
+ *   mjpbr_build_mips       mip chains of texture.upload_textures / EnvironmentMap
+ *                                                                         (mujoco_warp_pbr/_src/texture.py:63-101,
+ *                                                                          mujoco_warp_pbr/_src/envmap.py:330-340)
+ *   mjpbr_prefilter_env    envmap._prefilter                              (mujoco_warp_pbr/_src/envmap.py:171-221)
+ *   mjpbr_denoise_atrous   denoise.denoise                                (mujoco_warp_pbr/_src/denoise.py:214-248)
+ *   mjpbr_build_scene_bvh  scene BVH build of mujoco_warp.create_render_context (third party; called at
+ *                                                                          mujoco_warp_pbr/_src/io.py:511-528)
+ *   mjpbr_build_mesh_bvh   per-mesh BVH build (warp.Mesh, mujoco_warp_pbr/_src/io.py:164-179,198-203)
+ */
+#ifndef MJPBR_H_
+#define MJPBR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MJPBR_ABI_VERSION 1
+
+/* Most rendering cameras of one context (the per-camera tables below are inline). */
+#define MJPBR_MAX_RENDER 16
+/* MuJoCo's texture roles (mjNTEXROLE). */
+#define MJPBR_NTEXROLE 10
+/* Levels of a mip chain (16384² textures at most). */
+#define MJPBR_MAX_MIPS 15
+
+enum MjpbrStatus {
+  MJPBR_OK = 0,
+  MJPBR_ERR_ARG = 1,         /* invalid argument (message in mjpbr_last_error) */
+  MJPBR_ERR_CUDA = 2,        /* a CUDA call failed */
+  MJPBR_ERR_DEVICE = 3,      /* a kernel reported an error through the scene's error word */
+  MJPBR_ERR_UNSUPPORTED = 4  /* feature not built into this library */
+};
+
+/* MuJoCo enums used by the arrays (mjtGeom, mjtLightType, mjtProjection, mjtTextureRole). */
+enum MjpbrGeomType {
+  MJPBR_GEOM_PLANE = 0, MJPBR_GEOM_HFIELD = 1, MJPBR_GEOM_SPHERE = 2, MJPBR_GEOM_CAPSULE = 3,
+  MJPBR_GEOM_ELLIPSOID = 4, MJPBR_GEOM_CYLINDER = 5, MJPBR_GEOM_BOX = 6, MJPBR_GEOM_MESH = 7,
+  MJPBR_GEOM_SDF = 8
+};
+enum MjpbrLightType { MJPBR_LIGHT_SPOT = 0, MJPBR_LIGHT_DIRECTIONAL = 1, MJPBR_LIGHT_POINT = 2, MJPBR_LIGHT_IMAGE = 3 };
+enum MjpbrProjection { MJPBR_PROJ_PERSPECTIVE = 0, MJPBR_PROJ_ORTHOGRAPHIC = 1 };
+enum MjpbrTexRole {
+  MJPBR_ROLE_USER = 0, MJPBR_ROLE_RGB = 1, MJPBR_ROLE_OCCLUSION = 2, MJPBR_ROLE_ROUGHNESS = 3,
+  MJPBR_ROLE_METALLIC = 4, MJPBR_ROLE_NORMAL = 5, MJPBR_ROLE_OPACITY = 6, MJPBR_ROLE_EMISSIVE = 7,
+  MJPBR_ROLE_RGBA = 8, MJPBR_ROLE_ORM = 9
+};
+/* Tone mappers, light models, tiers and thread orders (mujoco_warp_pbr/_src/types.py:29-103). */
+enum MjpbrToneMapper { MJPBR_TONE_PBR_NEUTRAL = 0, MJPBR_TONE_ACES = 1, MJPBR_TONE_CLAMP = 2 };
+enum MjpbrLightModel { MJPBR_LIGHT_MODEL_PHYSICAL = 0, MJPBR_LIGHT_MODEL_MUJOCO = 1 };
+enum MjpbrTier { MJPBR_TIER_REALTIME = 0, MJPBR_TIER_PATH = 1 };
+enum MjpbrRenderOrder { MJPBR_ORDER_ROW = 0, MJPBR_ORDER_TILED = 1, MJPBR_ORDER_WORLD = 2 };
+/* Texel formats of MjpbrTexture. */
+enum MjpbrTexFormat { MJPBR_TEX_RGBA8 = 0, MJPBR_TEX_RGBA16F = 1 };
+
+/* A batched table: nbatch rows (1 or nworld), row r used by worlds with worldid % nbatch == r. */
+typedef struct mjpbr_f32b { const float* ptr; int32_t nbatch; int32_t pad_; } mjpbr_f32b;
+typedef struct mjpbr_i32b { const int32_t* ptr; int32_t nbatch; int32_t pad_; } mjpbr_i32b;
+
+/* One mipmapped 2D texture inside MjpbrScene.tex_data (RGBA, row-major levels). */
+typedef struct MjpbrTexture {
+  int32_t format;   /* MjpbrTexFormat */
+  int32_t width;    /* level 0 */
+  int32_t height;
+  int32_t nlevel;
+  int64_t level_offset[MJPBR_MAX_MIPS]; /* byte offset of each level in tex_data */
+  int32_t pad_[2];
+} MjpbrTexture;
+
+/* Render settings (mujoco_warp_pbr/_src/kernel_inputs.py:47-116 plus the path-tier and denoiser
+ * parameters of PbrRenderContext, mujoco_warp_pbr/_src/types.py:123-322). Booleans are 0 / 1. */
+typedef struct MjpbrSettings {
+  int32_t tier;
+  int32_t render_order;
+  int32_t samples_per_axis;  /* real-time supersampling per axis (N x N rays) */
+  int32_t tone_mapper;
+  int32_t render_hdr;
+  int32_t render_guides;
+  int32_t light_model;
+  int32_t use_shadows;
+  int32_t shadow_samples;    /* > 1: soft shadows from bulbradius */
+  int32_t headlight_active;
+  int32_t has_env;           /* an environment map lights the scene */
+  int32_t env_background;    /* missed rays show the environment map */
+  int32_t textures;          /* any texture role is sampled */
+  int32_t base_color_map;
+  int32_t normal_map;
+  int32_t orm_map;
+  int32_t emissive_map;
+  int32_t opacity_map;
+  int32_t specular_aa;
+  int32_t vertex_normals;
+  int32_t has_reflection;    /* MuJoCo reflectance adds a mirror ray */
+  int32_t has_transparency;
+  int32_t max_layers;
+  int32_t cull_backfaces;
+  int32_t path_samples;      /* path tier: samples per pixel */
+  int32_t max_depth;         /* path tier: bounces */
+  int32_t rr_depth;          /* path tier: Russian roulette start */
+  int32_t denoise;           /* path tier: write denoiser features instead of RGB */
+  float znear;
+  float zfar;                /* <= 0: unbounded */
+  float shadow_light_fraction;
+  float headlight_intensity; /* illuminance times exposure (physical model) */
+  float headlight_diffuse[3];
+  float headlight_specular[3];
+  float background[3];       /* linear display colour of missed rays */
+  float inv_texel_angle;     /* inverse angular size of a radiance texel (env background LOD) */
+  float denoise_sigma_color;
+  float denoise_sigma_normal;
+  float denoise_sigma_depth;
+  float denoise_sigma_albedo;
+} MjpbrSettings;
+
+/* Everything one render reads and writes. Device pointers unless stated otherwise. Pointers of
+ * features the settings switch off may be NULL. */
+typedef struct MjpbrScene {
+  int32_t abi_version;       /* MJPBR_ABI_VERSION */
+  int32_t nworld;
+  int32_t ngeom;
+  int32_t nmat;
+  int32_t nlight;
+  int32_t ncam;              /* model cameras */
+  int32_t nmesh;
+  int32_t ntex;
+  int32_t nenv;
+
+  /* ---- Model (mujoco_warp.Model fields) ---- */
+  const int32_t* geom_type;        /* (ngeom,) MjpbrGeomType */
+  mjpbr_i32b geom_dataid;          /* (*, ngeom) mesh id of mesh geoms */
+  mjpbr_i32b geom_matid;           /* (*, ngeom) */
+  mjpbr_f32b geom_size;            /* (*, ngeom, 3) */
+  mjpbr_f32b geom_rgba;            /* (*, ngeom, 4) */
+  mjpbr_f32b mat_rgba;             /* (*, nmat, 4) */
+  mjpbr_f32b mat_emission;         /* (*, nmat) */
+  mjpbr_i32b mat_texid;            /* (*, nmat, MJPBR_NTEXROLE) */
+  mjpbr_f32b mat_texrepeat;        /* (*, nmat, 2) */
+  mjpbr_i32b mat_texuniform;       /* (*, nmat) */
+  mjpbr_i32b light_type;           /* (*, nlight) */
+  mjpbr_i32b light_castshadow;     /* (*, nlight) */
+  mjpbr_i32b light_active;         /* (*, nlight) */
+  mjpbr_f32b light_attenuation;    /* (*, nlight, 3) */
+  mjpbr_f32b light_cutoff;         /* (*, nlight) degrees */
+  mjpbr_f32b light_exponent;       /* (*, nlight) */
+  mjpbr_f32b light_diffuse;        /* (*, nlight, 3) */
+  mjpbr_f32b light_specular;       /* (*, nlight, 3) */
+  const int32_t* cam_projection;   /* (ncam,) MjpbrProjection */
+  mjpbr_f32b cam_fovy;             /* (*, ncam) degrees (orthographic: frustum height) */
+  const float* cam_sensorsize;     /* (ncam, 2); 0: use fovy */
+  mjpbr_f32b cam_intrinsic;        /* (*, ncam, 4) fx, fy, cx, cy in sensor units */
+  const int32_t* mesh_vertadr;     /* (nmesh,) */
+  const int32_t* mesh_faceadr;     /* (nmesh,) */
+  const int32_t* mesh_normaladr;   /* (nmesh,) */
+  const int32_t* mesh_texcoordadr; /* (nmesh,) first texcoord, -1: no UVs */
+  const float* mesh_vert;          /* (nvert, 3) mesh frame */
+  const int32_t* mesh_face;        /* (nface, 3) */
+  const float* mesh_normal;        /* (nnormal, 3) */
+  const int32_t* mesh_facenormal;  /* (nface, 3) */
+  const float* mesh_texcoord;      /* (ntexcoord, 2) */
+  const int32_t* mesh_facetexcoord;/* (nface, 3) */
+
+  /* ---- Data (mujoco_warp.Data fields) ---- */
+  const float* geom_xpos;          /* (nworld, ngeom, 3) */
+  const float* geom_xmat;          /* (nworld, ngeom, 9) */
+  const float* cam_xpos;           /* (nworld, ncam, 3) */
+  const float* cam_xmat;           /* (nworld, ncam, 9) */
+  const float* light_xpos;         /* (nworld, nlight, 3) */
+  const float* light_xdir;         /* (nworld, nlight, 3) */
+
+  /* ---- Render context: cameras and outputs (mujoco_warp.RenderContext) ---- */
+  int32_t nrender;                               /* rendering cameras */
+  int32_t total_rays;                            /* sum of W*H over rendering cameras */
+  int32_t cam_id_map[MJPBR_MAX_RENDER];          /* rendering camera -> model camera */
+  int32_t cam_res[MJPBR_MAX_RENDER][2];          /* width, height */
+  int32_t render_rgb[MJPBR_MAX_RENDER];
+  int32_t render_depth[MJPBR_MAX_RENDER];
+  int32_t render_seg[MJPBR_MAX_RENDER];
+  int32_t ray_adr[MJPBR_MAX_RENDER];             /* first pixel of each camera among total_rays */
+  int32_t rgb_adr[MJPBR_MAX_RENDER];             /* -1: camera renders no RGB */
+  int32_t depth_adr[MJPBR_MAX_RENDER];
+  int32_t seg_adr[MJPBR_MAX_RENDER];
+  int32_t rgb_stride;                            /* pixels per world of rgb_data, hdr, guides */
+  int32_t depth_stride;
+  int32_t seg_stride;
+  int32_t pad0_;
+  uint32_t* rgb_data;                            /* (nworld, rgb_stride) RGBA8, R in the low byte */
+  float* depth_data;                             /* (nworld, depth_stride) */
+  int32_t* seg_data;                             /* (nworld, seg_stride, 2) (id, type) */
+  float* hdr_data;                               /* (nworld, rgb_stride, 3) linear, pre-exposure */
+  float* guide_albedo;                           /* (nworld, rgb_stride, 3) */
+  float* guide_normal;                           /* (nworld, rgb_stride, 3) */
+
+  /* ---- Render context: per-world material, light and exposure tables ---- */
+  mjpbr_f32b geom_metallic;        /* (*, ngeom) */
+  mjpbr_f32b geom_roughness;       /* (*, ngeom) perceptual */
+  mjpbr_f32b geom_reflectance;     /* (*, ngeom) dielectric F0 = 0.16 r^2 */
+  mjpbr_f32b mat_reflectance;      /* (*, nmat) MuJoCo mirror reflectance */
+  mjpbr_f32b light_intensity;      /* (*, nlight) lux or candela */
+  mjpbr_f32b light_range;          /* (*, nlight) */
+  mjpbr_f32b light_bulbradius;     /* (*, nlight) */
+  mjpbr_f32b exposure;             /* (*) */
+  mjpbr_f32b ambient_radiance;     /* (*, 3) */
+  mjpbr_i32b env_id;               /* (*) */
+  mjpbr_f32b env_intensity;        /* (*) */
+  mjpbr_f32b env_yaw;              /* (*) radians */
+
+  /* ---- Scene BVH: one binary tree per world over the enabled geoms ---- */
+  int32_t nbvh_geom;               /* enabled geoms (slots) per world */
+  int32_t nnode;                   /* inner nodes per world (nbvh_geom - 1, at least 1) */
+  const int32_t* enabled_geom_ids; /* (nbvh_geom,) slot -> geom id */
+  mjpbr_i32b tlas_child;           /* (*, nnode, 2) child refs: >= 0 inner node, < 0 leaf slot ~ref */
+  const float* mesh_bounds;        /* (nmesh, 6) local AABB of each mesh (lower, upper) */
+  float* world_blocks;             /* (nworld, world_block_floats) written by mjpbr_refit_bvh */
+  int32_t world_block_floats;      /* per-world block size in floats (a multiple of 4) */
+  int32_t pad1_;
+
+  /* ---- Mesh BVHs (one per mesh, shared by every world) ---- */
+  const float* blas_nodes;         /* (nblasnode, 16) child-bounds nodes, see mjpbr_build_mesh_bvh */
+  const float* blas_tris;          /* (nblastri, 12) v0, v1, v2 (xyz + face id bits in w of v0) */
+  const int32_t* blas_root;        /* (nmesh,) first node of each mesh */
+  const int32_t* blas_tri_base;    /* (nmesh,) first triangle of each mesh */
+
+  /* ---- Textures ---- */
+  const MjpbrTexture* textures;    /* (ntex,) device copy */
+  const uint8_t* tex_data;
+
+  /* ---- Environment maps (image-based lighting) ---- */
+  const float* dfg_lut;            /* (dfg_size, dfg_size, 2) rows: perceptual roughness, cols: NoV */
+  int32_t dfg_size;
+  int32_t prefilter_levels;        /* depth of the GGX-prefiltered stack */
+  int32_t prefilter_width;
+  int32_t prefilter_height;
+  const uint16_t* env_prefiltered; /* (nenv, levels, height, width, 4) float16 */
+  const MjpbrTexture* env_radiance;/* (nenv,) mipmapped radiance, formats RGBA16F, into env_data */
+  const uint8_t* env_data;
+  const float* env_sh;             /* (nenv, 9, 3) SH9 Lambertian radiance */
+  int32_t cdf_width;
+  int32_t cdf_height;
+  const float* env_prob;           /* (nenv, h, w) */
+  const float* env_marginal;       /* (nenv, h + 1) */
+  const float* env_conditional;    /* (nenv, h, w + 1) */
+
+  /* ---- Per-pixel camera rays (set_camera_rays), NULL for pinhole cameras ---- */
+  const float* ray_origin;         /* (total_rays, 3) camera frame */
+  const float* ray_direction;      /* (total_rays, 3) camera frame, zero: no ray */
+  int32_t bundle_res[MJPBR_MAX_RENDER][2];
+
+  /* ---- Path-tier denoiser features (nworld, rgb_stride) ---- */
+  float* aov_albedo;               /* (.., 3) */
+  float* aov_normal;               /* (.., 3) */
+  float* aov_depth;                /* (..) */
+  float* aov_emission;             /* (.., 3) */
+  float* aov_variance;             /* (..) */
+  float* denoise_buffers[2];       /* (.., 4) ping-pong */
+  int32_t denoise_iterations;
+  int32_t pad2_;
+
+  /* ---- Status ---- */
+  int32_t* error_word;             /* device int32, kernels OR error bits into it (may be NULL) */
+
+  MjpbrSettings settings;
+} MjpbrScene;
+
+/* ABI version this library was built with (MJPBR_ABI_VERSION). */
+int mjpbr_abi_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* mjpbr_last_error(void);
+
+/* Layout check for bindings written in other languages: out[0..7] = sizeof(MjpbrScene),
+ * sizeof(MjpbrSettings), sizeof(MjpbrTexture), offsetof(MjpbrScene, nrender),
+ * offsetof(MjpbrScene, world_blocks), offsetof(MjpbrScene, env_prefiltered),
+ * offsetof(MjpbrScene, error_word), offsetof(MjpbrScene, settings). */
+void mjpbr_struct_layout(int64_t out[8]);
+
+/* Size in floats of one world's block for a scene with these counts (used to size world_blocks). */
+int32_t mjpbr_world_block_floats(int32_t nbvh_geom, int32_t nnode, int32_t nlight, int32_t nrender);
+
+/* Per-geom world AABBs from the current poses, bottom-up refit of every world's scene BVH, and the
+ * per-world blocks (geom, light, camera records and BVH nodes) the render kernels stage into
+ * shared memory. Replaces mujoco_warp.refit_bvh(m, d, rc.base). Launches one kernel. */
+int mjpbr_refit_bvh(const MjpbrScene* scene, void* stream);
+
+/* Renders the frame into the output buffers (real-time or path-traced tier per settings.tier;
+ * with settings.denoise the path tier writes features and the caller runs mjpbr_denoise_atrous).
+ * Replaces mujoco_warp_pbr.render (mujoco_warp_pbr/_src/render.py:431-460). Call
+ * mjpbr_refit_bvh first whenever geometry or cameras moved. */
+int mjpbr_render(const MjpbrScene* scene, uint32_t seed, void* stream);
+
+/* Display RGB in [0, 1] of rendering camera `cam` into out (nworld_out, H, W, 3) float32.
+ * mujoco_warp_pbr/_src/output.py:34-38. */
+int mjpbr_get_rgb(const MjpbrScene* scene, int32_t cam, float* out, int32_t nworld_out, void* stream);
+
+/* Planar depth / depth_scale clamped to [0, 1] into out (nworld_out, H, W) float32.
+ * mujoco_warp_pbr/_src/output.py:41-45. */
+int mjpbr_get_depth(const MjpbrScene* scene, int32_t cam, float depth_scale, float* out, int32_t nworld_out,
+                    void* stream);
+
+/* (object id, object type) per pixel into out (nworld_out, H, W, 2) int32; background (-1, -1).
+ * mujoco_warp_pbr/_src/output.py:48-52. */
+int mjpbr_get_segmentation(const MjpbrScene* scene, int32_t cam, int32_t* out, int32_t nworld_out, void* stream);
+
+/* One camera's image of a per-RGB-pixel vec3 buffer: which = 0 hdr_data, 1 guide_albedo,
+ * 2 guide_normal, into out (nworld_out, H, W, 3). mujoco_warp_pbr/_src/output.py:55-152. */
+int mjpbr_get_image(const MjpbrScene* scene, int32_t which, int32_t cam, float* out, int32_t nworld_out,
+                    void* stream);
+
+/* Split-sum DFG table (size, size, 2) float32 into lut (device), nsample Hammersley samples per
+ * texel. mujoco_warp_pbr/_src/ibl.py:62-101. */
+int mjpbr_dfg_lut(float* lut, int32_t size, int32_t nsample, void* stream);
+
+/* Box-filters level 0 of a texture (tex: host description, data: device bytes at
+ * tex->level_offset) into its further levels
+ * (2x2 average per level, odd sizes truncate). The mip chains of texture uploads and environment
+ * maps, mujoco_warp_pbr/_src/texture.py:91-99 and mujoco_warp_pbr/_src/envmap.py:330-337. */
+int mjpbr_build_mips(const MjpbrTexture* tex, uint8_t* data, void* stream);
+
+/* GGX-prefiltered stack (levels, height, width, 4) float16 of one environment map (radiance: host
+ * description of a RGBA16F mipmapped texture in device bytes data), nsample importance samples per texel with filtered importance
+ * sampling. mujoco_warp_pbr/_src/envmap.py:171-221. */
+int mjpbr_prefilter_env(const MjpbrTexture* radiance, const uint8_t* data, int32_t levels, int32_t height,
+                        int32_t width, int32_t nsample, uint16_t* stack, void* stream);
+
+/* Edge-avoiding à-trous filter of the path tier's noisy HDR into rgb_data (and hdr_data with
+ * render_hdr): demodulation, denoise_iterations 5x5 passes, remodulation and tone mapping.
+ * mujoco_warp_pbr/_src/denoise.py:214-248. Uses scene.denoise_buffers as scratch. */
+int mjpbr_denoise_atrous(const MjpbrScene* scene, void* stream);
+
+/* Host: number of nodes of a binary BVH over nprim primitives (nprim - 1, at least 1). */
+int32_t mjpbr_bvh_node_count(int32_t nprim);
+
+/* Host: SAH-built binary BVH over nprim boxes (lower/upper (nprim, 3) host arrays), one primitive
+ * per leaf. child_out (nnode, 2) receives the child refs in the MjpbrScene.tlas_child encoding
+ * (>= 0 inner node, < 0 ~slot); children always come after their parent, so a reverse sweep
+ * refits bottom-up. Stands in for the scene BVH build of mujoco_warp.create_render_context. */
+int mjpbr_build_scene_bvh(const float* lower, const float* upper, int32_t nprim, int32_t* child_out);
+
+/* Host: SAH-built BVH of one triangle mesh (vert (nvert, 3), face (nface, 3) host arrays) with at
+ * most leaf_size triangles per leaf. nodes_out (mjpbr_bvh_node_count(nface), 16) floats and
+ * tris_out (nface, 12) floats receive the node and triangle records the render kernels read;
+ * bounds_out (6) the mesh AABB. Stands in for the warp.Mesh BVH of mujoco_warp's render context.
+ * Returns the number of nodes written in *nnode_out. */
+int mjpbr_build_mesh_bvh(const float* vert, int32_t nvert, const int32_t* face, int32_t nface, int32_t leaf_size,
+                         float* nodes_out, float* tris_out, float* bounds_out, int32_t* nnode_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MJPBR_H_ */

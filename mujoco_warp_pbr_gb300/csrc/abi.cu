@@ -1,0 +1,176 @@
+// C entry points of libmjpbr (declared in include/mjpbr.h): argument checks, error reporting and
+// dispatch to the kernel launchers. Nothing here synchronises or allocates.
+#include <cstdarg>
+#include <cstddef>
+#include <cstdio>
+#include <string>
+
+#include "abi_internal.h"
+#include "world_block.cuh"
+
+namespace mjpbr {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return MJPBR_OK;
+}
+
+namespace {
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int validate_scene(const MjpbrScene* s, bool need_outputs) {
+  if (!s) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  if (s->abi_version != MJPBR_ABI_VERSION) {
+    return set_error(MJPBR_ERR_ARG, "scene abi_version %d, library %d", s->abi_version, MJPBR_ABI_VERSION);
+  }
+  if (s->nworld < 1 || s->nworld > 65535) return set_error(MJPBR_ERR_ARG, "nworld must be in [1, 65535], got %d", s->nworld);
+  if (s->nrender < 1 || s->nrender > MJPBR_MAX_RENDER) {
+    return set_error(MJPBR_ERR_ARG, "nrender must be in [1, %d], got %d", MJPBR_MAX_RENDER, s->nrender);
+  }
+  if (s->nbvh_geom < 1 || s->nnode != (s->nbvh_geom > 1 ? s->nbvh_geom - 1 : 1)) {
+    return set_error(MJPBR_ERR_ARG, "scene BVH: %d geoms need %d nodes, got %d", s->nbvh_geom,
+                     s->nbvh_geom > 1 ? s->nbvh_geom - 1 : 1, s->nnode);
+  }
+  if (!s->world_blocks || !aligned16(s->world_blocks)) return set_error(MJPBR_ERR_ARG, "world_blocks must be 16-byte aligned");
+  BlockLayout L = block_layout(s->nbvh_geom, s->nnode, s->nlight, s->nrender);
+  if (s->world_block_floats < L.total || (s->world_block_floats & 3)) {
+    return set_error(MJPBR_ERR_ARG, "world_block_floats must be a multiple of 4 and >= %d, got %d", L.total,
+                     s->world_block_floats);
+  }
+  if (!s->geom_type || !s->geom_xpos || !s->geom_xmat || !s->cam_xpos || !s->cam_xmat || !s->enabled_geom_ids ||
+      !s->tlas_child.ptr || !s->geom_size.ptr || !s->geom_rgba.ptr || !s->geom_matid.ptr) {
+    return set_error(MJPBR_ERR_ARG, "scene is missing a geometry or camera array");
+  }
+  if (s->nlight > 0 && (!s->light_xpos || !s->light_xdir || !s->light_type.ptr || !s->light_active.ptr ||
+                        !s->light_castshadow.ptr || !s->light_intensity.ptr || !s->light_range.ptr ||
+                        !s->light_bulbradius.ptr || !s->light_diffuse.ptr || !s->light_specular.ptr ||
+                        !s->light_attenuation.ptr || !s->light_cutoff.ptr || !s->light_exponent.ptr)) {
+    return set_error(MJPBR_ERR_ARG, "scene is missing a light array");
+  }
+  for (int32_t c = 0; c < s->nrender; ++c) {
+    if (s->cam_res[c][0] < 1 || s->cam_res[c][1] < 1) return set_error(MJPBR_ERR_ARG, "camera %d has no pixels", c);
+    if (s->cam_id_map[c] < 0 || s->cam_id_map[c] >= s->ncam) return set_error(MJPBR_ERR_ARG, "camera map %d invalid", c);
+  }
+  if (need_outputs) {
+    if (!s->dfg_lut || s->dfg_size < 2) return set_error(MJPBR_ERR_ARG, "scene has no DFG table");
+    if (!s->exposure.ptr || !s->ambient_radiance.ptr || !s->geom_metallic.ptr || !s->geom_roughness.ptr ||
+        !s->geom_reflectance.ptr) {
+      return set_error(MJPBR_ERR_ARG, "scene is missing a material or exposure table");
+    }
+    const MjpbrSettings& st = s->settings;
+    if (st.samples_per_axis < 1 || st.shadow_samples < 1 || st.max_layers < 1) {
+      return set_error(MJPBR_ERR_ARG, "samples_per_axis, shadow_samples and max_layers must be at least 1");
+    }
+    if ((st.has_env || st.env_background) && (s->nenv < 1 || !s->env_sh || !s->env_prefiltered || !s->env_radiance)) {
+      return set_error(MJPBR_ERR_ARG, "environment lighting is on but the scene has no environment maps");
+    }
+    if (st.textures && (!s->textures || !s->tex_data || !s->mat_texid.ptr || !s->mat_texrepeat.ptr)) {
+      return set_error(MJPBR_ERR_ARG, "textures are on but the scene has no textures");
+    }
+    for (int32_t c = 0; c < s->nrender; ++c) {
+      if (s->render_rgb[c] && (s->rgb_adr[c] < 0 || !s->rgb_data)) return set_error(MJPBR_ERR_ARG, "rgb buffer missing");
+      if (s->render_depth[c] && (s->depth_adr[c] < 0 || !s->depth_data)) {
+        return set_error(MJPBR_ERR_ARG, "depth buffer missing");
+      }
+      if (s->render_seg[c] && (s->seg_adr[c] < 0 || !s->seg_data)) return set_error(MJPBR_ERR_ARG, "seg buffer missing");
+    }
+  }
+  return MJPBR_OK;
+}
+
+}  // namespace
+}  // namespace mjpbr
+
+using namespace mjpbr;
+
+extern "C" {
+
+int mjpbr_abi_version(void) { return MJPBR_ABI_VERSION; }
+
+const char* mjpbr_last_error(void) { return g_last_error.c_str(); }
+
+void mjpbr_struct_layout(int64_t out[8]) {
+  out[0] = (int64_t)sizeof(MjpbrScene);
+  out[1] = (int64_t)sizeof(MjpbrSettings);
+  out[2] = (int64_t)sizeof(MjpbrTexture);
+  out[3] = (int64_t)offsetof(MjpbrScene, nrender);
+  out[4] = (int64_t)offsetof(MjpbrScene, world_blocks);
+  out[5] = (int64_t)offsetof(MjpbrScene, env_prefiltered);
+  out[6] = (int64_t)offsetof(MjpbrScene, error_word);
+  out[7] = (int64_t)offsetof(MjpbrScene, settings);
+}
+
+int32_t mjpbr_world_block_floats(int32_t nbvh_geom, int32_t nnode, int32_t nlight, int32_t nrender) {
+  return block_layout(nbvh_geom, nnode, nlight, nrender).total;
+}
+
+int mjpbr_refit_bvh(const MjpbrScene* scene, void* stream) {
+  int rc = validate_scene(scene, false);
+  if (rc) return rc;
+  return refit_launch(*scene, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_render(const MjpbrScene* scene, uint32_t seed, void* stream) {
+  int rc = validate_scene(scene, true);
+  if (rc) return rc;
+  if (scene->settings.tier == MJPBR_TIER_PATH) return render_pt_launch(*scene, seed, static_cast<cudaStream_t>(stream));
+  return render_rt_launch(*scene, seed, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_get_rgb(const MjpbrScene* scene, int32_t cam, float* out, int32_t nworld_out, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return outputs_launch(*scene, 0, cam, 1.0f, out, nworld_out, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_get_depth(const MjpbrScene* scene, int32_t cam, float depth_scale, float* out, int32_t nworld_out,
+                    void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return outputs_launch(*scene, 1, cam, depth_scale, out, nworld_out, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_get_segmentation(const MjpbrScene* scene, int32_t cam, int32_t* out, int32_t nworld_out, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return outputs_launch(*scene, 2, cam, 1.0f, out, nworld_out, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_get_image(const MjpbrScene* scene, int32_t which, int32_t cam, float* out, int32_t nworld_out, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  if (which < 0 || which > 2) return set_error(MJPBR_ERR_ARG, "which must be 0 (hdr), 1 (albedo) or 2 (normal)");
+  return outputs_launch(*scene, 3 + which, cam, 1.0f, out, nworld_out, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_dfg_lut(float* lut, int32_t size, int32_t nsample, void* stream) {
+  return dfg_lut_launch(lut, size, nsample, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_build_mips(const MjpbrTexture* tex, uint8_t* data, void* stream) {
+  return build_mips_launch(tex, data, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_prefilter_env(const MjpbrTexture* radiance, const uint8_t* data, int32_t levels, int32_t height,
+                        int32_t width, int32_t nsample, uint16_t* stack, void* stream) {
+  return prefilter_launch(radiance, data, levels, height, width, nsample, stack, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_denoise_atrous(const MjpbrScene* scene, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return denoise_launch(*scene, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,450 @@
+// Real-time tier megakernel (mujoco_warp_pbr/_src/render.py:78-427 and camera.py:113-347).
+//
+// Work decomposition: one CTA of 256 threads per (world, camera tile). A tile is 32x8 pixels
+// (RenderOrder.ROW: a warp covers 32 pixels of one row) or 16x16 pixels made of 8x4 warp tiles
+// (RenderOrder.TILED). The CTA copies its world's block (BVH nodes, geom/light/camera records,
+// written by mjpbr_refit_bvh) into shared memory once; every thread then renders one pixel:
+// N x N supersamples, each a primary ray, surface evaluation, split-sum ambient, direct lights
+// with (soft) shadow rays, one optional mirror ray and translucent layers, tone mapped per sample,
+// averaged and sRGB-encoded. Depth, segmentation and guides come from the first sample.
+//
+// Pixels are addressed by camera and row-major pixel id; the random numbers of a pixel are keyed
+// by that id, so every thread order renders identical images.
+#include "abi_internal.h"
+#include "surface.cuh"
+
+namespace mjpbr {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr float kMinThroughput = 1.0f / 255.0f;
+constexpr float kMinTexels = 1.0e-8f;
+constexpr float kMinForward = 1.0e-6f;
+
+// Tiles of every rendering camera of a world, in camera order.
+struct TileMap {
+  int32_t ncam;
+  int32_t tile_w, tile_h;
+  int32_t tiles_x[MJPBR_MAX_RENDER];
+  int32_t tile_base[MJPBR_MAX_RENDER + 1];
+};
+
+struct Pixel {
+  int32_t cam;     // rendering camera
+  int32_t px, py;  // pixel
+  int32_t width, height;
+  int32_t pixelid;  // row-major within the camera image
+  const float* rec;  // camera record in the world block
+};
+
+// Camera-frame ray through sub-pixel cell (sx, sy) of a pixel divided into n x n cells (pinhole
+// or orthographic; MuJoCo Warp's compute_ray restated with the image plane at z = -1).
+MJ_DEV void camera_frame_ray(const Pixel& p, int32_t n, int32_t sx, int32_t sy, V3* dcam, V3* ocam) {
+  const float* c = p.rec;
+  int32_t ix = p.px * n + sx, iy = p.py * n + sy;
+  float u = ((float)ix + 0.5f) / (float)(p.width * n);
+  float v = ((float)iy + 0.5f) / (float)(p.height * n);
+  int32_t proj = __float_as_int(c[3]);
+  float half_h = c[13];
+  float aspect = (float)p.width / (float)p.height;
+  if (proj == MJPBR_PROJ_ORTHOGRAPHIC) {
+    *dcam = V3{0.0f, 0.0f, -1.0f};
+    *ocam = V3{(2.0f * u - 1.0f) * (half_h * aspect), (1.0f - 2.0f * v) * half_h, 0.0f};
+    return;
+  }
+  float x, y;
+  if (__float_as_int(c[14])) {
+    // intrinsics: principal point offset from the sensor centre, focal lengths in sensor units
+    x = (u * c[20] - 0.5f * c[20] - c[18]) / c[16];
+    y = (0.5f * c[21] - v * c[21] + c[19]) / c[17];
+  } else {
+    x = (2.0f * u - 1.0f) * (half_h * aspect);
+    y = (1.0f - 2.0f * v) * half_h;
+  }
+  float len = sqrtf(x * x + y * y + 1.0f);
+  *dcam = V3{x / len, y / len, -1.0f / len};
+  *ocam = v3(0.0f);
+}
+
+MJ_DEV M3 cam_mat(const float* c) {
+  M3 m;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) m.m[k] = c[4 + k];
+  return m;
+}
+
+struct RtCtx {
+  const MjpbrScene* s;
+  const float* blk;
+  BlockLayout L;
+  int32_t w;
+  float exposure;
+  V3 ambient;
+  int32_t env;
+  float env_yaw, env_scale;
+  int32_t err;
+};
+
+template <bool kMesh, bool kTex>
+struct Rt {
+  static MJ_DEV bool occluded(RtCtx& c, V3 o, V3 d, float max_dist) {
+    Ray r{o, d};
+    return any_hit<kMesh>(*c.s, c.blk, c.L, r, max_dist, c.s->settings.cull_backfaces != 0, &c.err);
+  }
+
+  // Fraction of the light reaching the point (render.py:81-127).
+  static MJ_DEV float light_visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist,
+                                       uint32_t seed, int32_t stream, int32_t nlight, int32_t li) {
+    const MjpbrSettings& st = c.s->settings;
+    V3 origin = point + normal * kRayOffset;
+    if (light.type == MJPBR_LIGHT_DIRECTIONAL) {
+      return occluded(c, origin, l, kUnboundedShadow) ? st.shadow_light_fraction : 1.0f;
+    }
+    if (st.shadow_samples <= 1) {
+      return occluded(c, origin, l, dist - kShadowGap) ? st.shadow_light_fraction : 1.0f;
+    }
+    V3 t1, t2;
+    orthonormal_basis(l, &t1, &t2);
+    float visible = 0.0f;
+    const int32_t ns = st.shadow_samples;
+    for (int32_t k = 0; k < ns; ++k) {
+      uint32_t counter = (uint32_t)(((stream * nlight + li) * ns + k) * 2);
+      float u0 = rand01(seed, counter), u1 = rand01(seed, counter + 1u);
+      float r = light.bulbradius * sqrtf(u0);
+      float sn, cs;
+      sincos_turns(u1, &sn, &cs);
+      V3 to = light.pos + (t1 * cs + t2 * sn) * r - origin;
+      float d = length(to);
+      if (!occluded(c, origin, to / d, d - kShadowGap)) visible += 1.0f;
+    }
+    float v = visible / (float)ns;
+    return v + (1.0f - v) * st.shadow_light_fraction;
+  }
+
+  static MJ_DEV V3 shade_light(RtCtx& c, const Light& light, const Lobes& lb, V3 point, V3 normal, V3 view, float nov,
+                               uint32_t seed, int32_t stream, int32_t nlight, int32_t li) {
+    const MjpbrSettings& st = c.s->settings;
+    V3 l, ds, ss;
+    float dist;
+    eval_light(light, st.light_model, point, &l, &dist, &ds, &ss);
+    float nol = dot(normal, l);
+    if (nol <= 0.0f || (length_sq(ds) == 0.0f && length_sq(ss) == 0.0f)) return v3(0.0f);
+    float vis = 1.0f;
+    if (st.use_shadows && light.castshadow) vis = light_visibility(c, light, point, normal, l, dist, seed, stream, nlight, li);
+    V3 h = fnormalize(l + view);
+    float noh = fmaxf(fdot(normal, h), 0.0f);
+    float loh = fmaxf(fdot(l, h), 0.0f);
+    V3 fr = cmul(specular_lobe(lb.f0, lb.alpha, noh, nov, nol, loh), lb.energy_comp);
+    V3 fd = lb.diffuse_color * (1.0f / kPi);
+    return (cmul(fd, ds) + cmul(fr, ss)) * (nol * vis);
+  }
+
+  // Outgoing radiance towards view, before exposure (render.py:184-239).
+  static MJ_DEV V3 shade_surface(RtCtx& c, const Surface& sf, V3 point, V3 normal, V3 view, V3 head_dir, uint32_t seed,
+                                 int32_t stream) {
+    const MjpbrScene& s = *c.s;
+    const MjpbrSettings& st = s.settings;
+    float nov = fmaxf(fdot(normal, view), 1.0e-4f);
+    Lobes lb = shading_lobes(s.dfg_lut, s.dfg_size, sf, nov);
+    V3 irradiance = c.ambient, prefiltered = c.ambient;
+    if (kTex && st.has_env) {
+      irradiance = c.ambient + eval_sh9(s.env_sh + c.env * 27, rotate_yaw(normal, -c.env_yaw)) * c.env_scale;
+      V3 r = view - normal * (2.0f * fdot(view, normal));
+      float a2 = lb.alpha * lb.alpha;
+      V3 dominant = fnormalize(-r * (1.0f - a2) + normal * a2);
+      const uint16_t* stack = s.env_prefiltered +
+                              (int64_t)c.env * s.prefilter_levels * s.prefilter_height * s.prefilter_width * 4;
+      V3 blurred = sample_prefiltered(stack, s.prefilter_levels, s.prefilter_height, s.prefilter_width, dominant,
+                                      c.env_yaw, lb.pr);
+      float t = lb.pr * ((float)s.prefilter_levels - 1.0f);
+      V3 spec = blurred;
+      if (t < 1.0f) {
+        V3 sharp = sample_radiance(s.env_radiance[c.env], s.env_data, dominant, c.env_yaw, 0.0f);
+        spec = sharp * (1.0f - t) + blurred * t;
+      }
+      prefiltered = c.ambient + spec * c.env_scale;
+    }
+    float ao = sf.occlusion;
+    float spec_ao = clampf(powf(nov + ao, exp2f(-16.0f * lb.alpha - 1.0f)) - 1.0f + ao, 0.0f, 1.0f);
+    V3 radiance = cmul(irradiance, lb.diffuse_color) * ao + cmul(prefiltered, cmul(lb.spec_albedo, lb.energy_comp)) * spec_ao;
+    for (int32_t li = 0; li < c.L.nlight; ++li) {
+      Light light = load_light(c.blk + c.L.light_off + li * kLightFloats);
+      if (!light.active) continue;
+      radiance += shade_light(c, light, lb, point, normal, view, nov, seed, stream, c.L.nlight, li);
+    }
+    if (st.headlight_active) {
+      Light head;
+      head.type = MJPBR_LIGHT_DIRECTIONAL;
+      head.castshadow = false;
+      head.active = true;
+      head.dir = head_dir;
+      head.diffuse = V3{st.headlight_diffuse[0], st.headlight_diffuse[1], st.headlight_diffuse[2]};
+      head.specular = V3{st.headlight_specular[0], st.headlight_specular[1], st.headlight_specular[2]};
+      head.attenuation = V3{1.0f, 0.0f, 0.0f};
+      head.intensity = st.headlight_intensity / c.exposure;
+      head.range = 1.0f;
+      head.bulbradius = 0.0f;
+      head.cutoff = 0.0f;
+      head.exponent = 0.0f;
+      head.pos = v3(0.0f);
+      radiance += shade_light(c, head, lb, point, normal, view, nov, seed, stream, 1, 0);
+    }
+    return radiance + sf.emissive / c.exposure;
+  }
+
+  static MJ_DEV V3 background(RtCtx& c, V3 d, float spread) {
+    const MjpbrScene& s = *c.s;
+    if (kTex && s.settings.env_background) {
+      float lod = log2f(fmaxf(spread * s.settings.inv_texel_angle, kMinTexels));
+      return sample_radiance(s.env_radiance[c.env], s.env_data, d, c.env_yaw, lod) * c.env_scale;
+    }
+    return V3{s.settings.background[0], s.settings.background[1], s.settings.background[2]} / c.exposure;
+  }
+
+  static MJ_DEV float mirror_reflectance(RtCtx& c, int32_t slot) {
+    int32_t matid = __float_as_int(c.blk[c.L.geom_off + slot * kGeomFloats + 18]);
+    if (matid < 0 || !c.s->mat_reflectance.ptr) return 0.0f;
+    return bf(c.s->mat_reflectance, c.w, c.s->nmat, matid);
+  }
+
+  // One mirror bounce (render.py:242-274).
+  static MJ_DEV V3 shade_reflection(RtCtx& c, V3 point, V3 normal, V3 dir, float footprint, float spread, V3 head_dir,
+                                    uint32_t seed, int32_t stream) {
+    const MjpbrScene& s = *c.s;
+    V3 r = dir - normal * (2.0f * dot(dir, normal));
+    V3 origin = point + normal * kRayOffset;
+    Ray ray{origin, r};
+    Hit hit = closest_hit<kMesh>(s, c.blk, c.L, ray, kMaxVal, s.settings.cull_backfaces != 0, &c.err);
+    if (hit.geom == -1) return background(c, r, spread);
+    V3 p = origin + r * hit.dist;
+    V3 n;
+    Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, p, r, footprint + spread * hit.dist, &n);
+    return shade_surface(c, sf, p, n, -r, head_dir, seed, stream);
+  }
+
+  // Radiance along a camera ray, its first hit, and that surface's base colour and normal
+  // (render.py:276-341).
+  static MJ_DEV V3 trace_pixel(RtCtx& c, V3 origin, V3 dir, float max_dist, float footprint, float spread, V3 head_dir,
+                               uint32_t seed, int32_t stream, Hit* first, V3* albedo, V3* gnormal) {
+    const MjpbrScene& s = *c.s;
+    const MjpbrSettings& st = s.settings;
+    V3 radiance = v3(0.0f);
+    float throughput = 1.0f, travelled = 0.0f;
+    int32_t nlayer = st.has_transparency ? st.max_layers : 1;
+    for (int32_t layer = 0; layer < nlayer; ++layer) {
+      Ray ray{origin, dir};
+      Hit hit = closest_hit<kMesh>(s, c.blk, c.L, ray, max_dist - travelled, st.cull_backfaces != 0, &c.err);
+      if (layer == 0) *first = hit;
+      if (hit.geom == -1) {
+        radiance += background(c, dir, spread) * throughput;
+        break;
+      }
+      V3 point = origin + dir * hit.dist;
+      float cone = footprint + spread * (travelled + hit.dist);
+      V3 normal;
+      Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, point, dir, cone, &normal);
+      if (layer == 0) {
+        *albedo = sf.base_color;
+        *gnormal = normal;
+      }
+      V3 shaded = shade_surface(c, sf, point, normal, -dir, head_dir, seed, stream);
+      if (st.has_reflection) {
+        float mirror = mirror_reflectance(c, hit.slot);
+        if (mirror > 0.0f) {
+          V3 refl = shade_reflection(c, point, normal, dir, cone, spread, head_dir, seed, stream + 1);
+          shaded = shaded * (1.0f - mirror) + refl * mirror;
+        }
+      }
+      if (st.has_transparency) {
+        float opacity = clampf(sf.alpha, 0.0f, 1.0f);
+        radiance += shaded * (throughput * opacity);
+        throughput *= 1.0f - opacity;
+        if (throughput < kMinThroughput) break;
+        travelled += hit.dist;
+        origin = point + dir * kRayOffset;
+      } else {
+        radiance += shaded;
+        break;
+      }
+    }
+    return radiance;
+  }
+};
+
+MJ_DEV void write_geometry(const MjpbrScene& s, int32_t w, const Pixel& p, const Hit& hit, float dcam_z) {
+  if (s.render_seg[p.cam]) {
+    int32_t* o = s.seg_data + ((int64_t)w * s.seg_stride + s.seg_adr[p.cam] + p.pixelid) * 2;
+    int2 v = hit.geom != -1 ? make_int2(hit.geom, 5) : make_int2(-1, -1);  // mjOBJ_GEOM
+    *reinterpret_cast<int2*>(o) = v;
+  }
+  if (s.render_depth[p.cam]) {
+    s.depth_data[(int64_t)w * s.depth_stride + s.depth_adr[p.cam] + p.pixelid] =
+        hit.geom != -1 ? hit.dist * -dcam_z : 0.0f;
+  }
+}
+
+template <bool kMesh, bool kTex>
+__global__ void __launch_bounds__(kThreads) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+                                                      const __grid_constant__ TileMap tm) {
+  extern __shared__ __align__(16) float blk[];
+  const int32_t w = blockIdx.y;
+  // ---- stage the world block
+  {
+    const float4* src = reinterpret_cast<const float4*>(s.world_blocks + (int64_t)w * s.world_block_floats);
+    float4* dst = reinterpret_cast<float4*>(blk);
+    const int32_t n4 = s.world_block_floats >> 2;
+    for (int32_t i = threadIdx.x; i < n4; i += kThreads) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+
+  // ---- this thread's pixel
+  const int32_t tile = blockIdx.x;
+  int32_t cam = 0;
+  while (cam + 1 < tm.ncam && tile >= tm.tile_base[cam + 1]) ++cam;
+  const int32_t t = tile - tm.tile_base[cam];
+  const int32_t tx = t % tm.tiles_x[cam], ty = t / tm.tiles_x[cam];
+  Pixel p;
+  p.cam = cam;
+  p.width = s.cam_res[cam][0];
+  p.height = s.cam_res[cam][1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (s.settings.render_order == MJPBR_ORDER_ROW) {
+    p.px = tx * 32 + lane;
+    p.py = ty * 8 + warp;
+  } else {
+    p.px = tx * 16 + (warp & 1) * 8 + (lane & 7);
+    p.py = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
+  }
+  if (p.px >= p.width || p.py >= p.height) return;
+  p.pixelid = p.py * p.width + p.px;
+  p.rec = blk + L.cam_off + cam * kCamFloats;
+  const bool want_rgb = s.render_rgb[cam] != 0;
+  const MjpbrSettings& st = s.settings;
+
+  RtCtx c;
+  c.s = &s;
+  c.blk = blk;
+  c.L = L;
+  c.w = w;
+  c.err = 0;
+  c.exposure = bf(s.exposure, w, 1, 0);
+  c.ambient = bv3(s.ambient_radiance, w, 1, 0);
+  c.env = 0;
+  c.env_yaw = 0.0f;
+  c.env_scale = 0.0f;
+  if (kTex && s.nenv > 0) {
+    c.env = bi(s.env_id, w, 1, 0);
+    c.env_yaw = bf(s.env_yaw, w, 1, 0);
+    c.env_scale = bf(s.env_intensity, w, 1, 0);
+  }
+  const M3 R = cam_mat(p.rec);
+  const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
+  const bool cull = st.cull_backfaces != 0;
+
+  if (!want_rgb) {
+    V3 dcam, ocam;
+    camera_frame_ray(p, 1, 0, 0, &dcam, &ocam);
+    float max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
+    Ray ray{cpos + mul(R, ocam), mul(R, dcam)};
+    Hit hit = closest_hit<kMesh>(s, blk, L, ray, max_dist, cull, &c.err);
+    write_geometry(s, w, p, hit, dcam.z);
+    if (c.err && s.error_word) atomicOr(s.error_word, c.err);
+    return;
+  }
+
+  const int32_t n = st.samples_per_axis;
+  const float inv_n = 1.0f / (float)n;
+  float pixel_spread, pixel_width;
+  {
+    V3 d0, o0, d1, o1;
+    camera_frame_ray(p, 1, 0, 0, &d0, &o0);
+    camera_frame_ray(p, 1, 1, 0, &d1, &o1);
+    pixel_spread = length(d1 - d0);
+    pixel_width = length(o1 - o0);
+  }
+  const float spread = pixel_spread * inv_n, width = pixel_width * inv_n;
+  const V3 head_dir = -V3{R.m[2], R.m[5], R.m[8]};
+  const uint32_t pixel_seed = seed + (uint32_t)w * (uint32_t)s.total_rays + (uint32_t)(s.ray_adr[cam] + p.pixelid);
+
+  V3 display = v3(0.0f), hdr = v3(0.0f);
+  for (int32_t smp = 0; smp < n * n; ++smp) {
+    V3 dcam, ocam;
+    camera_frame_ray(p, n, smp % n, smp / n, &dcam, &ocam);
+    float max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
+    V3 origin = cpos + mul(R, ocam);
+    V3 dir = mul(R, dcam);
+    Hit first;
+    V3 albedo = v3(0.0f), gnormal = v3(0.0f);
+    V3 radiance = Rt<kMesh, kTex>::trace_pixel(c, origin, dir, max_dist, width, spread, head_dir, pixel_seed, 2 * smp,
+                                               &first, &albedo, &gnormal);
+    if (smp == 0) {
+      write_geometry(s, w, p, first, dcam.z);
+      if (st.render_guides && s.guide_albedo) {
+        int64_t a = ((int64_t)w * s.rgb_stride + s.rgb_adr[cam] + p.pixelid) * 3;
+        V3 al = first.geom != -1 ? albedo : v3(0.0f), nm = first.geom != -1 ? gnormal : v3(0.0f);
+        s.guide_albedo[a] = al.x;
+        s.guide_albedo[a + 1] = al.y;
+        s.guide_albedo[a + 2] = al.z;
+        s.guide_normal[a] = nm.x;
+        s.guide_normal[a + 1] = nm.y;
+        s.guide_normal[a + 2] = nm.z;
+      }
+    }
+    display += display_transform(radiance * c.exposure, st.tone_mapper);
+    hdr += radiance;
+  }
+  const int64_t adr = (int64_t)w * s.rgb_stride + s.rgb_adr[cam] + p.pixelid;
+  const float inv_nn = inv_n * inv_n;
+  if (st.render_hdr && s.hdr_data) {
+    s.hdr_data[adr * 3] = hdr.x * inv_nn;
+    s.hdr_data[adr * 3 + 1] = hdr.y * inv_nn;
+    s.hdr_data[adr * 3 + 2] = hdr.z * inv_nn;
+  }
+  s.rgb_data[adr] = encode_display(display * inv_nn);
+  if (c.err && s.error_word) atomicOr(s.error_word, c.err);
+}
+
+template <bool kMesh, bool kTex>
+int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaStream_t stream) {
+  size_t smem = (size_t)s.world_block_floats * sizeof(float);
+  auto kern = rt_kernel<kMesh, kTex>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render: world block of %zu bytes: %s", smem, cudaGetErrorString(e));
+  }
+  dim3 grid(tm.tile_base[tm.ncam], s.nworld);
+  kern<<<grid, kThreads, smem, stream>>>(s, seed, tm);
+  return check_launch("rt_kernel");
+}
+
+}  // namespace
+
+int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
+  TileMap tm;
+  tm.ncam = s.nrender;
+  if (s.settings.render_order == MJPBR_ORDER_ROW) {
+    tm.tile_w = 32;
+    tm.tile_h = 8;
+  } else {
+    tm.tile_w = 16;
+    tm.tile_h = 16;
+  }
+  tm.tile_base[0] = 0;
+  for (int32_t c = 0; c < s.nrender; ++c) {
+    int32_t W = s.cam_res[c][0], H = s.cam_res[c][1];
+    bool any = s.render_rgb[c] || s.render_depth[c] || s.render_seg[c];
+    tm.tiles_x[c] = (W + tm.tile_w - 1) / tm.tile_w;
+    int32_t ty = (H + tm.tile_h - 1) / tm.tile_h;
+    tm.tile_base[c + 1] = tm.tile_base[c] + (any ? tm.tiles_x[c] * ty : 0);
+  }
+  if (tm.tile_base[s.nrender] == 0 || s.nworld == 0) return MJPBR_OK;
+  bool mesh = s.nmesh > 0 && s.blas_root != nullptr;
+  bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
+  if (mesh && tex) return launch_variant<true, true>(s, seed, tm, stream);
+  if (mesh) return launch_variant<true, false>(s, seed, tm, stream);
+  if (tex) return launch_variant<false, true>(s, seed, tm, stream);
+  return launch_variant<false, false>(s, seed, tm, stream);
+}
+
+}  // namespace mjpbr

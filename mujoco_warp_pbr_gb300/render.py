@@ -1,0 +1,311 @@
+"""render / refit_bvh: the host side of one frame.
+
+`render(m, d, rc, seed)` mirrors mujoco_warp_pbr.render (mujoco_warp_pbr/_src/render.py:431-460);
+`refit_bvh(m, d, rc)` stands in for mujoco_warp.refit_bvh(m, d, rc.base), which reference users
+call after physics moved the geometry. Each builds (or reuses) the MjpbrScene descriptor and makes
+one libmjpbr call on the current torch stream, asynchronously: both can be captured into a CUDA
+graph. The descriptor is rebuilt only when an array of m, d or rc was replaced (identity check,
+like the reference's launch-input cache, mujoco_warp_pbr/_src/launch.py:89-115).
+"""
+
+from __future__ import annotations
+
+from typing import Any
+
+import numpy as np
+import torch
+
+from mujoco_warp_pbr_gb300 import _lib
+from mujoco_warp_pbr_gb300 import _scene
+from mujoco_warp_pbr_gb300.types import PbrRenderContext
+
+_MODEL_FIELDS = (
+  "geom_type",
+  "geom_dataid",
+  "geom_matid",
+  "geom_size",
+  "geom_rgba",
+  "mat_rgba",
+  "mat_emission",
+  "mat_texid",
+  "mat_texrepeat",
+  "mat_texuniform",
+  "light_type",
+  "light_castshadow",
+  "light_active",
+  "light_attenuation",
+  "light_cutoff",
+  "light_exponent",
+  "light_diffuse",
+  "light_specular",
+  "cam_projection",
+  "cam_fovy",
+  "cam_sensorsize",
+  "cam_intrinsic",
+  "mesh_vertadr",
+  "mesh_faceadr",
+  "mesh_normaladr",
+  "mesh_texcoordadr",
+  "mesh_vert",
+  "mesh_face",
+  "mesh_normal",
+  "mesh_facenormal",
+  "mesh_texcoord",
+  "mesh_facetexcoord",
+)
+_DATA_FIELDS = ("geom_xpos", "geom_xmat", "cam_xpos", "cam_xmat", "light_xpos", "light_xdir")
+_CONTEXT_TABLES = (
+  "geom_metallic",
+  "geom_roughness",
+  "geom_reflectance",
+  "mat_reflectance",
+  "light_intensity",
+  "light_range",
+  "light_bulbradius",
+  "exposure",
+  "ambient_radiance",
+  "env_id",
+  "env_intensity",
+  "env_yaw",
+)
+_INT_FIELDS = {
+  "geom_type",
+  "geom_dataid",
+  "geom_matid",
+  "mat_texid",
+  "mat_texuniform",
+  "light_type",
+  "light_castshadow",
+  "light_active",
+  "cam_projection",
+  "mesh_vertadr",
+  "mesh_faceadr",
+  "mesh_normaladr",
+  "mesh_texcoordadr",
+  "mesh_face",
+  "mesh_facenormal",
+  "mesh_facetexcoord",
+  "env_id",
+}
+
+
+def as_tensor(value: Any, name: str, device: torch.device) -> torch.Tensor:
+  """A contiguous float32 / int32 tensor on `device` for a model, data or context array."""
+  dtype = torch.int32 if name in _INT_FIELDS else torch.float32
+  if isinstance(value, torch.Tensor):
+    t = value
+  elif hasattr(value, "__cuda_array_interface__"):
+    t = torch.as_tensor(value, device=device)
+  else:
+    t = torch.as_tensor(np.asarray(value))
+  if t.dtype == torch.bool:
+    t = t.to(torch.int32)
+  if t.dtype != dtype:
+    t = t.to(dtype)
+  if t.device != device:
+    t = t.to(device)
+  return t.contiguous()
+
+
+def _batched(t: torch.Tensor, inner: int) -> torch.Tensor:
+  """A batched table viewed as (nbatch, inner...) with nbatch its leading dimension."""
+  if t.dim() == 0:
+    return t.reshape(1)
+  return t
+
+
+def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
+  """MjpbrScene fields (tensors and ints) of a frame; the tensors must stay alive."""
+  dev = rc.device
+  f: dict[str, Any] = {}
+  for name in _MODEL_FIELDS:
+    v = getattr(m, name, None)
+    f[name] = None if v is None or (hasattr(v, "numel") and v.numel() == 0) else as_tensor(v, name, dev)
+  for name in _DATA_FIELDS:
+    v = getattr(d, name, None)
+    f[name] = None if v is None or (hasattr(v, "numel") and v.numel() == 0) else as_tensor(v, name, dev)
+  for name in _CONTEXT_TABLES:
+    f[name] = as_tensor(getattr(rc, name), name, dev)
+  # batched tables must carry their batch dimension first
+  for name in ("exposure", "env_id", "env_intensity", "env_yaw"):
+    f[name] = f[name].reshape(-1)
+  f["ambient_radiance"] = f["ambient_radiance"].reshape(-1, 3)
+  ngeom = int(f["geom_type"].shape[0])
+  nworld = int(d.nworld)
+  if nworld != rc.nworld:
+    raise ValueError(f"data has {nworld} worlds, the render context {rc.nworld}")
+  b = rc.base
+  st = dict(rc._host_cache["settings"])
+  st.update(
+    {
+      "render_order": int(rc.render_order),
+      "samples_per_axis": int(rc.samples_per_pixel),
+      "tone_mapper": int(rc.tone_mapper),
+      "render_hdr": int(bool(rc.render_hdr)),
+      "light_model": int(rc.light_model),
+      "use_shadows": int(bool(rc.use_shadows)),
+      "shadow_samples": int(rc.shadow_samples),
+      "has_reflection": int(bool(rc.has_reflection)),
+      "has_transparency": int(bool(rc.has_transparency)),
+      "max_layers": int(rc.max_layers),
+      "shadow_light_fraction": float(rc.shadow_light_fraction),
+      "has_env": int(bool(rc.has_env)),
+      "env_background": int(bool(rc.env_background)),
+      "tier": int(rc.tier),
+      "path_samples": int(rc.path_samples),
+      "max_depth": int(rc.max_depth),
+      "rr_depth": int(rc.rr_depth),
+      "denoise": int(bool(rc.denoise)),
+      "denoise_sigma_color": float(rc.denoise_sigma_color),
+      "denoise_sigma_normal": float(rc.denoise_sigma_normal),
+      "denoise_sigma_depth": float(rc.denoise_sigma_depth),
+      "denoise_sigma_albedo": float(rc.denoise_sigma_albedo),
+    }
+  )
+  env = rc.env
+  f.update(
+    {
+      "nworld": nworld,
+      "ngeom": ngeom,
+      "nmat": int(f["mat_rgba"].shape[1]) if f["mat_rgba"] is not None else 0,
+      "nlight": int(f["light_xpos"].shape[1]) if f["light_xpos"] is not None else 0,
+      "ncam": int(f["cam_projection"].shape[0]),
+      "nmesh": len(rc.mesh_nface),
+      "ntex": len(rc.tex_desc),
+      "nenv": env.nenv if env is not None else 0,
+      "nrender": b.nrender,
+      "total_rays": b.total_rays,
+      "cam_id_map": b.cam_id_map,
+      "cam_res": b.cam_res,
+      "render_rgb": [int(v) for v in b.render_rgb],
+      "render_depth": [int(v) for v in b.render_depth],
+      "render_seg": [int(v) for v in b.render_seg],
+      "ray_adr": b.ray_adr,
+      "rgb_adr": b.rgb_adr,
+      "depth_adr": b.depth_adr,
+      "seg_adr": b.seg_adr,
+      "rgb_stride": int(b.rgb_data.shape[1]),
+      "depth_stride": int(b.depth_data.shape[1]),
+      "seg_stride": int(b.seg_data.shape[1]),
+      "rgb_data": b.rgb_data,
+      "depth_data": b.depth_data,
+      "seg_data": b.seg_data,
+      "hdr_data": rc.hdr_data if (rc.render_hdr or rc.denoise) else None,
+      "guide_albedo": rc.guide_albedo if rc.render_guides else None,
+      "guide_normal": rc.guide_normal if rc.render_guides else None,
+      "nbvh_geom": int(rc.enabled_geom_ids.shape[0]),
+      "nnode": int(rc.tlas_child.shape[1]),
+      "enabled_geom_ids": rc.enabled_geom_ids,
+      "tlas_child": rc.tlas_child,
+      "mesh_bounds": rc.mesh_bounds,
+      "world_blocks": rc.world_blocks,
+      "world_block_floats": rc.world_block_floats,
+      "blas_nodes": rc.blas_nodes,
+      "blas_tris": rc.blas_tris,
+      "blas_root": rc.blas_root,
+      "blas_tri_base": rc.blas_tri_base,
+      "textures": rc.textures,
+      "tex_data": rc.tex_data,
+      "dfg_lut": rc.dfg_lut,
+      "dfg_size": rc.dfg_size,
+      "aov_albedo": rc.aov_albedo,
+      "aov_normal": rc.aov_normal,
+      "aov_depth": rc.aov_depth,
+      "aov_emission": rc.aov_emission,
+      "aov_variance": rc.aov_variance,
+      "denoise_buffers": rc.denoise_buffers,
+      "denoise_iterations": int(rc.denoise_iterations),
+      "error_word": rc.error_word,
+      "settings": st,
+    }
+  )
+  if env is not None:
+    f.update(
+      {
+        "prefilter_levels": env.levels,
+        "prefilter_height": env.height,
+        "prefilter_width": env.width,
+        "env_prefiltered": env.prefiltered,
+        "env_radiance": env.radiance_desc,
+        "env_data": env.radiance_data,
+        "env_sh": env.sh,
+        "cdf_height": int(env.prob.shape[1]),
+        "cdf_width": int(env.prob.shape[2]),
+        "env_prob": env.prob,
+        "env_marginal": env.marginal,
+        "env_conditional": env.conditional,
+      }
+    )
+  if rc.ray_direction is not None:
+    f["ray_origin"] = rc.ray_origin
+    f["ray_direction"] = rc.ray_direction
+    f["bundle_res"] = rc.ray_res
+  return f
+
+
+def _sources(m: Any, d: Any, rc: PbrRenderContext) -> tuple:
+  public = [v for k, v in vars(rc).items() if not k.startswith("_")]
+  return (*vars(m).values(), *vars(d).values(), *public, *vars(rc.base).values())
+
+
+def scene(m: Any, d: Any, rc: PbrRenderContext) -> _lib.Scene:
+  """The (cached) MjpbrScene of a frame."""
+  sources = _sources(m, d, rc)
+  ids = tuple(map(id, sources))
+  cached = rc._host_cache.get("scene")
+  if cached is not None and cached[1] == ids:
+    return cached[2]
+  _check_env_id(rc)
+  fields = scene_fields(m, d, rc)
+  struct = _scene.fill_scene(fields)
+  # the cache holds the sources and the converted tensors so their addresses stay valid
+  rc._host_cache["scene"] = (sources, ids, struct, fields)
+  return struct
+
+
+def _check_env_id(rc: PbrRenderContext) -> None:
+  """ValueError if a replaced env_id selects a missing map (checked once per array, not while
+  capturing a graph; mujoco_warp_pbr/_src/kernel_inputs.py:480-490)."""
+  env_id = rc.env_id
+  if rc._host_cache.get("env_id") is env_id or torch.cuda.is_current_stream_capturing():
+    return
+  nenv = rc.env.nenv if rc.env is not None else 1
+  ids = env_id.detach().cpu().numpy()
+  if ids.size and (ids.min() < 0 or ids.max() >= nenv):
+    raise ValueError(f"env_id must be in [0, {nenv}) (one per environment map), got values in [{ids.min()}, {ids.max()}]")
+  rc._host_cache["env_id"] = env_id
+
+
+def _stream(rc: PbrRenderContext) -> int:
+  return torch.cuda.current_stream(rc.device).cuda_stream
+
+
+def refit_bvh(m: Any, d: Any, rc: PbrRenderContext) -> None:
+  """Refits every world's scene BVH to the current geom poses and packs the per-world blocks the
+  render kernels read (one kernel). Call after the geometry, cameras or lights moved."""
+  _lib.call("mjpbr_refit_bvh", scene(m, d, rc), _stream(rc))
+  rc._host_cache["refit"] = True
+
+
+def render(m: Any, d: Any, rc: PbrRenderContext, seed: int = 0) -> None:
+  """Renders the current frame into the context's output buffers (one kernel for the real-time
+  tier). The image is a deterministic function of the seed. The per-world blocks come from the
+  last refit_bvh; the first render of a context refits once itself."""
+  s = scene(m, d, rc)
+  stream = _stream(rc)
+  if not rc._host_cache.get("refit"):
+    _lib.call("mjpbr_refit_bvh", s, stream)
+    rc._host_cache["refit"] = True
+  _lib.call("mjpbr_render", s, int(seed) & 0xFFFFFFFF, stream)
+  if rc.tier == 1 and rc.denoise:
+    _lib.call("mjpbr_denoise_atrous", s, stream)
+
+
+def check_errors(rc: PbrRenderContext) -> int:
+  """Synchronises and returns (then clears) the error bits kernels reported (0: none).
+
+  Bit 1: a traversal stack overflowed. Bit 2: the work queue was inconsistent. Bit 4: a bounded
+  wait gave up."""
+  value = int(rc.error_word.item())
+  rc.error_word.zero_()
+  return value
