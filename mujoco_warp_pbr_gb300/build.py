@@ -60,7 +60,9 @@ def _stale(obj: Path, src: Path, newest_header: float) -> bool:
 
 
 def _compile(nvcc: str, src: Path, obj: Path, verbose_ptxas: bool) -> tuple[Path, str]:
-  cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+  # MJPBR_NVCC_DEFINES: extra -D options (tuning builds, e.g. "MJPBR_RT_MIN_BLOCKS=3")
+  defines = [f"-D{d}" for d in os.environ.get("MJPBR_NVCC_DEFINES", "").split()]
+  cmd = [nvcc, *ARCH, *NVCC_FLAGS, *defines, "-c", str(src), "-o", str(obj)]
   if verbose_ptxas and src.suffix == ".cu":
     cmd += ["-Xptxas", "-v"]
   proc = subprocess.run(cmd, capture_output=True, text=True)

@@ -17,6 +17,10 @@ namespace mjpbr {
 namespace {
 
 constexpr int kThreads = 256;
+// Resident CTAs per SM the register allocation targets (the register / occupancy trade-off).
+#ifndef MJPBR_RT_MIN_BLOCKS
+#define MJPBR_RT_MIN_BLOCKS 2
+#endif
 constexpr float kMinThroughput = 1.0f / 255.0f;
 constexpr float kMinTexels = 1.0e-8f;
 constexpr float kMinForward = 1.0e-6f;
@@ -93,7 +97,7 @@ struct Rt {
   }
 
   // Fraction of the light reaching the point (render.py:81-127).
-  static MJ_DEV float light_visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist,
+  static __device__ __noinline__ float light_visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist,
                                        uint32_t seed, int32_t stream, int32_t nlight, int32_t li) {
     const MjpbrSettings& st = c.s->settings;
     V3 origin = point + normal * kRayOffset;
@@ -140,7 +144,7 @@ struct Rt {
   }
 
   // Outgoing radiance towards view, before exposure (render.py:184-239).
-  static MJ_DEV V3 shade_surface(RtCtx& c, const Surface& sf, V3 point, V3 normal, V3 view, V3 head_dir, uint32_t seed,
+  static __device__ __noinline__ V3 shade_surface(RtCtx& c, const Surface& sf, V3 point, V3 normal, V3 view, V3 head_dir, uint32_t seed,
                                  int32_t stream) {
     const MjpbrScene& s = *c.s;
     const MjpbrSettings& st = s.settings;
@@ -207,65 +211,86 @@ struct Rt {
     return bf(c.s->mat_reflectance, c.w, c.s->nmat, matid);
   }
 
-  // One mirror bounce (render.py:242-274).
-  static MJ_DEV V3 shade_reflection(RtCtx& c, V3 point, V3 normal, V3 dir, float footprint, float spread, V3 head_dir,
-                                    uint32_t seed, int32_t stream) {
-    const MjpbrScene& s = *c.s;
-    V3 r = dir - normal * (2.0f * dot(dir, normal));
-    V3 origin = point + normal * kRayOffset;
-    Ray ray{origin, r};
-    Hit hit = closest_hit<kMesh>(s, c.blk, c.L, ray, kMaxVal, s.settings.cull_backfaces != 0, &c.err);
-    if (hit.geom == -1) return background(c, r, spread);
-    V3 p = origin + r * hit.dist;
-    V3 n;
-    Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, p, r, footprint + spread * hit.dist, &n);
-    return shade_surface(c, sf, p, n, -r, head_dir, seed, stream);
-  }
-
   // Radiance along a camera ray, its first hit, and that surface's base colour and normal
-  // (render.py:276-341).
+  // (render.py:242-341). Translucent layers and the one-bounce mirror ray of each layer are
+  // segments of a single loop, so the closest-hit / surface / shading code exists once in the
+  // kernel: layer i adds shaded_i (1 - m_i) w_i and schedules its mirror segment with weight
+  // m_i w_i (w_i = throughput_i * opacity_i), whose surface is shaded without further mirrors.
   static MJ_DEV V3 trace_pixel(RtCtx& c, V3 origin, V3 dir, float max_dist, float footprint, float spread, V3 head_dir,
                                uint32_t seed, int32_t stream, Hit* first, V3* albedo, V3* gnormal) {
     const MjpbrScene& s = *c.s;
     const MjpbrSettings& st = s.settings;
+    const bool cull = st.cull_backfaces != 0;
+    const int32_t nlayer = st.has_transparency ? st.max_layers : 1;
     V3 radiance = v3(0.0f);
     float throughput = 1.0f, travelled = 0.0f;
-    int32_t nlayer = st.has_transparency ? st.max_layers : 1;
-    for (int32_t layer = 0; layer < nlayer; ++layer) {
-      Ray ray{origin, dir};
-      Hit hit = closest_hit<kMesh>(s, c.blk, c.L, ray, max_dist - travelled, st.cull_backfaces != 0, &c.err);
-      if (layer == 0) *first = hit;
+    int32_t layer = 0;
+    // primary continuation (next translucent layer)
+    V3 po = origin;
+    bool have_primary = true;
+    // current segment
+    V3 so = origin, sd = dir;
+    float smax = max_dist, sweight = 1.0f, sfoot = footprint;
+    bool mirror_seg = false;
+#pragma unroll 1
+    for (int32_t iter = 0; iter < 2 * nlayer; ++iter) {
+      Ray ray{so, sd};
+      Hit hit = closest_hit<kMesh>(s, c.blk, c.L, ray, smax, cull, &c.err);
+      if (!mirror_seg && layer == 0) *first = hit;
+      bool cont = false;
       if (hit.geom == -1) {
-        radiance += background(c, dir, spread) * throughput;
-        break;
-      }
-      V3 point = origin + dir * hit.dist;
-      float cone = footprint + spread * (travelled + hit.dist);
-      V3 normal;
-      Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, point, dir, cone, &normal);
-      if (layer == 0) {
-        *albedo = sf.base_color;
-        *gnormal = normal;
-      }
-      V3 shaded = shade_surface(c, sf, point, normal, -dir, head_dir, seed, stream);
-      if (st.has_reflection) {
-        float mirror = mirror_reflectance(c, hit.slot);
-        if (mirror > 0.0f) {
-          V3 refl = shade_reflection(c, point, normal, dir, cone, spread, head_dir, seed, stream + 1);
-          shaded = shaded * (1.0f - mirror) + refl * mirror;
+        radiance += background(c, sd, spread) * (mirror_seg ? sweight : throughput);
+        if (mirror_seg) cont = have_primary;
+      } else {
+        V3 point = so + sd * hit.dist;
+        float cone = mirror_seg ? sfoot + spread * hit.dist : footprint + spread * (travelled + hit.dist);
+        V3 normal;
+        Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, point, sd, cone, &normal);
+        if (!mirror_seg && layer == 0) {
+          *albedo = sf.base_color;
+          *gnormal = normal;
+        }
+        V3 shaded = shade_surface(c, sf, point, normal, -sd, head_dir, seed, mirror_seg ? stream + 1 : stream);
+        if (mirror_seg) {
+          radiance += shaded * sweight;
+          cont = have_primary;
+        } else {
+          float mirror = st.has_reflection ? mirror_reflectance(c, hit.slot) : 0.0f;
+          float opacity = st.has_transparency ? clampf(sf.alpha, 0.0f, 1.0f) : 1.0f;
+          float w = throughput * opacity;
+          radiance += shaded * ((1.0f - mirror) * w);
+          have_primary = false;
+          if (st.has_transparency) {
+            throughput *= 1.0f - opacity;
+            if (throughput >= kMinThroughput && layer + 1 < nlayer) {
+              travelled += hit.dist;
+              po = point + sd * kRayOffset;
+              have_primary = true;
+            }
+          }
+          if (mirror > 0.0f) {
+            // the mirror segment of this layer, then the next layer (if any)
+            V3 r = sd - normal * (2.0f * dot(sd, normal));
+            so = point + normal * kRayOffset;
+            sd = r;
+            smax = kMaxVal;
+            sweight = mirror * w;
+            sfoot = cone;
+            mirror_seg = true;
+            if (have_primary) ++layer;
+            continue;
+          }
+          if (have_primary) ++layer;
+          cont = have_primary;
         }
       }
-      if (st.has_transparency) {
-        float opacity = clampf(sf.alpha, 0.0f, 1.0f);
-        radiance += shaded * (throughput * opacity);
-        throughput *= 1.0f - opacity;
-        if (throughput < kMinThroughput) break;
-        travelled += hit.dist;
-        origin = point + dir * kRayOffset;
-      } else {
-        radiance += shaded;
-        break;
-      }
+      if (!cont) break;
+      // next primary layer
+      so = po;
+      sd = dir;
+      smax = max_dist - travelled;
+      mirror_seg = false;
+      have_primary = true;
     }
     return radiance;
   }
@@ -284,7 +309,7 @@ MJ_DEV void write_geometry(const MjpbrScene& s, int32_t w, const Pixel& p, const
 }
 
 template <bool kMesh, bool kTex>
-__global__ void __launch_bounds__(kThreads) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+__global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                       const __grid_constant__ TileMap tm) {
   extern __shared__ __align__(16) float blk[];
   const int32_t w = blockIdx.y;

@@ -282,7 +282,7 @@ MJ_DEV float4 sample_level(const MjpbrTexture& t, const uint8_t* data, int level
 }
 
 // Trilinear sample at level of detail lod (clamped to the chain).
-MJ_DEV float4 sample_trilinear(const MjpbrTexture& t, const uint8_t* data, float u, float v, float lod, bool wrap_u,
+static __device__ __noinline__ float4 sample_trilinear(const MjpbrTexture& t, const uint8_t* data, float u, float v, float lod, bool wrap_u,
                                bool wrap_v) {
   float l = clampf(lod, 0.0f, (float)(t.nlevel - 1));
   float l0f = floorf(l);
@@ -349,7 +349,7 @@ MJ_DEV float4 stack_texel(const uint16_t* stack, int w, int h, int level, int x,
 
 // Trilinear lookup of the prefiltered stack (u WRAP, v CLAMP, roughness axis CLAMP), a 3D texture
 // sampled at w = (pr (levels - 1) + 0.5) / levels.
-MJ_DEV V3 sample_prefiltered(const uint16_t* stack, int levels, int h, int w, V3 d, float yaw, float pr) {
+static __device__ __noinline__ V3 sample_prefiltered(const uint16_t* stack, int levels, int h, int w, V3 d, float yaw, float pr) {
   float u, v;
   direction_to_uv(d, yaw, &u, &v);
   float wz = (clampf(pr, 0.0f, 1.0f) * ((float)levels - 1.0f) + 0.5f) / (float)levels;

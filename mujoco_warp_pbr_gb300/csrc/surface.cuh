@@ -162,7 +162,7 @@ MJ_DEV float4 fetch_role(const MjpbrScene& s, int32_t tex_id, const TexFrame& f,
 
 // Surface and viewer-facing shading normal (world frame) at a hit (material.py:301-503).
 template <bool kMesh, bool kTex>
-MJ_DEV Surface eval_surface(const MjpbrScene& s, const float* blk, const BlockLayout& L, int32_t w, const Hit& hit,
+__device__ __noinline__ Surface eval_surface(const MjpbrScene& s, const float* blk, const BlockLayout& L, int32_t w, const Hit& hit,
                             int32_t slot, V3 point, V3 dir, float footprint, V3* shading_world) {
   Surface sf;
   sf.occlusion = 1.0f;

@@ -34,7 +34,7 @@ MJ_DEV float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*
 // Closest (or, with kAny, any) triangle of mesh `mesh` hit by the local ray in [0, tmax).
 // Returns the distance or -1; on a closest hit fills the local geometric normal and barycentrics.
 template <bool kAny>
-MJ_DEV float mesh_query(const MjpbrScene& sc, int32_t mesh, V3 lo, V3 ld, float tmax, bool cull, V3* n_local,
+__device__ __noinline__ float mesh_query(const MjpbrScene& sc, int32_t mesh, V3 lo, V3 ld, float tmax, bool cull, V3* n_local,
                         float* bu, float* bv, int32_t* face, int32_t* err) {
   const float* nodes = sc.blas_nodes + (int64_t)sc.blas_root[mesh] * kNodeFloats;
   const float* tris = sc.blas_tris + (int64_t)sc.blas_tri_base[mesh] * kTriFloats;
@@ -161,7 +161,7 @@ MJ_DEV float intersect_geom(const MjpbrScene& sc, const float* g, const Ray& r, 
 
 // Closest hit within max_dist (the reference's trace_closest).
 template <bool kMesh>
-MJ_DEV Hit closest_hit(const MjpbrScene& sc, const float* blk, const BlockLayout& L, const Ray& r, float max_dist,
+__device__ __noinline__ Hit closest_hit(const MjpbrScene& sc, const float* blk, const BlockLayout& L, const Ray& r, float max_dist,
                        bool cull, int32_t* err) {
   Hit h;
   h.geom = -1;
@@ -246,7 +246,7 @@ MJ_DEV Hit closest_hit(const MjpbrScene& sc, const float* blk, const BlockLayout
 
 // True if anything is hit before max_dist (the reference's trace_any).
 template <bool kMesh>
-MJ_DEV bool any_hit(const MjpbrScene& sc, const float* blk, const BlockLayout& L, const Ray& r, float max_dist,
+__device__ __noinline__ bool any_hit(const MjpbrScene& sc, const float* blk, const BlockLayout& L, const Ray& r, float max_dist,
                     bool cull, int32_t* err) {
   RayInv ri = make_inv(r);
   int32_t st_code[kTlasStack];
