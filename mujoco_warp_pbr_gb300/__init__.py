@@ -7,8 +7,8 @@ package is the host side. There is no CPU fallback: without the built library, r
 """
 
 from mujoco_warp_pbr_gb300.envmap import load_hdr as load_hdr
-from mujoco_warp_pbr_gb300.io import create_render_context as create_render_context
-from mujoco_warp_pbr_gb300.io import resolve_geom_materials as resolve_geom_materials
+from mujoco_warp_pbr_gb300.context import create_render_context as create_render_context
+from mujoco_warp_pbr_gb300.context import resolve_geom_materials as resolve_geom_materials
 from mujoco_warp_pbr_gb300.model import Data as Data
 from mujoco_warp_pbr_gb300.model import HostData as HostData
 from mujoco_warp_pbr_gb300.model import HostModel as HostModel
@@ -25,12 +25,12 @@ from mujoco_warp_pbr_gb300.render import check_errors as check_errors
 from mujoco_warp_pbr_gb300.render import refit_bvh as refit_bvh
 from mujoco_warp_pbr_gb300.render import render as render
 from mujoco_warp_pbr_gb300.render import scene as scene_descriptor
-from mujoco_warp_pbr_gb300.types import LightModel as LightModel
-from mujoco_warp_pbr_gb300.types import PbrRenderContext as PbrRenderContext
-from mujoco_warp_pbr_gb300.types import RenderOrder as RenderOrder
-from mujoco_warp_pbr_gb300.types import Tier as Tier
-from mujoco_warp_pbr_gb300.types import ToneMapper as ToneMapper
-from mujoco_warp_pbr_gb300.types import UnsetMaterial as UnsetMaterial
+from mujoco_warp_pbr_gb300.pbr_types import LightModel as LightModel
+from mujoco_warp_pbr_gb300.pbr_types import PbrRenderContext as PbrRenderContext
+from mujoco_warp_pbr_gb300.pbr_types import RenderOrder as RenderOrder
+from mujoco_warp_pbr_gb300.pbr_types import Tier as Tier
+from mujoco_warp_pbr_gb300.pbr_types import ToneMapper as ToneMapper
+from mujoco_warp_pbr_gb300.pbr_types import UnsetMaterial as UnsetMaterial
 
 __all__ = [
   "Data",

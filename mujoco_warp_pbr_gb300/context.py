@@ -22,13 +22,13 @@ import torch
 
 from mujoco_warp_pbr_gb300 import _lib
 from mujoco_warp_pbr_gb300 import envmap as envmap_lib
-from mujoco_warp_pbr_gb300.types import LightModel
-from mujoco_warp_pbr_gb300.types import Outputs
-from mujoco_warp_pbr_gb300.types import PbrRenderContext
-from mujoco_warp_pbr_gb300.types import RenderOrder
-from mujoco_warp_pbr_gb300.types import Tier
-from mujoco_warp_pbr_gb300.types import ToneMapper
-from mujoco_warp_pbr_gb300.types import UnsetMaterial
+from mujoco_warp_pbr_gb300.pbr_types import LightModel
+from mujoco_warp_pbr_gb300.pbr_types import Outputs
+from mujoco_warp_pbr_gb300.pbr_types import PbrRenderContext
+from mujoco_warp_pbr_gb300.pbr_types import RenderOrder
+from mujoco_warp_pbr_gb300.pbr_types import Tier
+from mujoco_warp_pbr_gb300.pbr_types import ToneMapper
+from mujoco_warp_pbr_gb300.pbr_types import UnsetMaterial
 
 # Filament's default camera: f/16, 1/125 s, ISO 100.
 DEFAULT_EV100 = 14.96578428466209

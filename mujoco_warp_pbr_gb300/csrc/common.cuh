@@ -78,6 +78,33 @@ MJ_DEV V3 fnormalize(V3 a) {
   return l2 > 0.0f ? a * rsqrtf(l2) : a;
 }
 
+// Compact shading-only math (colours tolerate ~1e-6 relative error): atan on [-1, 1] as x P(x^2)
+// with a degree-7 polynomial fitted by least squares on Chebyshev nodes (max error 1.7e-7 rad),
+// extended to atan2 by octant symmetry; acos(x) = atan2(sqrt((1 - x)(1 + x)), x); powers and
+// logarithms through the special-function unit.
+MJ_DEV float atan_unit(float x) {
+  float t = x * x;
+  float p = -0.004831168334931135f;
+  p = __fmaf_rn(p, t, 0.02475677989423275f);
+  p = __fmaf_rn(p, t, -0.06021912768483162f);
+  p = __fmaf_rn(p, t, 0.09967923909425735f);
+  p = __fmaf_rn(p, t, -0.14040139317512512f);
+  p = __fmaf_rn(p, t, 0.1997368186712265f);
+  p = __fmaf_rn(p, t, -0.33332303166389465f);
+  p = __fmaf_rn(p, t, 0.9999999403953552f);
+  return x * p;
+}
+MJ_DEV float fast_atan2(float y, float x) {
+  float ax = fabsf(x), ay = fabsf(y);
+  float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  float r = mx > 0.0f ? atan_unit(__fdividef(mn, mx)) : 0.0f;
+  if (ay > ax) r = 1.57079632679489662f - r;
+  if (x < 0.0f) r = 3.14159265358979324f - r;
+  return y < 0.0f ? -r : r;
+}
+MJ_DEV float fast_acos(float x) { return fast_atan2(sqrtf(fmaxf((1.0f - x) * (1.0f + x), 0.0f)), x); }
+MJ_DEV float fast_pow(float x, float y) { return x > 0.0f ? exp2f(y * __log2f(x)) : 0.0f; }
+
 // Row-major 3x3 matrix (MuJoCo xmat).
 struct M3 {
   float m[9];

@@ -87,17 +87,18 @@ struct RtCtx {
   int32_t env;
   float env_yaw, env_scale;
   int32_t err;
+  Stack st;
 };
 
 template <bool kMesh, bool kTex>
 struct Rt {
   static MJ_DEV bool occluded(RtCtx& c, V3 o, V3 d, float max_dist) {
     Ray r{o, d};
-    return any_hit<kMesh>(*c.s, c.blk, c.L, r, max_dist, c.s->settings.cull_backfaces != 0, &c.err);
+    return trace_ray<kMesh>(*c.s, c.st, c.blk, c.L, r, max_dist, c.s->settings.cull_backfaces != 0, true, &c.err).geom != -1;
   }
 
   // Fraction of the light reaching the point (render.py:81-127).
-  static __device__ __noinline__ float light_visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist,
+  static MJ_DEV float light_visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist,
                                        uint32_t seed, int32_t stream, int32_t nlight, int32_t li) {
     const MjpbrSettings& st = c.s->settings;
     V3 origin = point + normal * kRayOffset;
@@ -144,7 +145,7 @@ struct Rt {
   }
 
   // Outgoing radiance towards view, before exposure (render.py:184-239).
-  static __device__ __noinline__ V3 shade_surface(RtCtx& c, const Surface& sf, V3 point, V3 normal, V3 view, V3 head_dir, uint32_t seed,
+  static MJ_DEV V3 shade_surface(RtCtx& c, const Surface& sf, V3 point, V3 normal, V3 view, V3 head_dir, uint32_t seed,
                                  int32_t stream) {
     const MjpbrScene& s = *c.s;
     const MjpbrSettings& st = s.settings;
@@ -171,27 +172,34 @@ struct Rt {
     float ao = sf.occlusion;
     float spec_ao = clampf(powf(nov + ao, exp2f(-16.0f * lb.alpha - 1.0f)) - 1.0f + ao, 0.0f, 1.0f);
     V3 radiance = cmul(irradiance, lb.diffuse_color) * ao + cmul(prefiltered, cmul(lb.spec_albedo, lb.energy_comp)) * spec_ao;
-    for (int32_t li = 0; li < c.L.nlight; ++li) {
-      Light light = load_light(c.blk + c.L.light_off + li * kLightFloats);
-      if (!light.active) continue;
-      radiance += shade_light(c, light, lb, point, normal, view, nov, seed, stream, c.L.nlight, li);
-    }
-    if (st.headlight_active) {
-      Light head;
-      head.type = MJPBR_LIGHT_DIRECTIONAL;
-      head.castshadow = false;
-      head.active = true;
-      head.dir = head_dir;
-      head.diffuse = V3{st.headlight_diffuse[0], st.headlight_diffuse[1], st.headlight_diffuse[2]};
-      head.specular = V3{st.headlight_specular[0], st.headlight_specular[1], st.headlight_specular[2]};
-      head.attenuation = V3{1.0f, 0.0f, 0.0f};
-      head.intensity = st.headlight_intensity / c.exposure;
-      head.range = 1.0f;
-      head.bulbradius = 0.0f;
-      head.cutoff = 0.0f;
-      head.exponent = 0.0f;
-      head.pos = v3(0.0f);
-      radiance += shade_light(c, head, lb, point, normal, view, nov, seed, stream, 1, 0);
+    // MuJoCo lights, then the headlight (a directional light along the view, no shadow, its
+    // illuminance display-relative), through one shade_light call site.
+    const int32_t nl = c.L.nlight + (st.headlight_active ? 1 : 0);
+#pragma unroll 1
+    for (int32_t li = 0; li < nl; ++li) {
+      Light light;
+      int32_t count = c.L.nlight, index = li;
+      if (li < c.L.nlight) {
+        light = load_light(c.blk + c.L.light_off + li * kLightFloats);
+        if (!light.active) continue;
+      } else {
+        light.type = MJPBR_LIGHT_DIRECTIONAL;
+        light.castshadow = false;
+        light.active = true;
+        light.dir = head_dir;
+        light.diffuse = V3{st.headlight_diffuse[0], st.headlight_diffuse[1], st.headlight_diffuse[2]};
+        light.specular = V3{st.headlight_specular[0], st.headlight_specular[1], st.headlight_specular[2]};
+        light.attenuation = V3{1.0f, 0.0f, 0.0f};
+        light.intensity = st.headlight_intensity / c.exposure;
+        light.range = 1.0f;
+        light.bulbradius = 0.0f;
+        light.cutoff = 0.0f;
+        light.exponent = 0.0f;
+        light.pos = v3(0.0f);
+        count = 1;
+        index = 0;
+      }
+      radiance += shade_light(c, light, lb, point, normal, view, nov, seed, stream, count, index);
     }
     return radiance + sf.emissive / c.exposure;
   }
@@ -235,7 +243,7 @@ struct Rt {
 #pragma unroll 1
     for (int32_t iter = 0; iter < 2 * nlayer; ++iter) {
       Ray ray{so, sd};
-      Hit hit = closest_hit<kMesh>(s, c.blk, c.L, ray, smax, cull, &c.err);
+      Hit hit = trace_ray<kMesh>(s, c.st, c.blk, c.L, ray, smax, cull, false, &c.err);
       if (!mirror_seg && layer == 0) *first = hit;
       bool cont = false;
       if (hit.geom == -1) {
@@ -311,7 +319,8 @@ MJ_DEV void write_geometry(const MjpbrScene& s, int32_t w, const Pixel& p, const
 template <bool kMesh, bool kTex>
 __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                       const __grid_constant__ TileMap tm) {
-  extern __shared__ __align__(16) float blk[];
+  extern __shared__ __align__(16) float smem[];
+  float* blk = smem;
   const int32_t w = blockIdx.y;
   // ---- stage the world block
   {
@@ -350,6 +359,12 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   RtCtx c;
   c.s = &s;
   c.blk = blk;
+  {
+    int32_t* stack_base = reinterpret_cast<int32_t*>(smem + s.world_block_floats);
+    c.st.code = stack_base + threadIdx.x;
+    c.st.t = reinterpret_cast<float*>(stack_base + kThreads * kStackDepth) + threadIdx.x;
+    c.st.stride = kThreads;
+  }
   c.L = L;
   c.w = w;
   c.err = 0;
@@ -372,7 +387,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
     camera_frame_ray(p, 1, 0, 0, &dcam, &ocam);
     float max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
     Ray ray{cpos + mul(R, ocam), mul(R, dcam)};
-    Hit hit = closest_hit<kMesh>(s, blk, L, ray, max_dist, cull, &c.err);
+    Hit hit = trace_ray<kMesh>(s, c.st, blk, L, ray, max_dist, cull, false, &c.err);
     write_geometry(s, w, p, hit, dcam.z);
     if (c.err && s.error_word) atomicOr(s.error_word, c.err);
     return;
@@ -432,9 +447,9 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
 
 template <bool kMesh, bool kTex>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaStream_t stream) {
-  size_t smem = (size_t)s.world_block_floats * sizeof(float);
+  size_t smem = (size_t)s.world_block_floats * sizeof(float) + (size_t)kThreads * kStackDepth * 8;
   auto kern = rt_kernel<kMesh, kTex>;
-  if (smem > 48 * 1024) {
+  {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render: world block of %zu bytes: %s", smem, cudaGetErrorString(e));
   }

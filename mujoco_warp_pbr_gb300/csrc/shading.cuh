@@ -156,14 +156,14 @@ MJ_DEV void eval_light(const Light& light, int32_t light_model, V3 point, V3* l,
     if (light.type == MJPBR_LIGHT_SPOT) {
       float cos_theta = dot(-*l, light.dir);
       float outer = light.cutoff * (kPi / 180.0f);
-      float cos_outer = cosf(outer);
+      float cos_outer = __cosf(outer);
       if (physical) {
-        float cos_inner = cosf(outer * 0.75f);
+        float cos_inner = __cosf(outer * 0.75f);
         float cone_scale = 1.0f / fmaxf(cos_inner - cos_outer, 1.0f / 1024.0f);
         float s = clampf((cos_theta - cos_outer) * cone_scale, 0.0f, 1.0f);
         att = att * s * s;
       } else {
-        att = cos_theta < cos_outer ? 0.0f : att * powf(fmaxf(cos_theta, 0.0f), light.exponent);
+        att = cos_theta < cos_outer ? 0.0f : att * fast_pow(fmaxf(cos_theta, 0.0f), light.exponent);
       }
     }
   }
@@ -218,7 +218,7 @@ MJ_DEV V3 display_transform(V3 c, int32_t tone_mapper) {
   return vmin(vmax(c, v3(0.0f)), v3(1.0f));
 }
 
-MJ_DEV float srgb_oetf(float x) { return x <= 0.0031308f ? 12.92f * x : 1.055f * powf(x, 1.0f / 2.4f) - 0.055f; }
+MJ_DEV float srgb_oetf(float x) { return x <= 0.0031308f ? 12.92f * x : 1.055f * fast_pow(x, 1.0f / 2.4f) - 0.055f; }
 
 // Display-linear [0, 1] -> 8-bit sRGB RGBA packed with R in the low byte (round half up).
 MJ_DEV uint32_t encode_display(V3 c) {
@@ -297,21 +297,21 @@ static __device__ __noinline__ float4 sample_trilinear(const MjpbrTexture& t, co
 // Mip level of a ray-cone footprint (texture.py:225-228).
 MJ_DEV float texture_lod(float footprint, float uv_per_length, const MjpbrTexture& t) {
   float texels = footprint * uv_per_length * (float)max(t.width, t.height);
-  return log2f(fmaxf(texels, 1.0e-8f));
+  return __log2f(fmaxf(texels, 1.0e-8f));
 }
 
 // ---------------------------------------------------------------- environment
 
 // Equirect coordinates of a world direction (row 0 = +z, centre column = +x), yaw about +z.
 MJ_DEV void direction_to_uv(V3 d, float yaw, float* u, float* v) {
-  float phi = atan2f(d.y, d.x) - yaw;
+  float phi = fast_atan2(d.y, d.x) - yaw;
   float uu = 0.5f + phi * (0.5f / kPi);
   *u = uu - floorf(uu);
-  *v = acosf(clampf(d.z, -1.0f, 1.0f)) * (1.0f / kPi);
+  *v = fast_acos(clampf(d.z, -1.0f, 1.0f)) * (1.0f / kPi);
 }
 
 MJ_DEV V3 rotate_yaw(V3 d, float yaw) {
-  float c = cosf(yaw), s = sinf(yaw);
+  float c = __cosf(yaw), s = __sinf(yaw);
   return V3{c * d.x - s * d.y, s * d.x + c * d.y, d.z};
 }
 

@@ -55,8 +55,8 @@ MJ_DEV void primitive_uv(int32_t type, V3 p, V3 ln, V3 size, float rx, float ry,
     case MJPBR_GEOM_SPHERE:
     case MJPBR_GEOM_ELLIPSOID: {
       V3 q = type == MJPBR_GEOM_SPHERE ? p / size.x : V3{p.x / size.x, p.y / size.y, p.z / size.z};
-      *u = atan2f(q.y, q.x) * inv2pi + 0.5f;
-      *v = acosf(clampf(q.z / fmaxf(length(q), 1.0e-9f), -1.0f, 1.0f)) * (1.0f / kPi);
+      *u = fast_atan2(q.y, q.x) * inv2pi + 0.5f;
+      *v = fast_acos(clampf(q.z / fmaxf(length(q), 1.0e-9f), -1.0f, 1.0f)) * (1.0f / kPi);
       if (uniform) {
         *repx = rx * 2.0f * kPi * size.x;
         *repy = ry * kPi * size.x;
@@ -66,7 +66,7 @@ MJ_DEV void primitive_uv(int32_t type, V3 p, V3 ln, V3 size, float rx, float ry,
     case MJPBR_GEOM_CYLINDER:
     case MJPBR_GEOM_CAPSULE: {
       float h = size.y;
-      *u = atan2f(p.y, p.x) * inv2pi + 0.5f;
+      *u = fast_atan2(p.y, p.x) * inv2pi + 0.5f;
       *v = 0.5f - p.z / (2.0f * fmaxf(h + (type == MJPBR_GEOM_CAPSULE ? size.x : 0.0f), 1.0e-9f));
       if (uniform) {
         *repx = rx * 2.0f * kPi * size.x;

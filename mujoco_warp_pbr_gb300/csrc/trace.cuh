@@ -4,14 +4,25 @@
 // entry distances are stored with pushed children, a child whose entry is at or beyond the
 // current cut-off dist * (1 + tol) + tol_abs is skipped, ties within tol go to the higher geom id,
 // hits with a normal along the ray are culled when culling is on, alpha-0 geoms are skipped.
+//
+// Traversal stack: one per thread in shared memory, entry k of a thread at code[k * stride]
+// (consecutive threads in consecutive words: conflict-free), shared by the scene BVH and the mesh
+// BVH entered from one of its leaves (the mesh traversal pushes above the scene entries and pops
+// back to them). A push that would overflow sets kErrStackOverflow instead of writing.
 #pragma once
 
 #include "geometry.cuh"
 
 namespace mjpbr {
 
-constexpr int kTlasStack = 32;
-constexpr int kBlasStack = 40;
+// Stack entries per thread.
+constexpr int kStackDepth = 32;
+
+struct Stack {
+  int32_t* code;  // (ref << 3) | count, see world_block.cuh
+  float* t;       // entry distance of the pushed child
+  int32_t stride;
+};
 
 MJ_DEV GeomFrame geom_frame(const float* g) {
   GeomFrame f;
@@ -31,86 +42,75 @@ MJ_DEV GeomFrame geom_frame(const float* g) {
 
 MJ_DEV float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-// Closest (or, with kAny, any) triangle of mesh `mesh` hit by the local ray in [0, tmax).
-// Returns the distance or -1; on a closest hit fills the local geometric normal and barycentrics.
-template <bool kAny>
-__device__ __noinline__ float mesh_query(const MjpbrScene& sc, int32_t mesh, V3 lo, V3 ld, float tmax, bool cull, V3* n_local,
-                        float* bu, float* bv, int32_t* face, int32_t* err) {
+MJ_DEV void push(const Stack& st, int& sp, int32_t code, float t, int32_t* err) {
+  if (sp < kStackDepth) {
+    st.code[sp * st.stride] = code;
+    st.t[sp * st.stride] = t;
+    ++sp;
+  } else {
+    *err |= kErrStackOverflow;
+  }
+}
+
+// Tests both children of a node (child-bounds layout) and pushes the hit ones, far first.
+MJ_DEV void expand(const Stack& st, int& sp, const RayInv& ri, float4 alo, float4 ahi, float4 blo, float4 bhi, float cut,
+                   int32_t* err) {
+  const int32_t acnt = __float_as_int(ahi.w), bcnt = __float_as_int(bhi.w);
+  const float ta = acnt >= 0 ? box_entry(ri, alo.x, alo.y, alo.z, ahi.x, ahi.y, ahi.z, cut) : -1.0f;
+  const float tb = bcnt >= 0 ? box_entry(ri, blo.x, blo.y, blo.z, bhi.x, bhi.y, bhi.z, cut) : -1.0f;
+  const int32_t ca = (__float_as_int(alo.w) << 3) | acnt;
+  const int32_t cb = (__float_as_int(blo.w) << 3) | bcnt;
+  const bool swap = tb >= 0.0f && (ta < 0.0f || tb < ta);
+  const int32_t cn = swap ? cb : ca, cf = swap ? ca : cb;
+  const float tn = swap ? tb : ta, tf = swap ? ta : tb;
+  if (tf >= 0.0f) push(st, sp, cf, tf, err);
+  if (tn >= 0.0f) push(st, sp, cn, tn, err);
+}
+
+// Closest (or, with `any`, any) triangle of mesh `mesh` hit by the local ray in [0, tmax),
+// using stack entries above sp0. Returns the distance or -1; on a closest hit fills the local
+// geometric normal and the barycentrics of vertices 0 and 1. Any-hit queries do not cull.
+MJ_DEV float mesh_query(const MjpbrScene& sc, const Stack& st, int sp0, int32_t mesh, V3 lo, V3 ld, float tmax,
+                        bool cull, bool any, V3* n_local, float* bu, float* bv, int32_t* face, int32_t* err) {
   const float* nodes = sc.blas_nodes + (int64_t)sc.blas_root[mesh] * kNodeFloats;
   const float* tris = sc.blas_tris + (int64_t)sc.blas_tri_base[mesh] * kTriFloats;
-  WoopRay w = woop_setup(lo, ld);
-  Ray lr{lo, ld};
-  RayInv ri = make_inv(lr);
-  int32_t st_code[kBlasStack];
-  float st_t[kBlasStack];
-  int sp = 0;
+  const WoopRay w = woop_setup(lo, ld);
+  const RayInv ri = make_inv(Ray{lo, ld});
   float best = tmax;
   int32_t found = -1;
-  V3 e1b = v3(0.0f), e2b = v3(0.0f);
+  V3 nb = v3(0.0f);
   float ub = 0.0f, vb = 0.0f;
-  // start from the root node's children
-  st_code[0] = 0;  // node 0, count 0
-  st_t[0] = 0.0f;
-  sp = 1;
-  while (sp > 0) {
+  int sp = sp0;
+  push(st, sp, 0, 0.0f, err);  // the root node
+  while (sp > sp0) {
     --sp;
-    if (st_t[sp] >= best) continue;
-    int32_t code = st_code[sp];
-    int32_t ref = code >> 3, cnt = code & 7;
+    if (st.t[sp * st.stride] >= best) continue;
+    const int32_t code = st.code[sp * st.stride];
+    const int32_t ref = code >> 3, cnt = code & 7;
     if (cnt == 0) {
       const float* nd = nodes + (int64_t)ref * kNodeFloats;
-      float4 alo = ldg4(nd), ahi = ldg4(nd + 4), blo = ldg4(nd + 8), bhi = ldg4(nd + 12);
-      int32_t acnt = __float_as_int(ahi.w), bcnt = __float_as_int(bhi.w);
-      float ta = acnt >= 0 ? box_entry(ri, alo.x, alo.y, alo.z, ahi.x, ahi.y, ahi.z, best) : -1.0f;
-      float tb = bcnt >= 0 ? box_entry(ri, blo.x, blo.y, blo.z, bhi.x, bhi.y, bhi.z, best) : -1.0f;
-      int32_t ca = (__float_as_int(alo.w) << 3) | acnt;
-      int32_t cb = (__float_as_int(blo.w) << 3) | bcnt;
-      int32_t cn = ca, cf = cb;
-      float tn = ta, tf = tb;
-      if (tb >= 0.0f && (ta < 0.0f || tb < ta)) {
-        cn = cb;
-        cf = ca;
-        tn = tb;
-        tf = ta;
-      }
-      if (tf >= 0.0f) {
-        if (sp < kBlasStack) {
-          st_code[sp] = cf;
-          st_t[sp++] = tf;
-        } else {
-          *err |= kErrStackOverflow;
-        }
-      }
-      if (tn >= 0.0f) {
-        if (sp < kBlasStack) {
-          st_code[sp] = cn;
-          st_t[sp++] = tn;
-        } else {
-          *err |= kErrStackOverflow;
-        }
-      }
+      expand(st, sp, ri, ldg4(nd), ldg4(nd + 4), ldg4(nd + 8), ldg4(nd + 12), best, err);
       continue;
     }
     for (int32_t i = ref; i < ref + cnt; ++i) {
       const float* tr = tris + (int64_t)i * kTriFloats;
-      float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
-      V3 v0{a.x, a.y, a.z}, v1{b.x, b.y, b.z}, v2{c.x, c.y, c.z};
+      const float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
+      const V3 v0{a.x, a.y, a.z}, v1{b.x, b.y, b.z}, v2{c.x, c.y, c.z};
       float u, v;
-      float t = woop_hit(w, v0, v1, v2, best, &u, &v);
+      const float t = woop_hit(w, v0, v1, v2, best, &u, &v);
       if (t < 0.0f) continue;
-      V3 e1 = v1 - v0, e2 = v2 - v0;
-      if (!kAny && cull && dot(ld, cross(e1, e2)) > 0.0f) continue;
-      if (kAny) return t;
+      if (any) return t;
+      const V3 ng = cross(v1 - v0, v2 - v0);
+      if (cull && dot(ld, ng) > 0.0f) continue;
       best = t;
       found = __float_as_int(a.w);
-      e1b = e1;
-      e2b = e2;
+      nb = ng;
       ub = u;
       vb = v;
     }
   }
   if (found < 0) return -1.0f;
-  *n_local = normalize(cross(e1b, e2b));
+  *n_local = normalize(nb);
   *bu = ub;
   *bv = vb;
   *face = found;
@@ -118,11 +118,11 @@ __device__ __noinline__ float mesh_query(const MjpbrScene& sc, int32_t mesh, V3 
 }
 
 // One geom against the ray: distance (or -1), world normal, mesh hit details.
-template <bool kMesh, bool kAny>
-MJ_DEV float intersect_geom(const MjpbrScene& sc, const float* g, const Ray& r, float max_t, bool cull, V3* n,
-                            float* u, float* v, int32_t* face, int32_t* mesh, int32_t* err) {
-  int32_t type = __float_as_int(g[3]);
-  GeomFrame f = geom_frame(g);
+template <bool kMesh>
+MJ_DEV float intersect_geom(const MjpbrScene& sc, const Stack& st, int sp, const float* g, const Ray& r, float max_t,
+                            bool cull, bool any, V3* n, float* u, float* v, int32_t* face, int32_t* mesh, int32_t* err) {
+  const int32_t type = __float_as_int(g[3]);
+  const GeomFrame f = geom_frame(g);
   float d = -1.0f;
   switch (type) {
     case MJPBR_GEOM_PLANE:
@@ -145,12 +145,12 @@ MJ_DEV float intersect_geom(const MjpbrScene& sc, const float* g, const Ray& r, 
       break;
     default:
       if (kMesh && (type == MJPBR_GEOM_MESH || type == MJPBR_GEOM_SDF)) {
-        int32_t mid = __float_as_int(g[17]);
+        const int32_t mid = __float_as_int(g[17]);
         if (mid >= 0) {
           V3 lo, ld, nl = v3(0.0f);
           map_local(f, r, &lo, &ld);
-          d = mesh_query<kAny>(sc, mid, lo, ld, max_t, cull, &nl, u, v, face, err);
-          *n = kAny ? v3(0.0f) : mul(f.mat, nl);
+          d = mesh_query(sc, st, sp, mid, lo, ld, max_t, cull, any, &nl, u, v, face, err);
+          *n = any ? v3(0.0f) : mul(f.mat, nl);
           *mesh = mid;
         }
       }
@@ -159,10 +159,12 @@ MJ_DEV float intersect_geom(const MjpbrScene& sc, const float* g, const Ray& r, 
   return d;
 }
 
-// Closest hit within max_dist (the reference's trace_closest).
+// The ray query of the render kernels, one copy in the binary for every call site:
+//  * any = false: closest hit within max_dist (the reference's trace_closest);
+//  * any = true: the first hit found before max_dist (trace_any; hit.geom != -1 means occluded).
 template <bool kMesh>
-__device__ __noinline__ Hit closest_hit(const MjpbrScene& sc, const float* blk, const BlockLayout& L, const Ray& r, float max_dist,
-                       bool cull, int32_t* err) {
+__device__ __noinline__ Hit trace_ray(const MjpbrScene& sc, const Stack& st, const float* blk, const BlockLayout& L,
+                                      const Ray r, float max_dist, bool cull, bool any, int32_t* err) {
   Hit h;
   h.geom = -1;
   h.slot = -1;
@@ -172,49 +174,18 @@ __device__ __noinline__ Hit closest_hit(const MjpbrScene& sc, const float* blk, 
   h.v = 0.0f;
   h.face = -1;
   h.mesh = -1;
-  RayInv ri = make_inv(r);
-  int32_t st_code[kTlasStack];
-  float st_t[kTlasStack];
-  st_code[0] = 0;
-  st_t[0] = 0.0f;
-  int sp = 1;
+  const RayInv ri = make_inv(r);
+  int sp = 0;
+  push(st, sp, 0, 0.0f, err);
   while (sp > 0) {
     --sp;
     float cut = h.dist * (1.0f + kRayTolRel) + kRayTolAbs;
-    if (st_t[sp] >= cut) continue;
-    int32_t code = st_code[sp];
-    int32_t ref = code >> 3, cnt = code & 7;
+    if (st.t[sp * st.stride] >= cut) continue;
+    const int32_t code = st.code[sp * st.stride];
+    const int32_t ref = code >> 3, cnt = code & 7;
     if (cnt == 0) {
-      const float* nd = blk + L.node_off + ref * kNodeFloats;
-      int32_t acnt = __float_as_int(nd[7]), bcnt = __float_as_int(nd[15]);
-      float ta = acnt >= 0 ? box_entry(ri, nd[0], nd[1], nd[2], nd[4], nd[5], nd[6], cut) : -1.0f;
-      float tb = bcnt >= 0 ? box_entry(ri, nd[8], nd[9], nd[10], nd[12], nd[13], nd[14], cut) : -1.0f;
-      int32_t ca = (__float_as_int(nd[3]) << 3) | acnt;
-      int32_t cb = (__float_as_int(nd[11]) << 3) | bcnt;
-      int32_t cn = ca, cf = cb;
-      float tn = ta, tf = tb;
-      if (tb >= 0.0f && (ta < 0.0f || tb < ta)) {
-        cn = cb;
-        cf = ca;
-        tn = tb;
-        tf = ta;
-      }
-      if (tf >= 0.0f) {
-        if (sp < kTlasStack) {
-          st_code[sp] = cf;
-          st_t[sp++] = tf;
-        } else {
-          *err |= kErrStackOverflow;
-        }
-      }
-      if (tn >= 0.0f) {
-        if (sp < kTlasStack) {
-          st_code[sp] = cn;
-          st_t[sp++] = tn;
-        } else {
-          *err |= kErrStackOverflow;
-        }
-      }
+      const float4* nd = reinterpret_cast<const float4*>(blk + L.node_off + ref * kNodeFloats);
+      expand(st, sp, ri, nd[0], nd[1], nd[2], nd[3], cut, err);
       continue;
     }
     for (int32_t slot = ref; slot < ref + cnt; ++slot) {
@@ -224,11 +195,20 @@ __device__ __noinline__ Hit closest_hit(const MjpbrScene& sc, const float* blk, 
       V3 n = v3(0.0f);
       float u = 0.0f, v = 0.0f;
       int32_t face = -1, mesh = -1;
-      float d = intersect_geom<kMesh, false>(sc, g, r, cut, cull, &n, &u, &v, &face, &mesh, err);
+      float d = intersect_geom<kMesh>(sc, st, sp, g, r, any ? max_dist : cut, cull, any, &n, &u, &v, &face, &mesh, err);
       if (cull && d >= 0.0f && dot(r.d, n) > 0.0f) d = -1.0f;
-      int32_t gi = __float_as_int(g[16]);
-      float tol = kRayTolRel * fmaxf(h.dist, 1.0f);
-      bool closer = (d < h.dist - tol) || (fabsf(d - h.dist) <= tol && (h.geom < 0 || gi > h.geom));
+      const int32_t gi = __float_as_int(g[16]);
+      if (any) {
+        if (d >= 0.0f && d < max_dist) {
+          h.geom = gi;
+          h.slot = slot;
+          h.dist = d;
+          return h;
+        }
+        continue;
+      }
+      const float tol = kRayTolRel * fmaxf(h.dist, 1.0f);
+      const bool closer = (d < h.dist - tol) || (fabsf(d - h.dist) <= tol && (h.geom < 0 || gi > h.geom));
       if (d >= 0.0f && closer) {
         h.dist = d;
         h.normal = n;
@@ -242,63 +222,6 @@ __device__ __noinline__ Hit closest_hit(const MjpbrScene& sc, const float* blk, 
     }
   }
   return h;
-}
-
-// True if anything is hit before max_dist (the reference's trace_any).
-template <bool kMesh>
-__device__ __noinline__ bool any_hit(const MjpbrScene& sc, const float* blk, const BlockLayout& L, const Ray& r, float max_dist,
-                    bool cull, int32_t* err) {
-  RayInv ri = make_inv(r);
-  int32_t st_code[kTlasStack];
-  int sp = 1;
-  st_code[0] = 0;
-  while (sp > 0) {
-    --sp;
-    int32_t code = st_code[sp];
-    int32_t ref = code >> 3, cnt = code & 7;
-    if (cnt == 0) {
-      const float* nd = blk + L.node_off + ref * kNodeFloats;
-      int32_t acnt = __float_as_int(nd[7]), bcnt = __float_as_int(nd[15]);
-      float ta = acnt >= 0 ? box_entry(ri, nd[0], nd[1], nd[2], nd[4], nd[5], nd[6], max_dist) : -1.0f;
-      float tb = bcnt >= 0 ? box_entry(ri, nd[8], nd[9], nd[10], nd[12], nd[13], nd[14], max_dist) : -1.0f;
-      int32_t ca = (__float_as_int(nd[3]) << 3) | acnt;
-      int32_t cb = (__float_as_int(nd[11]) << 3) | bcnt;
-      int32_t cn = ca, cf = cb;
-      float tn = ta, tf = tb;
-      if (tb >= 0.0f && (ta < 0.0f || tb < ta)) {
-        cn = cb;
-        cf = ca;
-        tn = tb;
-        tf = ta;
-      }
-      if (tf >= 0.0f) {
-        if (sp < kTlasStack) {
-          st_code[sp++] = cf;
-        } else {
-          *err |= kErrStackOverflow;
-        }
-      }
-      if (tn >= 0.0f) {
-        if (sp < kTlasStack) {
-          st_code[sp++] = cn;
-        } else {
-          *err |= kErrStackOverflow;
-        }
-      }
-      continue;
-    }
-    for (int32_t slot = ref; slot < ref + cnt; ++slot) {
-      const float* g = blk + L.geom_off + slot * kGeomFloats;
-      if (__float_as_int(g[19]) & kGeomFlagSkip) continue;
-      V3 n = v3(0.0f);
-      float u = 0.0f, v = 0.0f;
-      int32_t face = -1, mesh = -1;
-      float d = intersect_geom<kMesh, true>(sc, g, r, max_dist, cull, &n, &u, &v, &face, &mesh, err);
-      if (cull && d >= 0.0f && dot(r.d, n) > 0.0f) d = -1.0f;
-      if (d >= 0.0f && d < max_dist) return true;
-    }
-  }
-  return false;
 }
 
 }  // namespace mjpbr

@@ -244,9 +244,9 @@ class DeviceEnvironments:
 
 
 def upload_environments(env: HostEnvironments, device: torch.device) -> DeviceEnvironments:
-  from mujoco_warp_pbr_gb300.io import TEX_RGBA16F
-  from mujoco_warp_pbr_gb300.io import pack_textures
-  from mujoco_warp_pbr_gb300.io import upload_textures
+  from mujoco_warp_pbr_gb300.context import TEX_RGBA16F
+  from mujoco_warp_pbr_gb300.context import pack_textures
+  from mujoco_warp_pbr_gb300.context import upload_textures
 
   ts = pack_textures([(TEX_RGBA16F, im) for im in env.radiance])
   desc, data = upload_textures(ts, device)

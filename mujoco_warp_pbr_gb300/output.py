@@ -11,7 +11,7 @@ from __future__ import annotations
 import torch
 
 from mujoco_warp_pbr_gb300 import _lib
-from mujoco_warp_pbr_gb300.types import PbrRenderContext
+from mujoco_warp_pbr_gb300.pbr_types import PbrRenderContext
 
 
 def _check(rc: PbrRenderContext, camera_index: int, out: torch.Tensor, name: str, tail: tuple[int, ...], dtype: torch.dtype) -> None:

@@ -17,7 +17,7 @@ import torch
 
 from mujoco_warp_pbr_gb300 import _lib
 from mujoco_warp_pbr_gb300 import _scene
-from mujoco_warp_pbr_gb300.types import PbrRenderContext
+from mujoco_warp_pbr_gb300.pbr_types import PbrRenderContext
 
 _MODEL_FIELDS = (
   "geom_type",

@@ -21,7 +21,7 @@ import numpy as np
 from mujoco_warp_pbr_gb300 import _lib
 from mujoco_warp_pbr_gb300 import _scene
 from mujoco_warp_pbr_gb300 import envmap as envmap_lib
-from mujoco_warp_pbr_gb300 import io as io_lib
+from mujoco_warp_pbr_gb300 import context as io_lib
 
 HERE = Path(__file__).resolve().parent
 SOURCE = HERE / "mjpbr_oracle.c"
