@@ -834,8 +834,8 @@ def create_render_context(mjm: Any, nworld: int = 1, **kwargs: Any) -> PbrRender
     ValueError: for invalid arguments, or a model with nothing to render.
   """
   device = kwargs.pop("device", None)
+  hc = prepare_context(mjm, nworld, **kwargs)  # validates every argument before any device work
   device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-  hc = prepare_context(mjm, nworld, **kwargs)
   return upload_context(hc, device)
 
 

@@ -81,6 +81,8 @@ class Builder:
   textures: list[dict[str, Any]] = dataclasses.field(default_factory=list)
   headlight_active: bool = False
   headlight_ambient: tuple[float, float, float] = (0.0, 0.0, 0.0)
+  headlight_diffuse: tuple[float, float, float] = (0.4, 0.4, 0.4)
+  headlight_specular: tuple[float, float, float] = (0.5, 0.5, 0.5)
 
   def geom(self, type: int, size: Any, pos: Any = (0, 0, 0), mat: Any = None, rgba: Any = (0.5, 0.5, 0.5, 1.0), matid: int = -1, dataid: int = -1, group: int = 0) -> int:
     self.geoms.append(
@@ -136,9 +138,19 @@ class Builder:
     )
     return len(self.lights) - 1
 
-  def camera(self, pos: Any, target: Any, fovy: float = 45.0, resolution: tuple[int, int] = (64, 64), orthographic: bool = False) -> int:
+  def camera(self, pos: Any, target: Any = None, fovy: float = 45.0, resolution: tuple[int, int] = (64, 64), orthographic: bool = False, xyaxes: Any = None) -> int:
+    """A camera looking from pos at target, or with MuJoCo's xyaxes (camera x and y axes)."""
     pos = np.asarray(pos, float)
-    self.cams.append({"pos": pos, "mat": look_at(pos, np.asarray(target, float)), "fovy": fovy, "res": resolution, "proj": int(orthographic)})
+    if xyaxes is not None:
+      x = np.asarray(xyaxes[:3], float)
+      y = np.asarray(xyaxes[3:], float)
+      x = x / np.linalg.norm(x)
+      y = y - x * np.dot(x, y)
+      y = y / np.linalg.norm(y)
+      mat = np.stack([x, y, np.cross(x, y)], axis=1).reshape(9)
+    else:
+      mat = look_at(pos, np.asarray(target, float))
+    self.cams.append({"pos": pos, "mat": mat, "fovy": fovy, "res": resolution, "proj": int(orthographic)})
     return len(self.cams) - 1
 
   def mesh(self, vert: np.ndarray, face: np.ndarray, normal: np.ndarray | None = None, texcoord: np.ndarray | None = None) -> int:
@@ -246,6 +258,8 @@ class Builder:
       tex_colorspace=np.array([t["colorspace"] for t in self.textures], np.int32),
       headlight_active=self.headlight_active,
       headlight_ambient=self.headlight_ambient,
+      headlight_diffuse=self.headlight_diffuse,
+      headlight_specular=self.headlight_specular,
       stat_center=tuple(float(c) for c in center),
       stat_extent=2.0,
     )

@@ -426,7 +426,142 @@ static float woop_hit(const woop_t* w, v3 v0, v3 v1, v3 v2, float tmax, float* b
   return t;
 }
 
-/* Closest (any_hit: first) triangle of a mesh in [0, tmax): brute force over its faces. */
+/* The oracle's own mesh BVH (median split, up to 4 triangles per leaf), used to make the CPU
+ * baseline representative; brute force over every face stays available (oracle_set_mesh_bvh(0))
+ * and both give the same closest hit. */
+typedef struct {
+  float lo[3], hi[3];
+  int left, right; /* children, or -1 */
+  int first, count; /* leaf triangles (indices into order) */
+} onode_t;
+
+typedef struct {
+  onode_t* nodes;
+  int* order; /* face indices */
+  int nnode;
+} obvh_t;
+
+static int g_use_mesh_bvh = 1;
+static obvh_t* g_mesh_bvh = NULL;
+static int g_mesh_bvh_count = 0;
+
+static int obvh_build_rec(obvh_t* b, const float* cen, const float* blo, const float* bhi, int begin, int end) {
+  int idx = b->nnode++;
+  onode_t* nd = &b->nodes[idx];
+  for (int a = 0; a < 3; ++a) {
+    nd->lo[a] = 1e30f;
+    nd->hi[a] = -1e30f;
+  }
+  for (int i = begin; i < end; ++i) {
+    int f = b->order[i];
+    for (int a = 0; a < 3; ++a) {
+      if (blo[f * 3 + a] < nd->lo[a]) nd->lo[a] = blo[f * 3 + a];
+      if (bhi[f * 3 + a] > nd->hi[a]) nd->hi[a] = bhi[f * 3 + a];
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    float pad = 1.0e-5f * (1.0f + maxf(fabsf(nd->lo[a]), fabsf(nd->hi[a])));
+    nd->lo[a] -= pad;
+    nd->hi[a] += pad;
+  }
+  if (end - begin <= 4) {
+    nd->left = nd->right = -1;
+    nd->first = begin;
+    nd->count = end - begin;
+    return idx;
+  }
+  /* median along the widest centroid axis (insertion-free: partial selection by sorting) */
+  float clo[3] = {1e30f, 1e30f, 1e30f}, chi[3] = {-1e30f, -1e30f, -1e30f};
+  for (int i = begin; i < end; ++i) {
+    int f = b->order[i];
+    for (int a = 0; a < 3; ++a) {
+      if (cen[f * 3 + a] < clo[a]) clo[a] = cen[f * 3 + a];
+      if (cen[f * 3 + a] > chi[a]) chi[a] = cen[f * 3 + a];
+    }
+  }
+  int axis = 0;
+  for (int a = 1; a < 3; ++a)
+    if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+  /* simple in-place partition around the centroid midpoint, median fallback */
+  float mid = 0.5f * (clo[axis] + chi[axis]);
+  int i = begin, j = end - 1;
+  while (i <= j) {
+    if (cen[b->order[i] * 3 + axis] < mid) {
+      ++i;
+    } else {
+      int t = b->order[i];
+      b->order[i] = b->order[j];
+      b->order[j] = t;
+      --j;
+    }
+  }
+  int m = i;
+  if (m == begin || m == end) m = (begin + end) / 2;
+  int l = obvh_build_rec(b, cen, blo, bhi, begin, m);
+  int r = obvh_build_rec(b, cen, blo, bhi, m, end);
+  b->nodes[idx].left = l;
+  b->nodes[idx].right = r;
+  b->nodes[idx].first = 0;
+  b->nodes[idx].count = 0;
+  return idx;
+}
+
+static void obvh_build(const MjpbrScene* s, int mesh, int nface, obvh_t* b) {
+  int vadr = s->mesh_vertadr[mesh], fadr = s->mesh_faceadr[mesh];
+  float* cen = (float*)malloc(sizeof(float) * 3 * nface);
+  float* blo = (float*)malloc(sizeof(float) * 3 * nface);
+  float* bhi = (float*)malloc(sizeof(float) * 3 * nface);
+  b->order = (int*)malloc(sizeof(int) * nface);
+  b->nodes = (onode_t*)malloc(sizeof(onode_t) * 2 * nface);
+  b->nnode = 0;
+  for (int f = 0; f < nface; ++f) {
+    const int32_t* fv = s->mesh_face + (int64_t)(fadr + f) * 3;
+    for (int a = 0; a < 3; ++a) {
+      float lo = 1e30f, hi = -1e30f;
+      for (int k = 0; k < 3; ++k) {
+        float x = s->mesh_vert[(int64_t)(vadr + fv[k]) * 3 + a];
+        lo = x < lo ? x : lo;
+        hi = x > hi ? x : hi;
+      }
+      blo[f * 3 + a] = lo;
+      bhi[f * 3 + a] = hi;
+      cen[f * 3 + a] = 0.5f * (lo + hi);
+    }
+    b->order[f] = f;
+  }
+  obvh_build_rec(b, cen, blo, bhi, 0, nface);
+  free(cen);
+  free(blo);
+  free(bhi);
+}
+
+static float obox(const onode_t* n, v3 o, v3 inv, float tmax) {
+  float t1x = (n->lo[0] - o.x) * inv.x, t2x = (n->hi[0] - o.x) * inv.x;
+  float t1y = (n->lo[1] - o.y) * inv.y, t2y = (n->hi[1] - o.y) * inv.y;
+  float t1z = (n->lo[2] - o.z) * inv.z, t2z = (n->hi[2] - o.z) * inv.z;
+  float tmin = maxf(maxf(minf(t1x, t2x), minf(t1y, t2y)), minf(t1z, t2z));
+  float tmx = minf(minf(maxf(t1x, t2x), maxf(t1y, t2y)), maxf(t1z, t2z));
+  float entry = maxf(tmin, 0.0f);
+  return (tmx >= entry && entry < tmax) ? entry : -1.0f;
+}
+
+static float rcp_safe(float x) { return 1.0f / (fabsf(x) > 1.0e-30f ? x : (x >= 0.0f ? 1.0e-30f : -1.0e-30f)); }
+
+/* Triangle test of face f (mesh-relative) for mesh_query. */
+static float face_hit(const MjpbrScene* s, int vadr, int fadr, int f, const woop_t* w, float best, float* u, float* v,
+                      v3* e1o, v3* e2o) {
+  const int32_t* fv = s->mesh_face + (int64_t)(fadr + f) * 3;
+  const float* p0 = s->mesh_vert + (int64_t)(vadr + fv[0]) * 3;
+  const float* p1 = s->mesh_vert + (int64_t)(vadr + fv[1]) * 3;
+  const float* p2 = s->mesh_vert + (int64_t)(vadr + fv[2]) * 3;
+  v3 v0 = V(p0[0], p0[1], p0[2]), v1 = V(p1[0], p1[1], p1[2]), v2 = V(p2[0], p2[1], p2[2]);
+  *e1o = vsub(v1, v0);
+  *e2o = vsub(v2, v0);
+  return woop_hit(w, v0, v1, v2, best, u, v);
+}
+
+/* Closest (any_hit: first) triangle of a mesh in [0, tmax): brute force over its faces, or the
+ * oracle's mesh BVH when built. */
 static float mesh_query(const MjpbrScene* s, int mesh, int nface, v3 lo, v3 ld, float tmax, int cull, int any_hit,
                         v3* nl, float* bu, float* bv, int* face) {
   woop_t w = woop_setup(lo, ld);
@@ -435,6 +570,64 @@ static float mesh_query(const MjpbrScene* s, int mesh, int nface, v3 lo, v3 ld, 
   int found = -1;
   v3 e1b = V(0, 0, 0), e2b = V(0, 0, 0);
   float ub = 0.0f, vb = 0.0f;
+  if (g_mesh_bvh && mesh < g_mesh_bvh_count && g_mesh_bvh[mesh].nodes) {
+    const obvh_t* b = &g_mesh_bvh[mesh];
+    v3 inv = V(rcp_safe(ld.x), rcp_safe(ld.y), rcp_safe(ld.z));
+    int stack[64];
+    float st_t[64];
+    int sp = 0;
+    if (obox(&b->nodes[0], lo, inv, best) >= 0.0f) {
+      stack[0] = 0;
+      st_t[0] = 0.0f;
+      sp = 1;
+    }
+    while (sp > 0) {
+      --sp;
+      if (st_t[sp] >= best) continue;
+      const onode_t* nd = &b->nodes[stack[sp]];
+      if (nd->left >= 0) {
+        float ta = obox(&b->nodes[nd->left], lo, inv, best), tb = obox(&b->nodes[nd->right], lo, inv, best);
+        int near = nd->left, far = nd->right;
+        float tn = ta, tf = tb;
+        if (tb >= 0.0f && (ta < 0.0f || tb < ta)) {
+          near = nd->right;
+          far = nd->left;
+          tn = tb;
+          tf = ta;
+        }
+        if (tf >= 0.0f && sp < 64) {
+          stack[sp] = far;
+          st_t[sp++] = tf;
+        }
+        if (tn >= 0.0f && sp < 64) {
+          stack[sp] = near;
+          st_t[sp++] = tn;
+        }
+        continue;
+      }
+      for (int k = nd->first; k < nd->first + nd->count; ++k) {
+        int f = b->order[k];
+        float u, v;
+        v3 e1, e2;
+        float t = face_hit(s, vadr, fadr, f, &w, best, &u, &v, &e1, &e2);
+        if (t < 0.0f) continue;
+        if (!any_hit && cull && vdot(ld, vcross(e1, e2)) > 0.0f) continue;
+        if (any_hit) return t;
+        best = t;
+        found = f;
+        e1b = e1;
+        e2b = e2;
+        ub = u;
+        vb = v;
+      }
+    }
+    if (found < 0) return -1.0f;
+    *nl = vnorm(vcross(e1b, e2b));
+    *bu = ub;
+    *bv = vb;
+    *face = found;
+    return best;
+  }
   for (int f = 0; f < nface; ++f) {
     const int32_t* fv = s->mesh_face + (int64_t)(fadr + f) * 3;
     const float* p0 = s->mesh_vert + (int64_t)(vadr + fv[0]) * 3;
@@ -1509,6 +1702,11 @@ int oracle_render_rt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t se
   for (int c = 0; c < s->nrender; ++c) row_cam[c + 1] = row_cam[c] + s->cam_res[c][1];
   nrow = row_cam[s->nrender];
   int64_t total = (int64_t)(w1 - w0) * nrow;
+  if (g_use_mesh_bvh && s->nmesh > 0 && mesh_nface && s->mesh_vert) {
+    g_mesh_bvh = (obvh_t*)calloc((size_t)s->nmesh, sizeof(obvh_t));
+    g_mesh_bvh_count = s->nmesh;
+    for (int m = 0; m < s->nmesh; ++m) obvh_build(s, m, mesh_nface[m], &g_mesh_bvh[m]);
+  }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 4)
@@ -1522,8 +1720,20 @@ int oracle_render_rt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t se
     int py = r - row_cam[c];
     for (int px = 0; px < s->cam_res[c][0]; ++px) render_pixel(s, mesh_nface, w, c, px, py, seed);
   }
+  if (g_mesh_bvh) {
+    for (int m = 0; m < g_mesh_bvh_count; ++m) {
+      free(g_mesh_bvh[m].nodes);
+      free(g_mesh_bvh[m].order);
+    }
+    free(g_mesh_bvh);
+    g_mesh_bvh = NULL;
+    g_mesh_bvh_count = 0;
+  }
   return 0;
 }
+
+/* 1: mesh queries use the oracle's own BVH (default); 0: brute force over every face. */
+void oracle_set_mesh_bvh(int enable) { g_use_mesh_bvh = enable; }
 
 /* Split-sum DFG table (size, size, 2), ibl.py:62-93. */
 void oracle_dfg_lut(float* lut, int n, int nsample) {

@@ -55,6 +55,7 @@ def load() -> ctypes.CDLL:
     lib.oracle_build_mips.argtypes = [ctypes.POINTER(_lib.Texture), vp]
     lib.oracle_prefilter.argtypes = [ctypes.POINTER(_lib.Texture), vp, i32, i32, i32, i32, vp]
     lib.oracle_struct_layout.argtypes = [ctypes.POINTER(ctypes.c_int64)]
+    lib.oracle_set_mesh_bvh.argtypes = [i32]
     lib.oracle_nthreads.restype = i32
     lib.oracle_sincos_turns.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     lib.oracle_rand01.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
