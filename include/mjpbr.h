@@ -273,17 +273,19 @@ typedef struct MjpbrScene {
   int32_t bundle_res[MJPBR_MAX_RENDER][2];
 
   /* ---- Path-tier denoiser features (nworld, rgb_stride) ---- */
-  float* aov_albedo;               /* (.., 3) */
-  float* aov_normal;               /* (.., 3) */
-  float* aov_depth;                /* (..) */
-  float* aov_emission;             /* (.., 3) */
-  float* aov_variance;             /* (..) */
-  float* denoise_buffers[2];       /* (.., 4) ping-pong */
+  uint32_t* aov_guide;             /* (.., 4) first-hit guide of the filter: words 0-2 hold the
+                                      normal xyz then the albedo xyz as IEEE half floats (low half
+                                      first), word 3 the depth (float bits) */
+  float* aov_emission;             /* (.., 3) exposed first-hit emission, kept out of filtering */
+  float* denoise_buffers[2];       /* (.., 4) demodulated radiance and its variance; the path
+                                      tracer writes [0], the filter passes ping-pong */
   int32_t denoise_iterations;
   int32_t pad2_;
 
-  /* ---- Status ---- */
+  /* ---- Status and scratch ---- */
   int32_t* error_word;             /* device int32, kernels OR error bits into it (may be NULL) */
+  int32_t* work_counter;           /* device int32[4] scratch of the persistent kernels' work queues
+                                      (the library zeroes it on the stream before each use) */
 
   MjpbrSettings settings;
 } MjpbrScene;

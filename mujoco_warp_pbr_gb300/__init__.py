@@ -22,6 +22,7 @@ from mujoco_warp_pbr_gb300.output import get_normal as get_normal
 from mujoco_warp_pbr_gb300.output import get_rgb as get_rgb
 from mujoco_warp_pbr_gb300.output import get_segmentation as get_segmentation
 from mujoco_warp_pbr_gb300.render import check_errors as check_errors
+from mujoco_warp_pbr_gb300.render import denoise as denoise
 from mujoco_warp_pbr_gb300.render import refit_bvh as refit_bvh
 from mujoco_warp_pbr_gb300.render import render as render
 from mujoco_warp_pbr_gb300.render import scene as scene_descriptor

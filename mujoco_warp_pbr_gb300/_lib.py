@@ -233,16 +233,14 @@ class Scene(ctypes.Structure):
     ("ray_direction", c_vp),
     ("bundle_res", _CAM2),
     # path-tier features
-    ("aov_albedo", c_vp),
-    ("aov_normal", c_vp),
-    ("aov_depth", c_vp),
+    ("aov_guide", c_vp),
     ("aov_emission", c_vp),
-    ("aov_variance", c_vp),
     ("denoise_buffers", c_vp * 2),
     ("denoise_iterations", c_i32),
     ("pad2_", c_i32),
     # status
     ("error_word", c_vp),
+    ("work_counter", c_vp),
     ("settings", Settings),
   ]
 

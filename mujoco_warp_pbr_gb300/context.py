@@ -942,16 +942,14 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     dfg_lut=dfg_lut(device),
     dfg_size=DFG_LUT_SIZE,
     env=env,
-    aov_albedo=torch.zeros((nworld, aov_pix, 3), dtype=f32, device=device),
-    aov_normal=torch.zeros((nworld, aov_pix, 3), dtype=f32, device=device),
-    aov_depth=torch.zeros((nworld, aov_pix), dtype=f32, device=device),
+    aov_guide=torch.zeros((nworld, aov_pix, 4), dtype=torch.int32, device=device),
     aov_emission=torch.zeros((nworld, aov_pix, 3), dtype=f32, device=device),
-    aov_variance=torch.zeros((nworld, aov_pix), dtype=f32, device=device),
     denoise_buffers=(
       torch.zeros((nworld, aov_pix, 4), dtype=f32, device=device),
       torch.zeros((nworld, aov_pix, 4), dtype=f32, device=device),
     ),
     error_word=torch.zeros(1, dtype=torch.int32, device=device),
+    work_counter=torch.zeros(4, dtype=torch.int32, device=device),
     device=device,
     block_dim=op["block_dim"],
     max_registers=op["max_registers"],

@@ -193,6 +193,9 @@ MJ_HD float rand01(uint32_t seed, uint32_t counter) {
   return (float)(h >> 8) * (1.0f / 16777216.0f);
 }
 
+// Relative luminance of linear Rec. 709 colour (color.py:91-93), plain arithmetic.
+MJ_HD float luminance(V3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+
 // Orthonormal basis around a unit vector (Duff et al., "Building an Orthonormal Basis,
 // Revisited", JCGT 2017), plain arithmetic.
 MJ_HD void orthonormal_basis(V3 n, V3* t1, V3* t2) {

@@ -180,7 +180,6 @@ MJ_DEV void eval_light(const Light& light, int32_t light_model, V3 point, V3* l,
 
 // ---------------------------------------------------------------- colour
 
-MJ_DEV float luminance(V3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
 
 MJ_DEV V3 tonemap_pbr_neutral(V3 c) {
   const float start = 0.8f - 0.04f;

@@ -168,13 +168,11 @@ class PbrRenderContext:
   dfg_size: int
   env: Any
   # path tier
-  aov_albedo: torch.Tensor
-  aov_normal: torch.Tensor
-  aov_depth: torch.Tensor
+  aov_guide: torch.Tensor
   aov_emission: torch.Tensor
-  aov_variance: torch.Tensor
   denoise_buffers: tuple[torch.Tensor, torch.Tensor]
   error_word: torch.Tensor
+  work_counter: torch.Tensor
   device: torch.device
   denoise_sigma_color: float = 4.0
   denoise_sigma_normal: float = 128.0

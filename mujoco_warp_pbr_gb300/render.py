@@ -208,14 +208,12 @@ def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
       "tex_data": rc.tex_data,
       "dfg_lut": rc.dfg_lut,
       "dfg_size": rc.dfg_size,
-      "aov_albedo": rc.aov_albedo,
-      "aov_normal": rc.aov_normal,
-      "aov_depth": rc.aov_depth,
+      "aov_guide": rc.aov_guide,
       "aov_emission": rc.aov_emission,
-      "aov_variance": rc.aov_variance,
       "denoise_buffers": rc.denoise_buffers,
       "denoise_iterations": int(rc.denoise_iterations),
       "error_word": rc.error_word,
+      "work_counter": rc.work_counter,
       "settings": st,
     }
   )
@@ -287,18 +285,30 @@ def refit_bvh(m: Any, d: Any, rc: PbrRenderContext) -> None:
   rc._host_cache["refit"] = True
 
 
-def render(m: Any, d: Any, rc: PbrRenderContext, seed: int = 0) -> None:
+def render(m: Any, d: Any, rc: PbrRenderContext, seed: int = 0, denoise: bool = True) -> None:
   """Renders the current frame into the context's output buffers (one kernel for the real-time
-  tier). The image is a deterministic function of the seed. The per-world blocks come from the
-  last refit_bvh; the first render of a context refits once itself."""
+  tier, one persistent kernel for the path-traced tier). The image is a deterministic function of
+  the seed. The per-world blocks come from the last refit_bvh; the first render of a context
+  refits once itself. A path-traced context created with denoise=True then runs the a-trous
+  filter (render.py:431-470); denoise=False leaves the noisy image and the filter's inputs for a
+  later denoise() call."""
   s = scene(m, d, rc)
   stream = _stream(rc)
   if not rc._host_cache.get("refit"):
     _lib.call("mjpbr_refit_bvh", s, stream)
     rc._host_cache["refit"] = True
   _lib.call("mjpbr_render", s, int(seed) & 0xFFFFFFFF, stream)
-  if rc.tier == 1 and rc.denoise:
+  if rc.tier == 1 and rc.denoise and denoise:
     _lib.call("mjpbr_denoise_atrous", s, stream)
+
+
+def denoise(m: Any, d: Any, rc: PbrRenderContext) -> None:
+  """Filters the path tracer's demodulated image into the RGB (and HDR) outputs
+  (denoise.py:214-248): denoise_iterations a-trous passes, the last one remodulating, tone
+  mapping and encoding."""
+  if not (rc.tier == 1 and rc.denoise):
+    raise ValueError("denoise applies to a path-traced context created with denoise=True")
+  _lib.call("mjpbr_denoise_atrous", scene(m, d, rc), _stream(rc))
 
 
 def check_errors(rc: PbrRenderContext) -> int:

@@ -1,8 +1,8 @@
 /*
  * CPU oracle of the GB300 render path — TEST INFRASTRUCTURE ONLY.
  *
- * A plain scalar C restatement of julien-blanchon/mujoco_warp_pbr's real-time tier and of its
- * context-creation tables. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
+ * A plain scalar C restatement of julien-blanchon/mujoco_warp_pbr's real-time and path-traced
+ * tiers and of its context-creation tables. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
  * may load it, as the checker (and, timed, as the CPU baseline); the product never calls it.
  *
  * It reads the same MjpbrScene descriptor as libmjpbr (include/mjpbr.h), but with HOST pointers,
@@ -28,6 +28,8 @@
  *   surface               mujoco_warp_pbr/_src/material.py:290-550, texture.py:104-233
  *   BRDF / lights / colour brdf.py:32-110, lights.py:151-198, color.py:40-119
  *   shading / pixel       render.py:67-395, kernel_inputs.py:207-231
+ *   path-traced tier      pathtrace.py:64-424, brdf.py:116-191, envmap.py:433-490
+ *   denoiser              denoise.py:72-248
  *   environment           envmap.py:154-303, ibl.py:40-119
  */
 #include <math.h>
@@ -1682,6 +1684,511 @@ static void render_pixel(const MjpbrScene* s, const int32_t* mesh_nface, int w, 
   s->rgb_data[adr] = encode_display(vmul(display, inv_nn));
 }
 
+/* ------------------------------------------------------------------ path-traced tier (pathtrace.py) */
+
+/* Random-number layout of pathtrace.py:64-95: path vertex (sample, depth) owns PT_SLOTS counters,
+ * depth row PT_JITTER holds the sub-pixel jitter, lights past the fourth use a separate range. */
+#define PT_SLOTS 16
+#define PT_DEPTHS 64
+#define PT_JITTER (PT_DEPTHS - 1)
+#define PT_SUBPIXEL 15
+#define PT_EXTRA_LIGHTS (1u << 30)
+
+static float pt_rand(uint32_t seed, int sample, int depth, int slot) {
+  return rand01(seed, (uint32_t)((sample * PT_DEPTHS + depth) * PT_SLOTS + slot));
+}
+
+static void pt_light_rand2(uint32_t seed, int sample, int depth, int nlight, int li, float* u0, float* u1) {
+  if (li < 4) {
+    *u0 = pt_rand(seed, sample, depth, 4 + 2 * li);
+    *u1 = pt_rand(seed, sample, depth, 5 + 2 * li);
+    return;
+  }
+  uint32_t counter = PT_EXTRA_LIGHTS + (uint32_t)(((sample * PT_DEPTHS + depth) * nlight + li) * 2);
+  *u0 = rand01(seed, counter);
+  *u1 = rand01(seed, counter + 1u);
+}
+
+static float lum709(v3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+
+/* brdf.py:116-191 */
+static float smith_g1(float nov, float alpha) {
+  float a2 = alpha * alpha;
+  return 2.0f * nov / (nov + sqrtf(a2 + (1.0f - a2) * nov * nov));
+}
+
+static v3 ggx_vndf(v3 v, float alpha, float u0, float u1) {
+  v3 vh = vnorm(V(alpha * v.x, alpha * v.y, v.z));
+  float lensq = vh.x * vh.x + vh.y * vh.y;
+  v3 t1 = V(1, 0, 0);
+  if (lensq > 0.0f) t1 = vdiv(V(-vh.y, vh.x, 0.0f), sqrtf(lensq));
+  v3 t2 = vcross(vh, t1);
+  float r = sqrtf(u0), sn, cs;
+  sincos_turns(u1, &sn, &cs);
+  float p1 = r * cs, p2 = r * sn;
+  float sw = 0.5f * (1.0f + vh.z);
+  p2 = (1.0f - sw) * sqrtf(maxf(1.0f - p1 * p1, 0.0f)) + sw * p2;
+  v3 nh = vadd(vadd(vmul(t1, p1), vmul(t2, p2)), vmul(vh, sqrtf(maxf(1.0f - p1 * p1 - p2 * p2, 0.0f))));
+  return vnorm(V(alpha * nh.x, alpha * nh.y, maxf(nh.z, 0.0f)));
+}
+
+static v3 bsdf_cos(v3 diffuse_color, v3 f0, float alpha, v3 energy_comp, v3 v, v3 l) {
+  float nol = l.z, nov = maxf(v.z, 1.0e-4f);
+  if (nol <= 0.0f) return V(0, 0, 0);
+  v3 h = vnorm(vadd(l, v));
+  float noh = maxf(h.z, 0.0f), loh = maxf(vdot(l, h), 0.0f);
+  v3 spec = vcmul(vmul(f_schlick(f0, 1.0f, loh), d_ggx(noh, alpha) * v_smith(nov, nol, alpha)), energy_comp);
+  return vmul(vadd(vmul(diffuse_color, 1.0f / PI_F), spec), nol);
+}
+
+static float bsdf_pdf(float alpha, float p_spec, v3 v, v3 l) {
+  if (l.z <= 0.0f) return 0.0f;
+  float nov = maxf(v.z, 1.0e-4f);
+  v3 h = vnorm(vadd(l, v));
+  float pdf_spec = smith_g1(nov, alpha) * d_ggx(maxf(h.z, 0.0f), alpha) / (4.0f * nov);
+  return p_spec * pdf_spec + (1.0f - p_spec) * (l.z * (1.0f / PI_F));
+}
+
+static float spec_probability(v3 diffuse_color, v3 spec_albedo) {
+  float ws = lum709(spec_albedo), wd = lum709(diffuse_color);
+  if (wd <= 0.0f) return 1.0f;
+  return clampf_(ws / maxf(ws + wd, 1.0e-6f), 0.1f, 0.9f);
+}
+
+static v3 bsdf_sample(float alpha, float p_spec, v3 v, float u_lobe, float u0, float u1) {
+  if (u_lobe < p_spec) {
+    v3 h = ggx_vndf(v, alpha, u0, u1);
+    return vsub(vmul(h, 2.0f * vdot(v, h)), v);
+  }
+  float r = sqrtf(u0), sn, cs;
+  sincos_turns(u1, &sn, &cs);
+  return V(r * cs, r * sn, sqrtf(maxf(1.0f - u0, 0.0f)));
+}
+
+static float power_heuristic(float a, float b) {
+  float a2 = a * a;
+  return a2 / maxf(a2 + b * b, 1.0e-30f);
+}
+
+static int cdf_find(const float* cdf, int n, float u) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) / 2;
+    if (cdf[mid] <= u)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+/* envmap.py:446-490: a world direction drawn proportional to luminance x sin(theta), its pdf. */
+static v3 env_sample(const MjpbrScene* s, int env, float yaw, float u0, float u1, float* pdf) {
+  int h = s->cdf_height, w = s->cdf_width;
+  const float* marginal = s->env_marginal + (int64_t)env * (h + 1);
+  int r = cdf_find(marginal, h, u0);
+  float c0 = marginal[r];
+  float dv = (u0 - c0) / maxf(marginal[r + 1] - c0, 1.0e-12f);
+  const float* crow = s->env_conditional + ((int64_t)env * h + r) * (w + 1);
+  int c = cdf_find(crow, w, u1);
+  float k0 = crow[c];
+  float du = (u1 - k0) / maxf(crow[c + 1] - k0, 1.0e-12f);
+  float uu = ((float)c + clampf_(du, 0.0f, 1.0f)) / (float)w;
+  float vv = ((float)r + clampf_(dv, 0.0f, 1.0f)) / (float)h;
+  float sp, cp, sth, cth, sy, cy;
+  sincos_turns(uu - 0.5f, &sp, &cp);
+  sincos_turns(vv * 0.5f, &sth, &cth);
+  v3 d = V(sth * cp, sth * sp, cth);
+  sincos_turns(yaw * (0.5f / PI_F), &sy, &cy);
+  d = V(cy * d.x - sy * d.y, sy * d.x + cy * d.y, d.z);
+  *pdf = s->env_prob[((int64_t)env * h + r) * w + c] * (float)(w * h) / (2.0f * PI_F * PI_F * maxf(sth, 1.0e-6f));
+  return d;
+}
+
+static float env_pdf(const MjpbrScene* s, int env, float yaw, v3 d) {
+  int h = s->cdf_height, w = s->cdf_width;
+  float u, v, sn, cs;
+  direction_to_uv(d, yaw, &u, &v);
+  int c = (int)(u * (float)w), r = (int)(v * (float)h);
+  if (c > w - 1) c = w - 1;
+  if (r > h - 1) r = h - 1;
+  sincos_turns(v * 0.5f, &sn, &cs);
+  return s->env_prob[((int64_t)env * h + r) * w + c] * (float)(w * h) / (2.0f * PI_F * PI_F * maxf(sn, 1.0e-6f));
+}
+
+static v3 pt_environment(const ctx_t* c, v3 d) { return vmul(sample_radiance(c->W.s, c->env, d, c->env_yaw, 0.0f), c->env_scale); }
+
+/* Next-event estimate of one light (pathtrace.py:126-160). */
+static v3 pt_light(const ctx_t* c, light_t light, const lobes_t* lb, v3 point, v3 normal, v3 t1, v3 t2, v3 v, float u0,
+                   float u1) {
+  const MjpbrSettings* st = &c->W.s->settings;
+  if (light.type != MJPBR_LIGHT_DIRECTIONAL && light.bulbradius > 0.0f) {
+    v3 b1, b2;
+    orthonormal_basis(vnorm(vsub(point, light.pos)), &b1, &b2);
+    float r = light.bulbradius * sqrtf(u0), sn, cs;
+    sincos_turns(u1, &sn, &cs);
+    light.pos = vadd(light.pos, vmul(vadd(vmul(b1, cs), vmul(b2, sn)), r));
+  }
+  v3 l, ds, ss;
+  float dist;
+  eval_light(&light, st->light_model, point, &l, &dist, &ds, &ss);
+  v3 ll = V(vdot(l, t1), vdot(l, t2), vdot(l, normal));
+  if (ll.z <= 0.0f || (vdot(ds, ds) == 0.0f && vdot(ss, ss) == 0.0f)) return V(0, 0, 0);
+  if (st->use_shadows && light.castshadow) {
+    float max_t = light.type == MJPBR_LIGHT_DIRECTIONAL ? UNBOUNDED : dist - SHADOW_GAP;
+    if (occluded(&c->W, vadd(point, vmul(normal, RAY_OFFSET)), l, max_t, st->cull_backfaces)) return V(0, 0, 0);
+  }
+  v3 zero = V(0, 0, 0);
+  v3 diffuse = bsdf_cos(lb->diffuse_color, zero, lb->alpha, zero, v, ll);
+  v3 specular = bsdf_cos(zero, lb->f0, lb->alpha, lb->energy_comp, v, ll);
+  return vadd(vcmul(diffuse, ds), vcmul(specular, ss));
+}
+
+typedef struct {
+  hit_t hit;
+  v3 albedo, normal, emission, base_color;
+} primary_t;
+
+/* Radiance of one path and its first surface (pathtrace.py:200-337). */
+static v3 trace_path(const ctx_t* c, v3 origin, v3 dir, float max_dist, v3 head_dir, uint32_t seed, int sample,
+                     primary_t* first) {
+  const MjpbrScene* s = c->W.s;
+  const MjpbrSettings* st = &s->settings;
+  int cull = st->cull_backfaces;
+  v3 radiance = V(0, 0, 0), beta = V(1, 1, 1);
+  first->hit.geom = -1;
+  first->albedo = V(1, 1, 1);
+  first->normal = V(0, 0, 0);
+  first->emission = V(0, 0, 0);
+  first->base_color = V(0, 0, 0);
+  int camera_ray = 1, delta = 1, depth = 0, passes = 0;
+  float pdf_prev = 0.0f;
+  while (depth <= st->max_depth) {
+    hit_t hit = closest(&c->W, origin, dir, max_dist, cull);
+    if (camera_ray && passes == 0) first->hit = hit;
+    if (hit.geom == -1) {
+      if (camera_ray) {
+        if (st->env_background) {
+          radiance = vadd(radiance, vcmul(beta, pt_environment(c, dir)));
+        } else {
+          v3 bg = vdiv(V(st->background[0], st->background[1], st->background[2]), c->exposure);
+          radiance = vadd(radiance, vcmul(beta, bg));
+        }
+      } else {
+        v3 env_light = c->ambient;
+        if (st->has_env) {
+          float weight = 1.0f;
+          if (!delta) weight = power_heuristic(pdf_prev, env_pdf(s, c->env, c->env_yaw, dir));
+          env_light = vadd(env_light, vmul(pt_environment(c, dir), weight));
+        }
+        radiance = vadd(radiance, vcmul(beta, env_light));
+      }
+      break;
+    }
+    v3 point = vadd(origin, vmul(dir, hit.dist));
+    v3 normal;
+    surface_t sf = eval_surface(&c->W, &hit, point, dir, 0.0f, &normal);
+    if (st->has_transparency) {
+      if (pt_rand(seed, sample, depth + passes, 0) >= sf.alpha && passes < 4 * st->max_layers) {
+        origin = vadd(point, vmul(dir, RAY_OFFSET));
+        max_dist = max_dist - hit.dist;
+        passes += 1;
+        continue;
+      }
+    }
+    radiance = vadd(radiance, vcmul(beta, vdiv(sf.emissive, c->exposure)));
+    if (depth == st->max_depth) break;
+    max_dist = MAXVAL;
+    if (camera_ray) {
+      first->albedo = sf.base_color;
+      first->normal = normal;
+      first->base_color = sf.base_color;
+      first->emission = vdiv(sf.emissive, c->exposure);
+    }
+    camera_ray = 0;
+    if (st->has_reflection) {
+      if (pt_rand(seed, sample, depth, 1) < mirror_reflectance(c, hit.geom)) {
+        dir = vsub(dir, vmul(normal, 2.0f * vdot(dir, normal)));
+        origin = vadd(point, vmul(normal, RAY_OFFSET));
+        delta = 1;
+        depth += 1;
+        continue;
+      }
+    }
+    v3 t1, t2;
+    orthonormal_basis(normal, &t1, &t2);
+    v3 view = vneg(dir);
+    v3 v = V(vdot(view, t1), vdot(view, t2), vdot(view, normal));
+    float nov = maxf(v.z, 1.0e-4f);
+    lobes_t lb = shading_lobes(s, &sf, nov);
+    v3 spec_weight = vcmul(lb.spec_albedo, lb.energy_comp);
+    float p_spec = spec_probability(lb.diffuse_color, spec_weight);
+    if (depth == 0) first->albedo = vadd(lb.diffuse_color, spec_weight);
+
+    v3 direct = V(0, 0, 0);
+    for (int li = 0; li < s->nlight; ++li) {
+      light_t light = fetch_light(s, c->W.w, li);
+      if (!light.active) continue;
+      float u0, u1;
+      pt_light_rand2(seed, sample, depth, s->nlight, li, &u0, &u1);
+      direct = vadd(direct, pt_light(c, light, &lb, point, normal, t1, t2, v, u0, u1));
+    }
+    if (st->headlight_active) {
+      light_t head;
+      memset(&head, 0, sizeof(head));
+      head.type = MJPBR_LIGHT_DIRECTIONAL;
+      head.active = 1;
+      head.dir = head_dir;
+      head.diffuse = V(st->headlight_diffuse[0], st->headlight_diffuse[1], st->headlight_diffuse[2]);
+      head.specular = V(st->headlight_specular[0], st->headlight_specular[1], st->headlight_specular[2]);
+      head.attenuation = V(1, 0, 0);
+      head.intensity = st->headlight_intensity / c->exposure;
+      head.range = 1.0f;
+      direct = vadd(direct, pt_light(c, head, &lb, point, normal, t1, t2, v, 0.0f, 0.0f));
+    }
+    radiance = vadd(radiance, vcmul(beta, direct));
+
+    if (st->has_env) {
+      float pdf_env;
+      v3 d_env = env_sample(s, c->env, c->env_yaw, pt_rand(seed, sample, depth, 2), pt_rand(seed, sample, depth, 3), &pdf_env);
+      v3 le = V(vdot(d_env, t1), vdot(d_env, t2), vdot(d_env, normal));
+      if (le.z > 0.0f && pdf_env > 0.0f) {
+        v3 f = bsdf_cos(lb.diffuse_color, lb.f0, lb.alpha, lb.energy_comp, v, le);
+        if (!occluded(&c->W, vadd(point, vmul(normal, RAY_OFFSET)), d_env, UNBOUNDED, cull)) {
+          float weight = power_heuristic(pdf_env, bsdf_pdf(lb.alpha, p_spec, v, le));
+          radiance = vadd(radiance, vmul(vcmul(beta, vcmul(f, pt_environment(c, d_env))), weight / pdf_env));
+        }
+      }
+    }
+
+    v3 l = bsdf_sample(lb.alpha, p_spec, v, pt_rand(seed, sample, depth, 12), pt_rand(seed, sample, depth, 13),
+                       pt_rand(seed, sample, depth, 14));
+    if (l.z <= 0.0f) break;
+    float pdf = bsdf_pdf(lb.alpha, p_spec, v, l);
+    if (pdf <= 0.0f) break;
+    beta = vcmul(beta, vdiv(bsdf_cos(lb.diffuse_color, lb.f0, lb.alpha, lb.energy_comp, v, l), pdf));
+    dir = vnorm(vadd(vadd(vmul(t1, l.x), vmul(t2, l.y)), vmul(normal, l.z)));
+    origin = vadd(point, vmul(normal, RAY_OFFSET));
+    pdf_prev = pdf;
+    delta = 0;
+    depth += 1;
+    if (depth >= st->rr_depth) {
+      float q = clampf_(maxf(beta.x, maxf(beta.y, beta.z)), 0.05f, 0.95f);
+      if (pt_rand(seed, sample, depth, 15) >= q) break;
+      beta = vdiv(beta, q);
+    }
+  }
+  return radiance;
+}
+
+static v3 round_half3(v3 a) {
+  return V(half_to_float(float_to_half(a.x)), half_to_float(float_to_half(a.y)), half_to_float(float_to_half(a.z)));
+}
+
+/* The filter's first-hit guide: normal and albedo as half floats, depth (the GPU packs the same
+ * values into four 32-bit words). */
+#define MIN_ALBEDO 1.0e-2f
+
+typedef struct {
+  v3 normal, albedo;
+  float depth;
+} guide_t;
+
+static void store_guide(uint32_t* o, const guide_t* g) {
+  o[0] = (uint32_t)float_to_half(g->normal.x) | ((uint32_t)float_to_half(g->normal.y) << 16);
+  o[1] = (uint32_t)float_to_half(g->normal.z) | ((uint32_t)float_to_half(g->albedo.x) << 16);
+  o[2] = (uint32_t)float_to_half(g->albedo.y) | ((uint32_t)float_to_half(g->albedo.z) << 16);
+  memcpy(&o[3], &g->depth, 4);
+}
+
+static guide_t load_guide(const uint32_t* o) {
+  guide_t g;
+  g.normal = V(half_to_float((uint16_t)(o[0] & 0xffffu)), half_to_float((uint16_t)(o[0] >> 16)), half_to_float((uint16_t)(o[1] & 0xffffu)));
+  g.albedo = V(half_to_float((uint16_t)(o[1] >> 16)), half_to_float((uint16_t)(o[2] & 0xffffu)), half_to_float((uint16_t)(o[2] >> 16)));
+  memcpy(&g.depth, &o[3], 4);
+  return g;
+}
+
+/* One pixel of the path-traced megakernel (pathtrace.py:340-424). */
+static void render_pixel_pt(const MjpbrScene* s, const int32_t* mesh_nface, int w, int c, int px, int py, uint32_t seed) {
+  const MjpbrSettings* st = &s->settings;
+  int W = s->cam_res[c][0], H = s->cam_res[c][1];
+  int pixelid = py * W + px;
+  cam_t cam = camera(s, w, c);
+  ctx_t ctx;
+  ctx.W.s = s;
+  ctx.W.mesh_nface = mesh_nface;
+  ctx.W.w = w;
+  ctx.exposure = bf(s->exposure, w, 1, 0);
+  ctx.ambient = bv3(s->ambient_radiance, w, 1, 0);
+  ctx.env = 0;
+  ctx.env_yaw = 0.0f;
+  ctx.env_scale = 0.0f;
+  if (s->nenv > 0 && s->env_id.ptr) {
+    ctx.env = bi(s->env_id, w, 1, 0);
+    ctx.env_yaw = bf(s->env_yaw, w, 1, 0);
+    ctx.env_scale = bf(s->env_intensity, w, 1, 0);
+  }
+  const int centre = PT_SUBPIXEL / 2;
+  if (!s->render_rgb[c]) {
+    v3 dcam, ocam;
+    camera_frame_ray(&cam, W, H, px, py, PT_SUBPIXEL, centre, centre, &dcam, &ocam);
+    float max_dist = st->zfar > 0.0f ? st->zfar / maxf(-dcam.z, 1.0e-6f) : MAXVAL;
+    hit_t hit = closest(&ctx.W, vadd(cam.pos, mat_mul(cam.mat, ocam)), mat_mul(cam.mat, dcam), max_dist, st->cull_backfaces);
+    write_geometry(s, w, c, pixelid, &hit, dcam.z);
+    return;
+  }
+  v3 head_dir = vneg(V(cam.mat[2], cam.mat[5], cam.mat[8]));
+  uint32_t pixel_seed = seed + (uint32_t)w * (uint32_t)s->total_rays + (uint32_t)(s->ray_adr[c] + pixelid);
+  v3 hdr = V(0, 0, 0), albedo_sum = V(0, 0, 0), normal_sum = V(0, 0, 0), emission_sum = V(0, 0, 0);
+  float first_depth = 0.0f, lum_sq = 0.0f;
+  int n = st->path_samples;
+  int64_t adr = (int64_t)w * s->rgb_stride + s->rgb_adr[c] + pixelid;
+  for (int smp = 0; smp < n; ++smp) {
+    int sx = centre, sy = centre;
+    if (smp > 0) {
+      sx = (int)(pt_rand(pixel_seed, smp, PT_JITTER, 0) * (float)PT_SUBPIXEL);
+      sy = (int)(pt_rand(pixel_seed, smp, PT_JITTER, 1) * (float)PT_SUBPIXEL);
+    }
+    v3 dcam, ocam;
+    camera_frame_ray(&cam, W, H, px, py, PT_SUBPIXEL, sx, sy, &dcam, &ocam);
+    float max_dist = st->zfar > 0.0f ? st->zfar / maxf(-dcam.z, 1.0e-6f) : MAXVAL;
+    primary_t first;
+    v3 radiance =
+        trace_path(&ctx, vadd(cam.pos, mat_mul(cam.mat, ocam)), mat_mul(cam.mat, dcam), max_dist, head_dir, pixel_seed, smp, &first);
+    if (smp == 0) {
+      write_geometry(s, w, c, pixelid, &first.hit, dcam.z);
+      if (st->render_guides && s->guide_albedo) {
+        s->guide_albedo[adr * 3] = first.base_color.x;
+        s->guide_albedo[adr * 3 + 1] = first.base_color.y;
+        s->guide_albedo[adr * 3 + 2] = first.base_color.z;
+        s->guide_normal[adr * 3] = first.normal.x;
+        s->guide_normal[adr * 3 + 1] = first.normal.y;
+        s->guide_normal[adr * 3 + 2] = first.normal.z;
+      }
+      if (first.hit.geom != -1) first_depth = first.hit.dist * -dcam.z;
+    }
+    hdr = vadd(hdr, radiance);
+    albedo_sum = vadd(albedo_sum, first.albedo);
+    normal_sum = vadd(normal_sum, first.normal);
+    emission_sum = vadd(emission_sum, first.emission);
+    if (st->denoise) {
+      float lum = lum709(radiance) * ctx.exposure;
+      lum_sq += lum * lum;
+    }
+  }
+  float inv_n = 1.0f / (float)n;
+  hdr = vmul(hdr, inv_n);
+  if (st->denoise) {
+    /* denoise.py Features: albedo / normal at half precision, exposed emission, depth and the
+     * variance of the pixel's mean exposed luminance; then _demodulate (denoise.py:84-91). */
+    s->hdr_data[adr * 3] = hdr.x;
+    s->hdr_data[adr * 3 + 1] = hdr.y;
+    s->hdr_data[adr * 3 + 2] = hdr.z;
+    v3 em = vmul(emission_sum, ctx.exposure * inv_n);
+    v3 nm = normal_sum;
+    if (vdot(nm, nm) > 0.0f) nm = vnorm(nm);
+    guide_t g;
+    g.normal = round_half3(nm);
+    g.albedo = round_half3(vmul(albedo_sum, inv_n));
+    g.depth = first_depth;
+    store_guide(s->aov_guide + adr * 4, &g);
+    float* e = s->aov_emission + adr * 3;
+    e[0] = em.x, e[1] = em.y, e[2] = em.z;
+    float mean_lum = lum709(hdr) * ctx.exposure;
+    float variance = maxf(lum_sq * inv_n - mean_lum * mean_lum, 0.0f) * inv_n;
+    v3 c = vsub(vmul(hdr, ctx.exposure), em);
+    c = V(maxf(c.x, 0.0f) / maxf(g.albedo.x, MIN_ALBEDO), maxf(c.y, 0.0f) / maxf(g.albedo.y, MIN_ALBEDO),
+          maxf(c.z, 0.0f) / maxf(g.albedo.z, MIN_ALBEDO));
+    float scale = 1.0f / maxf(lum709(g.albedo), MIN_ALBEDO);
+    float* d = s->denoise_buffers[0] + adr * 4;
+    d[0] = c.x, d[1] = c.y, d[2] = c.z, d[3] = variance * scale * scale;
+    return;
+  }
+  if (st->render_hdr && s->hdr_data) {
+    s->hdr_data[adr * 3] = hdr.x;
+    s->hdr_data[adr * 3 + 1] = hdr.y;
+    s->hdr_data[adr * 3 + 2] = hdr.z;
+  }
+  s->rgb_data[adr] = encode_display(display_transform(vmul(hdr, ctx.exposure), st->tone_mapper));
+}
+
+/* ------------------------------------------------------------------ a-trous denoiser (denoise.py) */
+
+static float b3w(int i) { return i == 2 ? 0.375f : ((i == 1 || i == 3) ? 0.25f : 0.0625f); }
+
+/* One filter pass over one camera image of one world (denoise.py:101-178); step 0 copies. */
+static void atrous_image(const MjpbrScene* s, int64_t base, int W, int H, int step, const float* src, float* dst) {
+  const MjpbrSettings* st = &s->settings;
+  for (int py = 0; py < H; ++py) {
+    for (int px = 0; px < W; ++px) {
+      int64_t idx = base + (int64_t)py * W + px;
+      guide_t g0 = load_guide(s->aov_guide + idx * 4);
+      const float* s0 = src + idx * 4;
+      float* o = dst + idx * 4;
+      if (step == 0 || vdot(g0.normal, g0.normal) == 0.0f) {
+        memcpy(o, s0, 16);
+        continue;
+      }
+      float variance = 0.0f, variance_weight = 0.0f;
+      for (int j = 0; j < 3; ++j) {
+        int y = clampi(py + j - 1, 0, H - 1);
+        for (int i = 0; i < 3; ++i) {
+          int x = clampi(px + i - 1, 0, W - 1);
+          float g = (i == 1 ? 0.5f : 0.25f) * (j == 1 ? 0.5f : 0.25f);
+          variance += g * src[(base + (int64_t)y * W + x) * 4 + 3];
+          variance_weight += g;
+        }
+      }
+      float inv_sigma_l = 1.0f / (st->denoise_sigma_color * sqrtf(maxf(variance / variance_weight, 0.0f)) + 1.0e-6f);
+      float l0 = lum709(V(s0[0], s0[1], s0[2]));
+      float inv_sigma_a = 1.0f / st->denoise_sigma_albedo;
+      float inv_sigma_z = 1.0f / maxf(st->denoise_sigma_depth * g0.depth * (float)step, 1.0e-6f);
+      v3 total = V(0, 0, 0);
+      float total_variance = 0.0f, weight_sum = 0.0f;
+      for (int j = 0; j < 5; ++j) {
+        int y = py + (j - 2) * step;
+        if (y < 0 || y >= H) continue;
+        for (int i = 0; i < 5; ++i) {
+          int x = px + (i - 2) * step;
+          if (x < 0 || x >= W) continue;
+          int64_t q = base + (int64_t)y * W + x;
+          const float* sq = src + q * 4;
+          guide_t gq = load_guide(s->aov_guide + q * 4);
+          v3 c = V(sq[0], sq[1], sq[2]);
+          float wn = powf(maxf(vdot(g0.normal, gq.normal), 0.0f), st->denoise_sigma_normal);
+          float distance = fabsf(gq.depth - g0.depth) * inv_sigma_z + fabsf(lum709(c) - l0) * inv_sigma_l +
+                           vlen(vsub(gq.albedo, g0.albedo)) * inv_sigma_a;
+          float weight = b3w(i) * b3w(j) * wn * expf(-distance);
+          total = vadd(total, vmul(c, weight));
+          total_variance += weight * weight * sq[3];
+          weight_sum += weight;
+        }
+      }
+      v3 c = vdiv(total, weight_sum);
+      o[0] = c.x, o[1] = c.y, o[2] = c.z, o[3] = total_variance / (weight_sum * weight_sum);
+    }
+  }
+}
+
+/* Remodulation, tone mapping and encoding (denoise.py:181-201). */
+static void finish_image(const MjpbrScene* s, int w, int64_t base, int npix, const float* src) {
+  const MjpbrSettings* st = &s->settings;
+  float exposure = bf(s->exposure, w, 1, 0);
+  for (int64_t k = base; k < base + npix; ++k) {
+    guide_t g = load_guide(s->aov_guide + k * 4);
+    const float* c = src + k * 4;
+    const float* e = s->aov_emission + k * 3;
+    v3 exposed = V(e[0] + c[0] * maxf(g.albedo.x, MIN_ALBEDO), e[1] + c[1] * maxf(g.albedo.y, MIN_ALBEDO),
+                   e[2] + c[2] * maxf(g.albedo.z, MIN_ALBEDO));
+    if (st->render_hdr && s->hdr_data) {
+      v3 h = vdiv(exposed, exposure);
+      s->hdr_data[k * 3] = h.x, s->hdr_data[k * 3 + 1] = h.y, s->hdr_data[k * 3 + 2] = h.z;
+    }
+    s->rgb_data[k] = encode_display(display_transform(exposed, st->tone_mapper));
+  }
+}
+
 /* ------------------------------------------------------------------ exported */
 
 int oracle_nthreads(void) {
@@ -1692,9 +2199,8 @@ int oracle_nthreads(void) {
 #endif
 }
 
-/* Real-time tier of worlds [w0, w1) into the scene's (host) output buffers. mesh_nface: faces per
- * mesh (host). nthreads <= 0: all. */
-int oracle_render_rt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t seed, int w0, int w1, int nthreads) {
+static int render_worlds(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t seed, int w0, int w1, int nthreads,
+                         int path_traced) {
   if (!s || w0 < 0 || w1 > s->nworld || w0 > w1) return 1;
   int64_t nrow = 0;
   int row_cam[MJPBR_MAX_RENDER + 1];
@@ -1718,7 +2224,12 @@ int oracle_render_rt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t se
     while (c + 1 < s->nrender && r >= row_cam[c + 1]) ++c;
     if (!(s->render_rgb[c] || s->render_depth[c] || s->render_seg[c])) continue;
     int py = r - row_cam[c];
-    for (int px = 0; px < s->cam_res[c][0]; ++px) render_pixel(s, mesh_nface, w, c, px, py, seed);
+    for (int px = 0; px < s->cam_res[c][0]; ++px) {
+      if (path_traced)
+        render_pixel_pt(s, mesh_nface, w, c, px, py, seed);
+      else
+        render_pixel(s, mesh_nface, w, c, px, py, seed);
+    }
   }
   if (g_mesh_bvh) {
     for (int m = 0; m < g_mesh_bvh_count; ++m) {
@@ -1728,6 +2239,44 @@ int oracle_render_rt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t se
     free(g_mesh_bvh);
     g_mesh_bvh = NULL;
     g_mesh_bvh_count = 0;
+  }
+  return 0;
+}
+
+/* Real-time tier of worlds [w0, w1) into the scene's (host) output buffers. mesh_nface: faces per
+ * mesh (host). nthreads <= 0: all. */
+int oracle_render_rt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t seed, int w0, int w1, int nthreads) {
+  return render_worlds(s, mesh_nface, seed, w0, w1, nthreads, 0);
+}
+
+/* Path-traced tier of worlds [w0, w1): RGB (or, with settings.denoise, the noisy HDR and the
+ * denoiser's features), depth and segmentation. */
+int oracle_render_pt(const MjpbrScene* s, const int32_t* mesh_nface, uint32_t seed, int w0, int w1, int nthreads) {
+  return render_worlds(s, mesh_nface, seed, w0, w1, nthreads, 1);
+}
+
+/* The a-trous denoiser over every world and RGB camera: reads denoise_buffers[0] (demodulated
+ * radiance + variance, written by oracle_render_pt), aov_guide and aov_emission; ping-pongs
+ * through both denoise buffers; writes rgb_data (and hdr_data with render_hdr). */
+int oracle_denoise(const MjpbrScene* s, int nthreads) {
+  if (!s || !s->aov_guide || !s->aov_emission || !s->denoise_buffers[0] || !s->denoise_buffers[1]) return 1;
+  int passes = s->denoise_iterations;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int w = 0; w < s->nworld; ++w) {
+    for (int c = 0; c < s->nrender; ++c) {
+      if (!s->render_rgb[c] || s->rgb_adr[c] < 0) continue;
+      int W = s->cam_res[c][0], H = s->cam_res[c][1];
+      int64_t base = (int64_t)w * s->rgb_stride + s->rgb_adr[c];
+      int cur = 0;
+      for (int i = 0; i < passes; ++i) {
+        atrous_image(s, base, W, H, 1 << i, s->denoise_buffers[cur], s->denoise_buffers[1 - cur]);
+        cur = 1 - cur;
+      }
+      finish_image(s, w, base, W * H, s->denoise_buffers[cur]);
+    }
   }
   return 0;
 }

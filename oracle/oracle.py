@@ -1,7 +1,7 @@
 """Python side of the CPU oracle (oracle/mjpbr_oracle.c) — TEST INFRASTRUCTURE ONLY.
 
 Builds the same MjpbrScene descriptor the library renders from, but over host (numpy) arrays,
-and runs the C restatement of the reference's real-time tier on the CPU cores. The tables the GPU
+and runs the C restatement of the reference's real-time and path-traced tiers on the CPU cores. The tables the GPU
 computes at context creation (DFG table, texture mips, prefiltered environment stacks) come from
 the oracle's own C functions unless the caller passes the GPU's copies (to isolate the render
 kernel from the table kernels, which tests compare separately).
@@ -51,6 +51,10 @@ def load() -> ctypes.CDLL:
     vp, i32 = ctypes.c_void_p, ctypes.c_int
     lib.oracle_render_rt.argtypes = [ctypes.POINTER(_lib.Scene), vp, ctypes.c_uint32, i32, i32, i32]
     lib.oracle_render_rt.restype = i32
+    lib.oracle_render_pt.argtypes = [ctypes.POINTER(_lib.Scene), vp, ctypes.c_uint32, i32, i32, i32]
+    lib.oracle_render_pt.restype = i32
+    lib.oracle_denoise.argtypes = [ctypes.POINTER(_lib.Scene), i32]
+    lib.oracle_denoise.restype = i32
     lib.oracle_dfg_lut.argtypes = [vp, i32, i32]
     lib.oracle_build_mips.argtypes = [ctypes.POINTER(_lib.Texture), vp]
     lib.oracle_prefilter.argtypes = [ctypes.POINTER(_lib.Texture), vp, i32, i32, i32, i32, vp]
@@ -184,6 +188,13 @@ class OracleScene:
     self.hdr = np.zeros((nw, rgb_stride, 3), f32)
     self.albedo = np.zeros((nw, rgb_stride, 3), f32)
     self.normal = np.zeros((nw, rgb_stride, 3), f32)
+    aov_pix = rgb_stride if st.get("denoise") else 1
+    self.aov = {
+      "guide": np.zeros((nw, aov_pix, 4), np.uint32),
+      "emission": np.zeros((nw, aov_pix, 3), f32),
+      "demod": np.zeros((nw, aov_pix, 4), f32),
+      "pong": np.zeros((nw, aov_pix, 4), f32),
+    }
     self.dfg = np.ascontiguousarray(tables.get("dfg_lut", None) if "dfg_lut" in tables else dfg_lut())
     a.update(
       {
@@ -214,6 +225,10 @@ class OracleScene:
         "hdr_data": self.hdr,
         "guide_albedo": self.albedo,
         "guide_normal": self.normal,
+        "aov_guide": self.aov["guide"],
+        "aov_emission": self.aov["emission"],
+        "denoise_buffers": (self.aov["demod"], self.aov["pong"]),
+        "denoise_iterations": int(options.get("denoise_iterations", 3)),
         "nbvh_geom": len(self.hc.enabled_geom_ids),
         "nnode": self.hc.tlas_child.shape[1],
         "enabled_geom_ids": np.ascontiguousarray(self.hc.enabled_geom_ids, i32),
@@ -254,12 +269,26 @@ class OracleScene:
     self.arrays = a  # keeps every array alive
     self.scene = _scene.fill_scene({k: v for k, v in a.items() if v is not None})
 
-  def render(self, seed: int = 0, worlds: tuple[int, int] | None = None, nthreads: int = 0) -> dict[str, np.ndarray]:
+  def render(self, seed: int = 0, worlds: tuple[int, int] | None = None, nthreads: int = 0, denoise: bool = True) -> dict[str, np.ndarray]:
+    """Renders worlds [w0, w1) with the tier of the context's settings (real-time or path-traced);
+    with settings.denoise the a-trous filter then runs over every world (unless denoise=False)."""
     w0, w1 = worlds if worlds is not None else (0, self.nworld)
-    status = load().oracle_render_rt(self.scene, self.mesh_nface.ctypes.data if len(self.mesh_nface) else None, seed & 0xFFFFFFFF, w0, w1, nthreads)
+    lib = load()
+    fn = lib.oracle_render_pt if self.hc.settings["tier"] == 1 else lib.oracle_render_rt
+    status = fn(self.scene, self.mesh_nface.ctypes.data if len(self.mesh_nface) else None, seed & 0xFFFFFFFF, w0, w1, nthreads)
     if status != 0:
-      raise RuntimeError("oracle_render_rt failed")
-    return {"rgb": self.rgb, "depth": self.depth, "seg": self.seg, "hdr": self.hdr, "albedo": self.albedo, "normal": self.normal}
+      raise RuntimeError("oracle render failed")
+    out = {"rgb": self.rgb, "depth": self.depth, "seg": self.seg, "hdr": self.hdr, "albedo": self.albedo, "normal": self.normal}
+    if self.hc.settings["tier"] == 1 and self.hc.settings["denoise"]:
+      out.update({f"aov_{k}": v.copy() for k, v in self.aov.items()})
+      if denoise:
+        self.denoise(nthreads)
+    return out
+
+  def denoise(self, nthreads: int = 0) -> None:
+    """Runs the oracle's a-trous filter on the current demodulated buffer and guide arrays."""
+    if load().oracle_denoise(self.scene, nthreads) != 0:
+      raise RuntimeError("oracle_denoise failed")
 
 
 def unpack_rgb(rgb: np.ndarray) -> np.ndarray:
