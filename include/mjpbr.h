@@ -316,6 +316,16 @@ int mjpbr_refit_bvh(const MjpbrScene* scene, void* stream);
  * mjpbr_refit_bvh first whenever geometry or cameras moved. */
 int mjpbr_render(const MjpbrScene* scene, uint32_t seed, void* stream);
 
+/* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
+ * caller: the per-world blocks and the path tracer's work counter live in static device memory of
+ * the library (scene->world_blocks and scene->work_counter are ignored). For hosts that cannot
+ * give the library device memory after start-up (a fixed device-memory arena, a plugin host that
+ * owns every allocation). Limit: nworld * world_block_floats <= 4,194,304 (16 MiB), else
+ * MJPBR_ERR_ARG. Calls overlapping in time share the static memory and race. The first call on a
+ * device looks the memory up; make it before any stream capture. No counterpart in the
+ * reference. */
+int mjpbr_refit_render_static(const MjpbrScene* scene, uint32_t seed, void* stream);
+
 /* Display RGB in [0, 1] of rendering camera `cam` into out (nworld_out, H, W, 3) float32.
  * mujoco_warp_pbr/_src/output.py:34-38. */
 int mjpbr_get_rgb(const MjpbrScene* scene, int32_t cam, float* out, int32_t nworld_out, void* stream);

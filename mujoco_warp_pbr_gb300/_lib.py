@@ -253,6 +253,7 @@ _SIGNATURES = {
   "mjpbr_world_block_floats": (c_i32, [c_i32, c_i32, c_i32, c_i32]),
   "mjpbr_refit_bvh": (ctypes.c_int, [ctypes.POINTER(Scene), c_vp]),
   "mjpbr_render": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),
+  "mjpbr_refit_render_static": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),
   "mjpbr_get_rgb": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),
   "mjpbr_get_depth": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_f32, c_vp, c_i32, c_vp]),
   "mjpbr_get_segmentation": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),

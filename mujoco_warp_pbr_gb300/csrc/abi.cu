@@ -34,6 +34,8 @@ namespace {
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+}  // namespace
+
 int validate_scene(const MjpbrScene* s, bool need_outputs) {
   if (!s) return set_error(MJPBR_ERR_ARG, "scene is NULL");
   if (s->abi_version != MJPBR_ABI_VERSION) {
@@ -94,7 +96,6 @@ int validate_scene(const MjpbrScene* s, bool need_outputs) {
   return MJPBR_OK;
 }
 
-}  // namespace
 }  // namespace mjpbr
 
 using namespace mjpbr;

@@ -12,6 +12,9 @@ int set_error(int code, const char* fmt, ...);
 // MJPBR_OK, or MJPBR_ERR_CUDA with the launch error of the last kernel.
 int check_launch(const char* what);
 
+// MJPBR_OK, or MJPBR_ERR_ARG with a message naming the first inconsistent field of the scene.
+int validate_scene(const MjpbrScene* s, bool need_outputs);
+
 int refit_launch(const MjpbrScene& s, cudaStream_t stream);
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
 int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
