@@ -21,6 +21,7 @@ from mujoco_warp_pbr_gb300.output import get_hdr as get_hdr
 from mujoco_warp_pbr_gb300.output import get_normal as get_normal
 from mujoco_warp_pbr_gb300.output import get_rgb as get_rgb
 from mujoco_warp_pbr_gb300.output import get_segmentation as get_segmentation
+from mujoco_warp_pbr_gb300.rays import set_camera_rays as set_camera_rays
 from mujoco_warp_pbr_gb300.render import check_errors as check_errors
 from mujoco_warp_pbr_gb300.render import denoise as denoise
 from mujoco_warp_pbr_gb300.render import refit_bvh as refit_bvh

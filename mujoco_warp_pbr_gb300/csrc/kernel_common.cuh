@@ -51,6 +51,129 @@ MJ_DEV void camera_frame_ray(const Pixel& p, int32_t n, int32_t sx, int32_t sy, 
   *ocam = v3(0.0f);
 }
 
+// ---------------------------------------------------------------- per-pixel ray bundles
+// (camera.py:195-296): each pixel of a bundle camera has its own camera-frame ray (rays.py); a
+// sub-pixel sample interpolates its four nearest bundle rays, on the image plane z = -1 when all
+// four point forward (exact for pinhole bundles), else on the sphere; a zero direction is a pixel
+// without a ray.
+
+// Bundle rays x0, x1 and weight t of sample i of n along an axis of nb bundle rays: the sample
+// sits at bundle coordinate (i + 0.5) nb / n - 0.5 = num / den, in integers so that t is exactly 0
+// on a bundle pixel centre.
+MJ_DEV void bundle_axis(int32_t i, int32_t n, int32_t nb, int32_t* x0, int32_t* x1, float* t) {
+  const int64_t num = (int64_t)(2 * i + 1) * nb - n;
+  const int64_t den = 2 * (int64_t)n;
+  int32_t a = (int32_t)((num + den) / den) - 1;  // num + den > 0
+  a = min(max(a, 0), max(nb - 2, 0));
+  *x0 = a;
+  *x1 = min(a + 1, nb - 1);
+  *t = (float)(num - (int64_t)a * den) / (float)den;
+}
+
+MJ_DEV V3 ray_vec(const float* a, int64_t i) { return V3{a[i * 3], a[i * 3 + 1], a[i * 3 + 2]}; }
+MJ_DEV V3 lerp3(V3 a, V3 b, float t) { return a + (b - a) * t; }
+
+// Camera-frame (direction, origin) of the bundle ray through sub-pixel cell (sx, sy) of n x n.
+MJ_DEV void bundle_ray(const MjpbrScene& s, const Pixel& p, int32_t n, int32_t sx, int32_t sy, V3* dcam, V3* ocam) {
+  const int32_t rw = s.bundle_res[p.cam][0], rh = s.bundle_res[p.cam][1];
+  const int64_t adr = s.ray_adr[p.cam];
+  int32_t x0, x1, y0, y1;
+  float tx, ty;
+  bundle_axis(p.px * n + sx, p.width * n, rw, &x0, &x1, &tx);
+  bundle_axis(p.py * n + sy, p.height * n, rh, &y0, &y1, &ty);
+  const int64_t r0 = adr + (int64_t)y0 * rw, r1 = adr + (int64_t)y1 * rw;
+  V3 d00 = ray_vec(s.ray_direction, r0 + x0), d10 = ray_vec(s.ray_direction, r0 + x1);
+  V3 d01 = ray_vec(s.ray_direction, r1 + x0), d11 = ray_vec(s.ray_direction, r1 + x1);
+  if (length_sq(d00) == 0.0f || length_sq(d10) == 0.0f || length_sq(d01) == 0.0f || length_sq(d11) == 0.0f) {
+    // next to a pixel without a ray: the nearest bundle ray, no interpolation
+    const int64_t nearest = (ty < 0.5f ? r0 : r1) + (tx < 0.5f ? x0 : x1);
+    V3 d = ray_vec(s.ray_direction, nearest);
+    if (length_sq(d) > 0.0f) d = normalize(d);
+    *dcam = d;
+    *ocam = ray_vec(s.ray_origin, nearest);
+    return;
+  }
+  const V3 o00 = ray_vec(s.ray_origin, r0 + x0), o10 = ray_vec(s.ray_origin, r0 + x1);
+  const V3 o01 = ray_vec(s.ray_origin, r1 + x0), o11 = ray_vec(s.ray_origin, r1 + x1);
+  if (d00.z < 0.0f && d10.z < 0.0f && d01.z < 0.0f && d11.z < 0.0f) {
+    d00 = d00 * (-1.0f / d00.z);
+    d10 = d10 * (-1.0f / d10.z);
+    d01 = d01 * (-1.0f / d01.z);
+    d11 = d11 * (-1.0f / d11.z);
+  }
+  V3 d = lerp3(lerp3(d00, d10, tx), lerp3(d01, d11, tx), ty);
+  if (length_sq(d) > 0.0f) d = normalize(d);
+  *dcam = d;
+  *ocam = lerp3(lerp3(o00, o10, tx), lerp3(o01, o11, tx), ty);
+}
+
+// (angle, distance) between bundle rays a and b, or between b and its linear extrapolation.
+MJ_DEV void bundle_step(const MjpbrScene& s, int64_t a, int64_t b, bool extrapolate, float* spread, float* width) {
+  V3 da = ray_vec(s.ray_direction, a), db = ray_vec(s.ray_direction, b);
+  *spread = 0.0f;
+  *width = 0.0f;
+  if (length_sq(da) == 0.0f || length_sq(db) == 0.0f) return;
+  da = normalize(da);
+  db = normalize(db);
+  *width = length(ray_vec(s.ray_origin, b) - ray_vec(s.ray_origin, a));
+  if (!extrapolate) {
+    *spread = length(db - da);
+  } else if (da.z < 0.0f && db.z < 0.0f) {
+    *spread = length(normalize(db * (-2.0f / db.z) + da * (1.0f / da.z)) - db);
+  } else {
+    *spread = length(normalize(db * 2.0f - da) - db);
+  }
+}
+
+// Camera-frame ray of sub-pixel cell (sx, sy) of n x n (camera.py:300-330): direction, origin,
+// the maximum hit distance (zfar: planar for projections, along the ray for bundles; 0 for a
+// bundle pixel without a ray) and the z of the depth axis (depth = distance * -depth_z).
+MJ_DEV void primary_ray(const MjpbrScene& s, const Pixel& p, int32_t n, int32_t sx, int32_t sy, V3* dcam, V3* ocam,
+                        float* max_dist, float* depth_z) {
+  const float zfar = s.settings.zfar;
+  if (s.ray_direction) {
+    bundle_ray(s, p, n, sx, sy, dcam, ocam);
+    *max_dist = zfar > 0.0f ? zfar : kMaxVal;
+    if (length_sq(*dcam) == 0.0f) {
+      *max_dist = 0.0f;
+      *dcam = V3{0.0f, 0.0f, -1.0f};
+    }
+    *depth_z = -1.0f;
+    return;
+  }
+  camera_frame_ray(p, n, sx, sy, dcam, ocam);
+  *max_dist = zfar > 0.0f ? zfar / fmaxf(-dcam->z, 1.0e-6f) : kMaxVal;
+  *depth_z = dcam->z;
+}
+
+// Angular spread and width (orthographic origins) of one pixel, the ray-cone parameters
+// (camera.py:322-347): the difference to the next pixel's ray along x (for bundles, to the next
+// bundle ray, or the extrapolation of the previous one in the last column).
+MJ_DEV void pixel_cone(const MjpbrScene& s, const Pixel& p, float* spread, float* width) {
+  if (s.ray_direction) {
+    const int32_t rw = s.bundle_res[p.cam][0], rh = s.bundle_res[p.cam][1];
+    *spread = 0.0f;
+    *width = 0.0f;
+    if (rw < 2) return;
+    const int32_t bx = (p.px * rw) / p.width;
+    const int64_t b = s.ray_adr[p.cam] + (int64_t)((p.py * rh) / p.height) * rw + bx;
+    if (bx + 1 < rw) {
+      bundle_step(s, b, b + 1, false, spread, width);
+    } else {
+      bundle_step(s, b - 1, b, true, spread, width);
+    }
+    const float scale = (float)rw / (float)p.width;
+    *spread *= scale;
+    *width *= scale;
+    return;
+  }
+  V3 d0, o0, d1, o1;
+  camera_frame_ray(p, 1, 0, 0, &d0, &o0);
+  camera_frame_ray(p, 1, 1, 0, &d1, &o1);
+  *spread = length(d1 - d0);
+  *width = length(o1 - o0);
+}
+
 MJ_DEV M3 cam_mat(const float* c) {
   M3 m;
 #pragma unroll

@@ -24,7 +24,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kTile = 32;
 constexpr int kTilePixels = kTile * kTile;
-constexpr float kMinForward = 1.0e-6f;
 
 struct PtTiles {
   int32_t ncam;
@@ -225,7 +224,7 @@ struct Pt {
   }
 };
 
-MJ_DEV void start_sample(PathState& ps, const Pixel& p, const MjpbrSettings& st, uint32_t seed, const M3& R, V3 cpos,
+MJ_DEV void start_sample(PathState& ps, const MjpbrScene& s, const Pixel& p, uint32_t seed, const M3& R, V3 cpos,
                          int32_t sample) {
   int32_t sx = kSubpixel / 2, sy = kSubpixel / 2;
   if (sample > 0) {
@@ -233,9 +232,7 @@ MJ_DEV void start_sample(PathState& ps, const Pixel& p, const MjpbrSettings& st,
     sy = (int32_t)(pt_rand(seed, sample, kJitterDepth, 1) * (float)kSubpixel);
   }
   V3 dcam, ocam;
-  camera_frame_ray(p, kSubpixel, sx, sy, &dcam, &ocam);
-  ps.max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
-  ps.dcam_z = dcam.z;
+  primary_ray(s, p, kSubpixel, sx, sy, &dcam, &ocam, &ps.max_dist, &ps.dcam_z);
   ps.o = cpos + mul(R, ocam);
   ps.d = mul(R, dcam);
   ps.beta = v3(1.0f);
@@ -321,17 +318,17 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
               if (!want_rgb) {
                 // depth / segmentation only: the centre of the 15 x 15 grid
                 V3 dcam, ocam;
-                camera_frame_ray(p, kSubpixel, kSubpixel / 2, kSubpixel / 2, &dcam, &ocam);
-                float max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
+                float max_dist, depth_z;
+                primary_ray(s, p, kSubpixel, kSubpixel / 2, kSubpixel / 2, &dcam, &ocam, &max_dist, &depth_z);
                 Hit hit = Pt<kMesh, kTex>::trace(c, cpos + mul(R, ocam), mul(R, dcam), max_dist, false);
-                write_geometry(s, w, p, hit, dcam.z);
+                write_geometry(s, w, p, hit, depth_z);
               } else {
                 pixel_seed = seed + (uint32_t)w * (uint32_t)s.total_rays + (uint32_t)(s.ray_adr[cam] + p.pixelid);
                 acc.hdr = acc.albedo = acc.normal = acc.emission = v3(0.0f);
                 acc.lum_sq = 0.0f;
                 acc.first_depth = 0.0f;
                 acc.guide_albedo = acc.guide_normal = v3(0.0f);
-                start_sample(ps, p, st, pixel_seed, R, cpos, 0);
+                start_sample(ps, s, p, pixel_seed, R, cpos, 0);
                 has_pixel = true;
               }
             }
@@ -355,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
         acc.lum_sq += lum * lum;
       }
       if (ps.sample + 1 < nsample) {
-        start_sample(ps, p, st, pixel_seed, R, cpos, ps.sample + 1);
+        start_sample(ps, s, p, pixel_seed, R, cpos, ps.sample + 1);
         continue;
       }
       // the pixel's last sample: write it

@@ -23,7 +23,6 @@ constexpr int kThreads = 256;
 #endif
 constexpr float kMinThroughput = 1.0f / 255.0f;
 constexpr float kMinTexels = 1.0e-8f;
-constexpr float kMinForward = 1.0e-6f;
 
 template <bool kMesh, bool kTex>
 struct Rt {
@@ -270,30 +269,18 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
     c.st.t = reinterpret_cast<float*>(stack_base + kThreads * kStackDepth) + threadIdx.x;
     c.st.stride = kThreads;
   }
-  c.L = L;
-  c.w = w;
-  c.err = 0;
-  c.exposure = bf(s.exposure, w, 1, 0);
-  c.ambient = bv3(s.ambient_radiance, w, 1, 0);
-  c.env = 0;
-  c.env_yaw = 0.0f;
-  c.env_scale = 0.0f;
-  if (kTex && s.nenv > 0) {
-    c.env = bi(s.env_id, w, 1, 0);
-    c.env_yaw = bf(s.env_yaw, w, 1, 0);
-    c.env_scale = bf(s.env_intensity, w, 1, 0);
-  }
+  init_ctx(c, s, blk, L, w, kTex);
   const M3 R = cam_mat(p.rec);
   const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
   const bool cull = st.cull_backfaces != 0;
 
   if (!want_rgb) {
     V3 dcam, ocam;
-    camera_frame_ray(p, 1, 0, 0, &dcam, &ocam);
-    float max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
+    float max_dist, depth_z;
+    primary_ray(s, p, 1, 0, 0, &dcam, &ocam, &max_dist, &depth_z);
     Ray ray{cpos + mul(R, ocam), mul(R, dcam)};
     Hit hit = trace_ray<kMesh>(s, c.st, blk, L, ray, max_dist, cull, false, &c.err);
-    write_geometry(s, w, p, hit, dcam.z);
+    write_geometry(s, w, p, hit, depth_z);
     if (c.err && s.error_word) atomicOr(s.error_word, c.err);
     return;
   }
@@ -301,13 +288,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   const int32_t n = st.samples_per_axis;
   const float inv_n = 1.0f / (float)n;
   float pixel_spread, pixel_width;
-  {
-    V3 d0, o0, d1, o1;
-    camera_frame_ray(p, 1, 0, 0, &d0, &o0);
-    camera_frame_ray(p, 1, 1, 0, &d1, &o1);
-    pixel_spread = length(d1 - d0);
-    pixel_width = length(o1 - o0);
-  }
+  pixel_cone(s, p, &pixel_spread, &pixel_width);
   const float spread = pixel_spread * inv_n, width = pixel_width * inv_n;
   const V3 head_dir = -V3{R.m[2], R.m[5], R.m[8]};
   const uint32_t pixel_seed = seed + (uint32_t)w * (uint32_t)s.total_rays + (uint32_t)(s.ray_adr[cam] + p.pixelid);
@@ -315,8 +296,8 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   V3 display = v3(0.0f), hdr = v3(0.0f);
   for (int32_t smp = 0; smp < n * n; ++smp) {
     V3 dcam, ocam;
-    camera_frame_ray(p, n, smp % n, smp / n, &dcam, &ocam);
-    float max_dist = st.zfar > 0.0f ? st.zfar / fmaxf(-dcam.z, kMinForward) : kMaxVal;
+    float max_dist, depth_z;
+    primary_ray(s, p, n, smp % n, smp / n, &dcam, &ocam, &max_dist, &depth_z);
     V3 origin = cpos + mul(R, ocam);
     V3 dir = mul(R, dcam);
     Hit first;
@@ -324,7 +305,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
     V3 radiance = Rt<kMesh, kTex>::trace_pixel(c, origin, dir, max_dist, width, spread, head_dir, pixel_seed, 2 * smp,
                                                &first, &albedo, &gnormal);
     if (smp == 0) {
-      write_geometry(s, w, p, first, dcam.z);
+      write_geometry(s, w, p, first, depth_z);
       if (st.render_guides && s.guide_albedo) {
         int64_t a = ((int64_t)w * s.rgb_stride + s.rgb_adr[cam] + p.pixelid) * 3;
         V3 al = first.geom != -1 ? albedo : v3(0.0f), nm = first.geom != -1 ? gnormal : v3(0.0f);

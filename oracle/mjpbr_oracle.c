@@ -1601,6 +1601,112 @@ static void camera_frame_ray(const cam_t* cam, int W, int H, int px, int py, int
   *ocam = V(0, 0, 0);
 }
 
+/* Per-pixel ray bundles (camera.py:195-330, rays.py): bilinear interpolation of the four nearest
+ * bundle rays, on the image plane z = -1 when all point forward, else on the sphere. */
+static void bundle_axis(int i, int n, int nb, int* x0, int* x1, float* t) {
+  int64_t num = (int64_t)(2 * i + 1) * nb - n, den = 2 * (int64_t)n;
+  int a = (int)((num + den) / den) - 1;
+  int hi = nb - 2 > 0 ? nb - 2 : 0;
+  a = a < 0 ? 0 : (a > hi ? hi : a);
+  *x0 = a;
+  *x1 = a + 1 < nb - 1 ? a + 1 : nb - 1;
+  *t = (float)(num - (int64_t)a * den) / (float)den;
+}
+
+static v3 rvec(const float* a, int64_t i) { return V(a[i * 3], a[i * 3 + 1], a[i * 3 + 2]); }
+static v3 vlerp(v3 a, v3 b, float t) { return vadd(a, vmul(vsub(b, a), t)); }
+
+static void bundle_ray(const MjpbrScene* s, int c, int W, int H, int px, int py, int n, int sx, int sy, v3* dcam, v3* ocam) {
+  int rw = s->bundle_res[c][0], rh = s->bundle_res[c][1];
+  int64_t adr = s->ray_adr[c];
+  int x0, x1, y0, y1;
+  float tx, ty;
+  bundle_axis(px * n + sx, W * n, rw, &x0, &x1, &tx);
+  bundle_axis(py * n + sy, H * n, rh, &y0, &y1, &ty);
+  int64_t r0 = adr + (int64_t)y0 * rw, r1 = adr + (int64_t)y1 * rw;
+  v3 d00 = rvec(s->ray_direction, r0 + x0), d10 = rvec(s->ray_direction, r0 + x1);
+  v3 d01 = rvec(s->ray_direction, r1 + x0), d11 = rvec(s->ray_direction, r1 + x1);
+  if (vdot(d00, d00) == 0.0f || vdot(d10, d10) == 0.0f || vdot(d01, d01) == 0.0f || vdot(d11, d11) == 0.0f) {
+    int64_t nearest = (ty < 0.5f ? r0 : r1) + (tx < 0.5f ? x0 : x1);
+    v3 d = rvec(s->ray_direction, nearest);
+    if (vdot(d, d) > 0.0f) d = vnorm(d);
+    *dcam = d;
+    *ocam = rvec(s->ray_origin, nearest);
+    return;
+  }
+  v3 o00 = rvec(s->ray_origin, r0 + x0), o10 = rvec(s->ray_origin, r0 + x1);
+  v3 o01 = rvec(s->ray_origin, r1 + x0), o11 = rvec(s->ray_origin, r1 + x1);
+  if (d00.z < 0.0f && d10.z < 0.0f && d01.z < 0.0f && d11.z < 0.0f) {
+    d00 = vmul(d00, -1.0f / d00.z);
+    d10 = vmul(d10, -1.0f / d10.z);
+    d01 = vmul(d01, -1.0f / d01.z);
+    d11 = vmul(d11, -1.0f / d11.z);
+  }
+  v3 d = vlerp(vlerp(d00, d10, tx), vlerp(d01, d11, tx), ty);
+  if (vdot(d, d) > 0.0f) d = vnorm(d);
+  *dcam = d;
+  *ocam = vlerp(vlerp(o00, o10, tx), vlerp(o01, o11, tx), ty);
+}
+
+static void bundle_step(const MjpbrScene* s, int64_t a, int64_t b, int extrapolate, float* spread, float* width) {
+  v3 da = rvec(s->ray_direction, a), db = rvec(s->ray_direction, b);
+  *spread = 0.0f;
+  *width = 0.0f;
+  if (vdot(da, da) == 0.0f || vdot(db, db) == 0.0f) return;
+  da = vnorm(da);
+  db = vnorm(db);
+  *width = vlen(vsub(rvec(s->ray_origin, b), rvec(s->ray_origin, a)));
+  if (!extrapolate)
+    *spread = vlen(vsub(db, da));
+  else if (da.z < 0.0f && db.z < 0.0f)
+    *spread = vlen(vsub(vnorm(vadd(vmul(db, -2.0f / db.z), vmul(da, 1.0f / da.z))), db));
+  else
+    *spread = vlen(vsub(vnorm(vsub(vmul(db, 2.0f), da)), db));
+}
+
+/* Camera-frame ray of sub-pixel cell (sx, sy) of n x n, its maximum distance and depth axis z. */
+static void primary_ray(const MjpbrScene* s, const cam_t* cam, int c, int W, int H, int px, int py, int n, int sx, int sy,
+                        v3* dcam, v3* ocam, float* max_dist, float* depth_z) {
+  float zfar = s->settings.zfar;
+  if (s->ray_direction) {
+    bundle_ray(s, c, W, H, px, py, n, sx, sy, dcam, ocam);
+    *max_dist = zfar > 0.0f ? zfar : MAXVAL;
+    if (vdot(*dcam, *dcam) == 0.0f) {
+      *max_dist = 0.0f;
+      *dcam = V(0.0f, 0.0f, -1.0f);
+    }
+    *depth_z = -1.0f;
+    return;
+  }
+  camera_frame_ray(cam, W, H, px, py, n, sx, sy, dcam, ocam);
+  *max_dist = zfar > 0.0f ? zfar / maxf(-dcam->z, 1.0e-6f) : MAXVAL;
+  *depth_z = dcam->z;
+}
+
+static void pixel_cone(const MjpbrScene* s, const cam_t* cam, int c, int W, int H, int px, int py, float* spread, float* width) {
+  if (s->ray_direction) {
+    int rw = s->bundle_res[c][0], rh = s->bundle_res[c][1];
+    *spread = 0.0f;
+    *width = 0.0f;
+    if (rw < 2) return;
+    int bx = (px * rw) / W;
+    int64_t b = s->ray_adr[c] + (int64_t)((py * rh) / H) * rw + bx;
+    if (bx + 1 < rw)
+      bundle_step(s, b, b + 1, 0, spread, width);
+    else
+      bundle_step(s, b - 1, b, 1, spread, width);
+    float scale = (float)rw / (float)W;
+    *spread *= scale;
+    *width *= scale;
+    return;
+  }
+  v3 d0, o0, d1, o1;
+  camera_frame_ray(cam, W, H, px, py, 1, 0, 0, &d0, &o0);
+  camera_frame_ray(cam, W, H, px, py, 1, 1, 0, &d1, &o1);
+  *spread = vlen(vsub(d1, d0));
+  *width = vlen(vsub(o1, o0));
+}
+
 static void write_geometry(const MjpbrScene* s, int w, int c, int pixelid, const hit_t* hit, float dcam_z) {
   if (s->render_seg[c]) {
     int32_t* o = s->seg_data + ((int64_t)w * s->seg_stride + s->seg_adr[c] + pixelid) * 2;
@@ -1634,32 +1740,32 @@ static void render_pixel(const MjpbrScene* s, const int32_t* mesh_nface, int w, 
   int cull = st->cull_backfaces;
   if (!s->render_rgb[c]) {
     v3 dcam, ocam;
-    camera_frame_ray(&cam, W, H, px, py, 1, 0, 0, &dcam, &ocam);
-    float max_dist = st->zfar > 0.0f ? st->zfar / maxf(-dcam.z, 1.0e-6f) : MAXVAL;
+    float max_dist, depth_z;
+    primary_ray(s, &cam, c, W, H, px, py, 1, 0, 0, &dcam, &ocam, &max_dist, &depth_z);
     hit_t hit = closest(&ctx.W, vadd(cam.pos, mat_mul(cam.mat, ocam)), mat_mul(cam.mat, dcam), max_dist, cull);
-    write_geometry(s, w, c, pixelid, &hit, dcam.z);
+    write_geometry(s, w, c, pixelid, &hit, depth_z);
     return;
   }
   int n = st->samples_per_axis;
   float inv_n = 1.0f / (float)n;
-  v3 d0, o0, d1, o1;
-  camera_frame_ray(&cam, W, H, px, py, 1, 0, 0, &d0, &o0);
-  camera_frame_ray(&cam, W, H, px, py, 1, 1, 0, &d1, &o1);
-  float spread = vlen(vsub(d1, d0)) * inv_n, width = vlen(vsub(o1, o0)) * inv_n;
+  float spread, width;
+  pixel_cone(s, &cam, c, W, H, px, py, &spread, &width);
+  spread *= inv_n;
+  width *= inv_n;
   v3 head_dir = vneg(V(cam.mat[2], cam.mat[5], cam.mat[8]));
   uint32_t pixel_seed = seed + (uint32_t)w * (uint32_t)s->total_rays + (uint32_t)(s->ray_adr[c] + pixelid);
   v3 display = V(0, 0, 0), hdr = V(0, 0, 0);
   for (int smp = 0; smp < n * n; ++smp) {
     v3 dcam, ocam;
-    camera_frame_ray(&cam, W, H, px, py, n, smp % n, smp / n, &dcam, &ocam);
-    float max_dist = st->zfar > 0.0f ? st->zfar / maxf(-dcam.z, 1.0e-6f) : MAXVAL;
+    float max_dist, depth_z;
+    primary_ray(s, &cam, c, W, H, px, py, n, smp % n, smp / n, &dcam, &ocam, &max_dist, &depth_z);
     v3 origin = vadd(cam.pos, mat_mul(cam.mat, ocam));
     v3 dir = mat_mul(cam.mat, dcam);
     hit_t first;
     v3 albedo = V(0, 0, 0), gnormal = V(0, 0, 0);
     v3 radiance = trace_pixel(&ctx, origin, dir, max_dist, width, spread, head_dir, pixel_seed, 2 * smp, &first, &albedo, &gnormal);
     if (smp == 0) {
-      write_geometry(s, w, c, pixelid, &first, dcam.z);
+      write_geometry(s, w, c, pixelid, &first, depth_z);
       if (st->render_guides && s->guide_albedo) {
         int64_t a = ((int64_t)w * s->rgb_stride + s->rgb_adr[c] + pixelid) * 3;
         v3 al = first.geom != -1 ? albedo : V(0, 0, 0), nm = first.geom != -1 ? gnormal : V(0, 0, 0);
@@ -2032,10 +2138,10 @@ static void render_pixel_pt(const MjpbrScene* s, const int32_t* mesh_nface, int 
   const int centre = PT_SUBPIXEL / 2;
   if (!s->render_rgb[c]) {
     v3 dcam, ocam;
-    camera_frame_ray(&cam, W, H, px, py, PT_SUBPIXEL, centre, centre, &dcam, &ocam);
-    float max_dist = st->zfar > 0.0f ? st->zfar / maxf(-dcam.z, 1.0e-6f) : MAXVAL;
+    float max_dist, depth_z;
+    primary_ray(s, &cam, c, W, H, px, py, PT_SUBPIXEL, centre, centre, &dcam, &ocam, &max_dist, &depth_z);
     hit_t hit = closest(&ctx.W, vadd(cam.pos, mat_mul(cam.mat, ocam)), mat_mul(cam.mat, dcam), max_dist, st->cull_backfaces);
-    write_geometry(s, w, c, pixelid, &hit, dcam.z);
+    write_geometry(s, w, c, pixelid, &hit, depth_z);
     return;
   }
   v3 head_dir = vneg(V(cam.mat[2], cam.mat[5], cam.mat[8]));
@@ -2051,13 +2157,13 @@ static void render_pixel_pt(const MjpbrScene* s, const int32_t* mesh_nface, int 
       sy = (int)(pt_rand(pixel_seed, smp, PT_JITTER, 1) * (float)PT_SUBPIXEL);
     }
     v3 dcam, ocam;
-    camera_frame_ray(&cam, W, H, px, py, PT_SUBPIXEL, sx, sy, &dcam, &ocam);
-    float max_dist = st->zfar > 0.0f ? st->zfar / maxf(-dcam.z, 1.0e-6f) : MAXVAL;
+    float max_dist, depth_z;
+    primary_ray(s, &cam, c, W, H, px, py, PT_SUBPIXEL, sx, sy, &dcam, &ocam, &max_dist, &depth_z);
     primary_t first;
     v3 radiance =
         trace_path(&ctx, vadd(cam.pos, mat_mul(cam.mat, ocam)), mat_mul(cam.mat, dcam), max_dist, head_dir, pixel_seed, smp, &first);
     if (smp == 0) {
-      write_geometry(s, w, c, pixelid, &first.hit, dcam.z);
+      write_geometry(s, w, c, pixelid, &first.hit, depth_z);
       if (st->render_guides && s->guide_albedo) {
         s->guide_albedo[adr * 3] = first.base_color.x;
         s->guide_albedo[adr * 3 + 1] = first.base_color.y;
@@ -2066,7 +2172,7 @@ static void render_pixel_pt(const MjpbrScene* s, const int32_t* mesh_nface, int 
         s->guide_normal[adr * 3 + 1] = first.normal.y;
         s->guide_normal[adr * 3 + 2] = first.normal.z;
       }
-      if (first.hit.geom != -1) first_depth = first.hit.dist * -dcam.z;
+      if (first.hit.geom != -1) first_depth = first.hit.dist * -depth_z;
     }
     hdr = vadd(hdr, radiance);
     albedo_sum = vadd(albedo_sum, first.albedo);

@@ -265,6 +265,11 @@ class OracleScene:
           "cdf_width": env.prob.shape[2],
         }
       )
+    if options.get("camera_rays") is not None:
+      from mujoco_warp_pbr_gb300 import rays as rays_lib
+
+      self.ray_origin, self.ray_direction = rays_lib.pack_camera_rays(options["camera_rays"], o["cam_res"])
+      a.update({"ray_origin": self.ray_origin, "ray_direction": self.ray_direction, "bundle_res": o["cam_res"]})
     self.mesh_nface = np.ascontiguousarray(self.hc.meshes.get("mesh_nface", []), i32)
     self.arrays = a  # keeps every array alive
     self.scene = _scene.fill_scene({k: v for k, v in a.items() if v is not None})
