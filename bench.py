@@ -42,6 +42,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mpix/s (real-time tier, 1 GB300)"
+PATH_METRIC = "Mpix/s (path-traced tier, 1 GB300)"
 UNIT = "Mpix/s"
 
 
@@ -150,7 +151,53 @@ def make_scene(args):
 
   if args.workload == "mesh_ibl":
     return synthetic.mesh_ibl_scene(seed=args.seed, nworld=args.nworld, res=args.res)
+  if args.workload == "path":
+    return synthetic.path_scene(seed=args.seed, nworld=args.nworld, res=args.res, spp=args.spp)
   return synthetic.primitive_scene(seed=args.seed, nworld=args.nworld, res=args.res)
+
+
+def path_tier(dev, steps: int, nworld: int = 1024, res: int = 128, spp: int = 2) -> dict:
+  """Secondary line: the path-traced tier on the emissive-quad scene (device-resident, per-step
+  events, L2 flushed outside them)."""
+  import torch
+
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import _lib
+  from mujoco_warp_pbr_gb300 import synthetic
+
+  sc = synthetic.path_scene(seed=0, nworld=nworld, res=res, spp=spp)
+  m = mjpbr.put_model(sc.mjm, device=dev)
+  d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld, device=dev)
+  rc = mjpbr.create_render_context(sc.mjm, sc.nworld, data=sc.mjd, device=dev, **sc.options)
+  synthetic.apply_per_world(sc, m, rc)
+  stream = torch.cuda.current_stream(dev)
+  flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+  scene = mjpbr.scene_descriptor(m, d, rc)
+  for i in range(3):
+    _lib.call("mjpbr_refit_bvh", scene, stream.cuda_stream)
+    _lib.call("mjpbr_render", scene, i, stream.cuda_stream)
+  torch.cuda.synchronize()
+  ms = []
+  for i in range(steps):
+    flush.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    _lib.call("mjpbr_refit_bvh", scene, stream.cuda_stream)
+    _lib.call("mjpbr_render", scene, 100 + i, stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    ms.append(e0.elapsed_time(e1))
+  assert mjpbr.check_errors(rc) == 0
+  npix = sc.nworld * res * res
+  avg = sum(ms) / len(ms)
+  return {
+    "workload": sc.name,
+    "value": npix / (avg / 1000.0) / 1e6,
+    "unit": UNIT,
+    "samples_per_s": npix * spp / (avg / 1000.0),
+    "ms_per_step": avg,
+    "config": {"nworld": nworld, "cam_res": [res, res], "spp": spp, "max_depth": 4, "rr_depth": 2, "emissive_quads": 3},
+  }
 
 
 def cpu_baseline(sc, budget_s: float, nthreads: int = 0) -> dict:
@@ -207,7 +254,7 @@ def run_reference(args) -> None:
     json.dumps(
       {
         "impl": "reference",
-        "metric": METRIC,
+        "metric": PATH_METRIC if args.workload == "path" else METRIC,
         "value": value,
         "unit": UNIT,
         "n_gpus": args.gpus,
@@ -245,6 +292,8 @@ def _config(args, sc) -> dict:
   }
   if args.workload == "mesh_ibl":
     cfg.update({"meshes": 6, "triangles_per_mesh": 5120, "primitives": 10, "env": "1024x512", "textures": "3x512^2", "mirror_floor": 0.3})
+  elif args.workload == "path":
+    cfg.update({"tier": "path", "spp": args.spp, "max_depth": 4, "rr_depth": 2, "primitives": 8, "emissive_quads": 3})
   else:
     cfg.update({"primitives": 8, "lights": 2, "shadow_samples": sc.options.get("shadow_samples", 1)})
   return cfg
@@ -354,7 +403,7 @@ def run(args) -> None:
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = _traffic(sc.name)
     line = {
-      "metric": METRIC,
+      "metric": PATH_METRIC if args.workload == "path" else METRIC,
       "value": value,
       "unit": UNIT,
       "n_gpus": world_size,
@@ -370,7 +419,7 @@ def run(args) -> None:
       "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
       "roofline": {
         "bound": "hbm",
-        "kernel": "rt_kernel",
+        "kernel": "pt_kernel" if args.workload == "path" else "rt_kernel",
         "achieved": achieved,
         "peak": peak,
         "unit": "GB/s",
@@ -386,6 +435,8 @@ def run(args) -> None:
       "clocks": clocks.summary(),
       "cpu_baseline": baseline,
     }
+    if args.workload == "mesh_ibl" and not args.no_path_tier:
+      line["path_tier"] = path_tier(dev, max(3, args.steps // 2))
     print(json.dumps(line))
   if world_size > 1:
     dist.destroy_process_group()
@@ -397,7 +448,9 @@ def main() -> None:
   p.add_argument("--steps", type=int, default=20)
   p.add_argument("--warmup", type=int, default=3)
   p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-  p.add_argument("--workload", choices=["mesh_ibl", "primitives"], default="mesh_ibl")
+  p.add_argument("--workload", choices=["mesh_ibl", "primitives", "path"], default="mesh_ibl")
+  p.add_argument("--spp", type=int, default=2)
+  p.add_argument("--no-path-tier", action="store_true")
   p.add_argument("--nworld", type=int, default=None)
   p.add_argument("--res", type=int, default=None)
   p.add_argument("--seed", type=int, default=0)
@@ -405,9 +458,9 @@ def main() -> None:
   p.add_argument("--no-cpu-baseline", action="store_true")
   args = p.parse_args()
   if args.nworld is None:
-    args.nworld = 4096 if args.workload == "mesh_ibl" else 16
+    args.nworld = {"mesh_ibl": 4096, "path": 1024}.get(args.workload, 16)
   if args.res is None:
-    args.res = 128 if args.workload == "mesh_ibl" else 64
+    args.res = 128 if args.workload in ("mesh_ibl", "path") else 64
   args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
   if args.impl == "reference":
     run_reference(args)

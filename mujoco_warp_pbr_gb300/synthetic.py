@@ -362,7 +362,7 @@ def apply_per_world(scene: SyntheticScene, m: Any, rc: Any) -> None:
   import torch
 
   for name, value in scene.per_world.items():
-    owner = m if name in ("geom_rgba",) else rc
+    owner = m if name in ("geom_rgba", "mat_emission") else rc
     t = torch.as_tensor(value).to(rc.device)
     setattr(owner, name, t)
 
@@ -438,6 +438,59 @@ def primitive_scene(seed: int = 0, nworld: int = 16, res: int = 64, shadow_sampl
     },
     seed=seed,
   )
+
+
+def path_scene(seed: int = 0, nworld: int = 1024, res: int = 128, spp: int = 2, nquad: int = 3) -> SyntheticScene:
+  """Path-traced tier: the primitive scene plus emissive quads (thin boxes whose material emission,
+  display-relative radiance, is drawn per world from U(1, 20)), next-event estimation over the
+  lights, max depth 4, Russian roulette after bounce 2, `spp` jittered samples per pixel."""
+  base = primitive_scene(seed=seed, nworld=nworld, res=res)
+  rng = np.random.default_rng(seed + 7919)
+  b = Builder()
+  b.geom(GEOM_PLANE, (3.0, 3.0, 0.1), rgba=(0.6, 0.6, 0.6, 1.0))
+  for t, size in _random_primitives(np.random.default_rng(seed), 8):
+    b.geom(t, size)
+  quads = []
+  for _ in range(nquad):
+    mat = b.material(rgba=(1, 1, 1, 1), roughness=1.0, specular=0.0, emission=1.0)
+    pos = (rng.uniform(-1.2, 1.2), rng.uniform(-1.2, 1.2), rng.uniform(1.0, 1.6))
+    quads.append(b.geom(GEOM_BOX, (rng.uniform(0.15, 0.35), rng.uniform(0.15, 0.35), 0.005), pos=pos, matid=mat, rgba=(1, 1, 1, 1)))
+  b.light(LIGHT_DIRECTIONAL, pos=(0, 0, 4), dir=(0.3, 0.2, -1.0), diffuse=(0.7, 0.7, 0.7), castshadow=True)
+  b.light(LIGHT_POINT, pos=(0.5, -0.5, 2.0), diffuse=(0.5, 0.5, 0.5), range=10.0, bulbradius=0.05, castshadow=True)
+  b.camera((0.0, -3.2, 2.2), (0.0, 0.0, 0.25), fovy=45.0, resolution=(res, res))
+  mjm, mjd0 = b.build()
+  ngeom, nprim = mjm.ngeom, 9
+  xpos = np.broadcast_to(mjd0.geom_xpos, (nworld, ngeom, 3)).copy()
+  xmat = np.broadcast_to(mjd0.geom_xmat, (nworld, ngeom, 9)).copy()
+  xpos[:, :nprim] = base.mjd.geom_xpos
+  xmat[:, :nprim] = base.mjd.geom_xmat
+  mjd = HostData(
+    geom_xpos=xpos.astype(np.float32),
+    geom_xmat=xmat.astype(np.float32),
+    cam_xpos=base.mjd.cam_xpos,
+    cam_xmat=base.mjd.cam_xmat,
+    light_xpos=base.mjd.light_xpos,
+    light_xdir=base.mjd.light_xdir,
+  )
+  pw = dict(base.per_world)
+  rgba = np.ones((nworld, ngeom, 4), np.float32)
+  rgba[:, :nprim] = pw["geom_rgba"]
+  rough = np.ones((nworld, ngeom), np.float32)
+  rough[:, :nprim] = pw["geom_roughness"]
+  metal = np.zeros((nworld, ngeom), np.float32)
+  metal[:, :nprim] = pw["geom_metallic"]
+  pw.update(
+    {
+      "geom_rgba": rgba,
+      "geom_roughness": rough,
+      "geom_metallic": metal,
+      "mat_emission": rng.uniform(1.0, 20.0, (nworld, mjm.nmat)).astype(np.float32),
+    }
+  )
+  options = dict(base.options)
+  options.update({"tier": 1, "path_samples": spp, "max_depth": 4, "rr_depth": 2})
+  options.pop("shadow_samples", None)
+  return SyntheticScene(name=f"path_{nworld}x{res}_spp{spp}", mjm=mjm, mjd=mjd, nworld=nworld, options=options, per_world=pw, seed=seed)
 
 
 def procedural_env(rng: np.random.Generator, width: int = 1024) -> np.ndarray:

@@ -136,7 +136,7 @@ class OracleScene:
       "geom_size": _b(mjm.geom_size, f32, (1, ngeom, 3))[0:1].reshape(1, ngeom, 3),
       "geom_rgba": np.ascontiguousarray(np.asarray(per_world.pop("geom_rgba", mjm.geom_rgba), f32).reshape(-1, ngeom, 4)),
       "mat_rgba": _b(mjm.mat_rgba if nmat else np.zeros((1, 4)), f32, (max(nmat, 1), 4)),
-      "mat_emission": _b(mjm.mat_emission if nmat else np.zeros(1), f32, ()),
+      "mat_emission": np.ascontiguousarray(np.asarray(per_world.pop("mat_emission", mjm.mat_emission if nmat else np.zeros(1)), f32).reshape(-1, max(nmat, 1))),
       "mat_texid": _b(mjm.mat_texid if nmat else -np.ones((1, 10)), i32, (max(nmat, 1), 10)),
       "mat_texrepeat": _b(mjm.mat_texrepeat if nmat else np.ones((1, 2)), f32, (max(nmat, 1), 2)),
       "mat_texuniform": _b(mjm.mat_texuniform if nmat else np.zeros(1), i32, ()),

@@ -84,7 +84,7 @@ def render_gpu(b: Builder, nworld: int = 1, seed: int = 0, per_world: dict | Non
   d = mjpbr.put_data(mjm, mjd, nworld=nworld)
   rc = mjpbr.create_render_context(mjm, nworld, data=mjd, **options)
   for name, value in (per_world or {}).items():
-    owner = m if name == "geom_rgba" else rc
+    owner = m if name in ("geom_rgba", "mat_emission") else rc
     setattr(owner, name, torch.as_tensor(np.asarray(value)).to(rc.device))
   mjpbr.refit_bvh(m, d, rc)
   mjpbr.render(m, d, rc, seed=seed)
