@@ -55,7 +55,7 @@ struct Pt {
     return trace_ray<kMesh>(*c.s, c.st, c.blk, c.L, Ray{o, d}, max_dist, c.s->settings.cull_backfaces != 0, any, &c.err);
   }
 
-  static MJ_DEV V3 environment(const RtCtx& c, V3 d) {
+  static __device__ __noinline__ V3 environment(const RtCtx& c, V3 d) {
     const MjpbrScene& s = *c.s;
     return sample_radiance(s.env_radiance[c.env], s.env_data, d, c.env_yaw, 0.0f) * c.env_scale;
   }

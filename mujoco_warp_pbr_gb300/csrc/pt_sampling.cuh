@@ -12,6 +12,15 @@
 
 namespace mjpbr {
 
+// The BSDF evaluation and pdf are called from several places of the bounce loop (each light's
+// sample, the environment sample, the continuation); one out-of-line copy keeps the loop's code
+// small (the path kernel is bound by instruction fetch when everything is inlined).
+#ifdef MJPBR_PT_INLINE
+#define MJPBR_PT_CALL static __device__ __forceinline__
+#else
+#define MJPBR_PT_CALL static __device__ __noinline__
+#endif
+
 // Random-number layout: path vertex (sample, depth) owns kSlots consecutive counters; depth row
 // kJitterDepth holds the sub-pixel jitter. Slots: 0 alpha, 1 mirror, 2-3 environment, 4-11 the
 // light samples of lights 0-3, 12-14 BSDF, 15 Russian roulette; further lights draw from a
@@ -66,7 +75,7 @@ MJ_HD V3 sample_ggx_vndf(V3 v, float alpha, float u0, float u1) {
 }
 
 // BRDF x cos(theta_l) for local view v and light l (diffuse already (1 - E) weighted).
-MJ_HD V3 eval_bsdf_cos(V3 diffuse_color, V3 f0, float alpha, V3 energy_comp, V3 v, V3 l) {
+MJPBR_PT_CALL V3 eval_bsdf_cos(V3 diffuse_color, V3 f0, float alpha, V3 energy_comp, V3 v, V3 l) {
   float nol = l.z;
   float nov = fmaxf(v.z, 1.0e-4f);
   if (nol <= 0.0f) return v3(0.0f);
@@ -88,7 +97,7 @@ MJ_HD V3 eval_bsdf_cos(V3 diffuse_color, V3 f0, float alpha, V3 energy_comp, V3 
 }
 
 // Solid-angle pdf of sample_bsdf: mixture of GGX VNDF and cosine-weighted hemisphere.
-MJ_HD float pdf_bsdf(float alpha, float p_spec, V3 v, V3 l) {
+MJPBR_PT_CALL float pdf_bsdf(float alpha, float p_spec, V3 v, V3 l) {
   if (l.z <= 0.0f) return 0.0f;
   float nov = fmaxf(v.z, 1.0e-4f);
   V3 h = normalize(l + v);
