@@ -77,6 +77,10 @@ enum MjpbrToneMapper { MJPBR_TONE_PBR_NEUTRAL = 0, MJPBR_TONE_ACES = 1, MJPBR_TO
 enum MjpbrLightModel { MJPBR_LIGHT_MODEL_PHYSICAL = 0, MJPBR_LIGHT_MODEL_MUJOCO = 1 };
 enum MjpbrTier { MJPBR_TIER_REALTIME = 0, MJPBR_TIER_PATH = 1 };
 enum MjpbrRenderOrder { MJPBR_ORDER_ROW = 0, MJPBR_ORDER_TILED = 1, MJPBR_ORDER_WORLD = 2 };
+/* Real-time tier schedules: one CTA per (camera tile, world), or a persistent launch whose warps
+ * pull work items (settings.queue_item pixels of one camera image of one world) from a device
+ * counter (scene.work_counter[1]). */
+enum MjpbrSchedule { MJPBR_SCHEDULE_GRID = 0, MJPBR_SCHEDULE_QUEUE = 1 };
 /* Texel formats of MjpbrTexture. */
 enum MjpbrTexFormat { MJPBR_TEX_RGBA8 = 0, MJPBR_TEX_RGBA16F = 1 };
 
@@ -125,6 +129,8 @@ typedef struct MjpbrSettings {
   int32_t max_depth;         /* path tier: bounces */
   int32_t rr_depth;          /* path tier: Russian roulette start */
   int32_t denoise;           /* path tier: write denoiser features instead of RGB */
+  int32_t schedule;          /* real-time tier: MjpbrSchedule */
+  int32_t queue_item;        /* queue schedule: pixels per work item (32, 64 or 128) */
   float znear;
   float zfar;                /* <= 0: unbounded */
   float shadow_light_fraction;
@@ -315,6 +321,14 @@ int mjpbr_refit_bvh(const MjpbrScene* scene, void* stream);
  * Replaces mujoco_warp_pbr.render (mujoco_warp_pbr/_src/render.py:431-460). Call
  * mjpbr_refit_bvh first whenever geometry or cameras moved. */
 int mjpbr_render(const MjpbrScene* scene, uint32_t seed, void* stream);
+
+/* BF16 tensor-core GEMM: d (m x n, FP32, row-major) = a (m x k, BF16 bits, row-major) times the
+ * transpose of b (n x k, BF16 bits, row-major), FP32 accumulation. m a multiple of 128, n a
+ * multiple of 16 in [16, 256], k a multiple of 16; 16-byte aligned device pointers. A bounded
+ * wait that gives up ORs bit 4 into *error_word (may be NULL). Building block of the learned
+ * denoiser; no counterpart in the reference. */
+int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
+                    void* stream);
 
 /* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
  * caller: the per-world blocks and the path tracer's work counter live in static device memory of

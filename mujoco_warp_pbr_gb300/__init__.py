@@ -6,6 +6,8 @@ compute runs in hand-written CUDA kernels of libmjpbr.so behind a C ABI (include
 package is the host side. There is no CPU fallback: without the built library, rendering raises.
 """
 
+from mujoco_warp_pbr_gb300.autotune import autotune as autotune
+from mujoco_warp_pbr_gb300.autotune import capture_frame as capture_frame
 from mujoco_warp_pbr_gb300.envmap import load_hdr as load_hdr
 from mujoco_warp_pbr_gb300.context import create_render_context as create_render_context
 from mujoco_warp_pbr_gb300.context import resolve_geom_materials as resolve_geom_materials

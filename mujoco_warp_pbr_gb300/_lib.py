@@ -87,6 +87,8 @@ class Settings(ctypes.Structure):
       "max_depth",
       "rr_depth",
       "denoise",
+      "schedule",
+      "queue_item",
     )
   ] + [
     ("znear", c_f32),
@@ -254,6 +256,7 @@ _SIGNATURES = {
   "mjpbr_refit_bvh": (ctypes.c_int, [ctypes.POINTER(Scene), c_vp]),
   "mjpbr_render": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),
   "mjpbr_refit_render_static": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),
+  "mjpbr_gemm_bf16": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp]),
   "mjpbr_get_rgb": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),
   "mjpbr_get_depth": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_f32, c_vp, c_i32, c_vp]),
   "mjpbr_get_segmentation": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),

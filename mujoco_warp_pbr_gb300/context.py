@@ -71,6 +71,19 @@ def _enum(cls: type[enum.IntEnum], value: int, name: str) -> enum.IntEnum:
     raise ValueError(f"{name} must be one of {options}, got {value!r}") from None
 
 
+SCHEDULES = {"grid": 0, "queue": 1}
+
+
+def _schedule(schedule: str | int) -> int:
+  """The real-time tier's schedule: "grid" (one CTA per camera tile and world) or "queue" (a
+  persistent launch whose warps pull work items from a device counter)."""
+  if isinstance(schedule, str) and schedule in SCHEDULES:
+    return SCHEDULES[schedule]
+  if not isinstance(schedule, str) and int(schedule) in SCHEDULES.values():
+    return int(schedule)
+  raise ValueError(f'schedule must be "grid" or "queue", got {schedule!r}')
+
+
 def _check_at_least(name: str, value: int, low: int) -> None:
   if value < low:
     raise ValueError(f"{name} must be at least {low}, got {value}")
@@ -497,6 +510,8 @@ def prepare_context(
   use_skybox: bool = True,
   render_order: RenderOrder | int = RenderOrder.TILED,
   block_dim: int | None = None,
+  schedule: str | int = "grid",
+  queue_item: int = 64,
   max_registers: int | None = None,
   mesh_bvh_constructor: str = "cubql",
   mesh_bvh_frame: str = "auto",
@@ -538,6 +553,9 @@ def prepare_context(
   _check_default_material(default_material)
   if denoise and tier != Tier.PATH:
     raise ValueError("denoise applies to the path-traced tier (Tier.PATH)")
+  schedule = _schedule(schedule)
+  if queue_item not in (32, 64, 128):
+    raise ValueError(f"queue_item must be 32, 64 or 128 pixels, got {queue_item}")
   if mesh_bvh_frame not in _MESH_BVH_FRAMES:
     raise ValueError(f'mesh_bvh_frame must be "auto" or "mujoco", got {mesh_bvh_frame!r}')
   if mesh_bvh_constructor not in _MESH_BVH_CONSTRUCTORS:
@@ -753,6 +771,8 @@ def prepare_context(
     "max_layers": int(max_layers),
     "has_reflection": has_reflection,
     "render_order": int(render_order),
+    "schedule": int(schedule),
+    "queue_item": int(queue_item),
     "tier": int(tier),
     "path_samples": int(path_samples),
     "max_depth": int(max_depth),
@@ -911,6 +931,8 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     max_layers=op["max_layers"],
     has_reflection=op["has_reflection"],
     render_order=op["render_order"],
+    schedule=op["schedule"],
+    queue_item=op["queue_item"],
     tier=op["tier"],
     path_samples=op["path_samples"],
     max_depth=op["max_depth"],

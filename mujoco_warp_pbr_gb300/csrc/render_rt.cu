@@ -10,6 +10,9 @@
 //
 // Pixels are addressed by camera and row-major pixel id; the random numbers of a pixel are keyed
 // by that id, so every thread order renders identical images.
+#include <algorithm>
+#include <climits>
+
 #include "abi_internal.h"
 #include "kernel_common.cuh"
 
@@ -220,55 +223,18 @@ struct Rt {
   }
 };
 
+// Renders pixel p of world w (render.py:343-395) from the world block blk: N x N supersamples,
+// depth / segmentation / guides from the first one, tone mapped per sample, averaged and encoded.
 template <bool kMesh, bool kTex>
-__global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
-                                                      const __grid_constant__ TileMap tm) {
-  extern __shared__ __align__(16) float smem[];
-  float* blk = smem;
-  const int32_t w = blockIdx.y;
-  // ---- stage the world block
-  {
-    const float4* src = reinterpret_cast<const float4*>(s.world_blocks + (int64_t)w * s.world_block_floats);
-    float4* dst = reinterpret_cast<float4*>(blk);
-    const int32_t n4 = s.world_block_floats >> 2;
-    for (int32_t i = threadIdx.x; i < n4; i += kThreads) dst[i] = __ldg(src + i);
-  }
-  __syncthreads();
-  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-
-  // ---- this thread's pixel
-  const int32_t tile = blockIdx.x;
-  int32_t cam = 0;
-  while (cam + 1 < tm.ncam && tile >= tm.tile_base[cam + 1]) ++cam;
-  const int32_t t = tile - tm.tile_base[cam];
-  const int32_t tx = t % tm.tiles_x[cam], ty = t / tm.tiles_x[cam];
-  Pixel p;
-  p.cam = cam;
-  p.width = s.cam_res[cam][0];
-  p.height = s.cam_res[cam][1];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (s.settings.render_order == MJPBR_ORDER_ROW) {
-    p.px = tx * 32 + lane;
-    p.py = ty * 8 + warp;
-  } else {
-    p.px = tx * 16 + (warp & 1) * 8 + (lane & 7);
-    p.py = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
-  }
-  if (p.px >= p.width || p.py >= p.height) return;
+MJ_DEV void render_pixel(const MjpbrScene& s, uint32_t seed, const float* blk, const BlockLayout& L, int32_t w, Pixel& p,
+                         const Stack& stack) {
+  const int32_t cam = p.cam;
   p.pixelid = p.py * p.width + p.px;
   p.rec = blk + L.cam_off + cam * kCamFloats;
   const bool want_rgb = s.render_rgb[cam] != 0;
   const MjpbrSettings& st = s.settings;
-
   RtCtx c;
-  c.s = &s;
-  c.blk = blk;
-  {
-    int32_t* stack_base = reinterpret_cast<int32_t*>(smem + s.world_block_floats);
-    c.st.code = stack_base + threadIdx.x;
-    c.st.t = reinterpret_cast<float*>(stack_base + kThreads * kStackDepth) + threadIdx.x;
-    c.st.stride = kThreads;
-  }
+  c.st = stack;
   init_ctx(c, s, blk, L, w, kTex);
   const M3 R = cam_mat(p.rec);
   const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
@@ -331,22 +297,196 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   if (c.err && s.error_word) atomicOr(s.error_word, c.err);
 }
 
+MJ_DEV Stack thread_stack(float* stacks) {
+  Stack st;
+  int32_t* base = reinterpret_cast<int32_t*>(stacks);
+  st.code = base + threadIdx.x;
+  st.t = reinterpret_cast<float*>(base + kThreads * kStackDepth) + threadIdx.x;
+  st.stride = kThreads;
+  return st;
+}
+
+// Grid schedule: one CTA per (camera tile, world); the hardware scheduler balances the CTAs.
+template <bool kMesh, bool kTex>
+__global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+                                                                           const __grid_constant__ TileMap tm) {
+  extern __shared__ __align__(16) float smem[];
+  float* blk = smem;
+  const int32_t w = blockIdx.y;
+  stage_world_block(s, w, blk, kThreads);
+  __syncthreads();
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const int32_t tile = blockIdx.x;
+  int32_t cam = 0;
+  while (cam + 1 < tm.ncam && tile >= tm.tile_base[cam + 1]) ++cam;
+  const int32_t t = tile - tm.tile_base[cam];
+  const int32_t tx = t % tm.tiles_x[cam], ty = t / tm.tiles_x[cam];
+  Pixel p;
+  p.cam = cam;
+  p.width = s.cam_res[cam][0];
+  p.height = s.cam_res[cam][1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (s.settings.render_order == MJPBR_ORDER_ROW) {
+    p.px = tx * 32 + lane;
+    p.py = ty * 8 + warp;
+  } else {
+    p.px = tx * 16 + (warp & 1) * 8 + (lane & 7);
+    p.py = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
+  }
+  if (p.px >= p.width || p.py >= p.height) return;
+  render_pixel<kMesh, kTex>(s, seed, blk, L, w, p, thread_stack(smem + s.world_block_floats));
+}
+
+// Work items of the queue schedule: runs of `per_item` warp tiles (8 x 4 pixels) of one camera
+// image of one world, world-major.
+struct QueueMap {
+  int32_t ncam;
+  int32_t per_item;                         // warp tiles per item
+  int32_t wtiles_x[MJPBR_MAX_RENDER];       // warp tiles per row of each camera
+  int32_t wtiles[MJPBR_MAX_RENDER];         // warp tiles of each camera
+  int32_t item_base[MJPBR_MAX_RENDER + 1];  // first item of each camera within a world
+  int32_t items_per_world;
+  int32_t total;
+};
+
+// Queue schedule: a persistent launch (resident CTAs only) whose warps pull work items from a
+// device counter. Each warp keeps its own copy of the current item's world block in shared
+// memory (re-staged only when the world changes), so warps never wait for one another: uneven
+// cameras, enable masks and per-pixel costs balance at warp granularity.
+template <bool kMesh, bool kTex>
+__global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_queue_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+                                                                                 const __grid_constant__ QueueMap qm) {
+  extern __shared__ __align__(16) float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  float* blk = smem + warp * s.world_block_floats;
+  const Stack stack = thread_stack(smem + (kThreads / 32) * s.world_block_floats);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  int32_t staged = -1;
+  for (;;) {
+    int32_t item = 0;
+    if (lane == 0) item = atomicAdd(s.work_counter + 1, 1);
+    item = __shfl_sync(full, item, 0);
+    if (item >= qm.total) break;
+    const int32_t w = item / qm.items_per_world;
+    const int32_t li = item - w * qm.items_per_world;
+    int32_t cam = 0;
+    while (cam + 1 < qm.ncam && li >= qm.item_base[cam + 1]) ++cam;
+    if (w != staged) {
+      __syncwarp();
+      const float4* src = reinterpret_cast<const float4*>(s.world_blocks + (int64_t)w * s.world_block_floats);
+      float4* dst = reinterpret_cast<float4*>(blk);
+      for (int32_t i = lane; i < (s.world_block_floats >> 2); i += 32) dst[i] = __ldg(src + i);
+      __syncwarp();
+      staged = w;
+    }
+    const int32_t first = (li - qm.item_base[cam]) * qm.per_item;
+#pragma unroll 1
+    for (int32_t j = 0; j < qm.per_item; ++j) {
+      const int32_t wt = first + j;
+      if (wt >= qm.wtiles[cam]) break;
+      Pixel p;
+      p.cam = cam;
+      p.width = s.cam_res[cam][0];
+      p.height = s.cam_res[cam][1];
+      p.px = (wt % qm.wtiles_x[cam]) * 8 + (lane & 7);
+      p.py = (wt / qm.wtiles_x[cam]) * 4 + (lane >> 3);
+      if (p.px < p.width && p.py < p.height) render_pixel<kMesh, kTex>(s, seed, blk, L, w, p, stack);
+    }
+  }
+}
+
+int g_sm_count = 0;
+
+int sm_count() {
+  if (g_sm_count == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sm_count <= 0) g_sm_count = 1;
+  }
+  return g_sm_count;
+}
+
+// Largest dynamic shared memory a CTA may use while MJPBR_RT_MIN_BLOCKS CTAs stay resident.
+constexpr size_t kSmemPerSm = 228 * 1024;
+constexpr size_t kQueueSmemLimit = kSmemPerSm / MJPBR_RT_MIN_BLOCKS - 2048;
+
+size_t stack_bytes() { return (size_t)kThreads * kStackDepth * 8; }
+
 template <bool kMesh, bool kTex>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaStream_t stream) {
-  size_t smem = (size_t)s.world_block_floats * sizeof(float) + (size_t)kThreads * kStackDepth * 8;
+  static size_t smem_set = 0;
+  const size_t smem = (size_t)s.world_block_floats * sizeof(float) + stack_bytes();
   auto kern = rt_kernel<kMesh, kTex>;
-  {
+  if (smem > smem_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render: world block of %zu bytes: %s", smem, cudaGetErrorString(e));
+    smem_set = smem;
   }
   dim3 grid(tm.tile_base[tm.ncam], s.nworld);
   kern<<<grid, kThreads, smem, stream>>>(s, seed, tm);
   return check_launch("rt_kernel");
 }
 
+template <bool kMesh, bool kTex>
+int launch_queue_variant(const MjpbrScene& s, uint32_t seed, const QueueMap& qm, cudaStream_t stream) {
+  static size_t smem_set = 0;
+  const size_t smem = (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes();
+  auto kern = rt_queue_kernel<kMesh, kTex>;
+  if (smem > smem_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render queue: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
+    smem_set = smem;
+  }
+  cudaError_t e = cudaMemsetAsync(s.work_counter + 1, 0, sizeof(int32_t), stream);
+  if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render queue: work counter: %s", cudaGetErrorString(e));
+  const int grid = std::min(qm.total, sm_count() * MJPBR_RT_MIN_BLOCKS);
+  kern<<<grid, kThreads, smem, stream>>>(s, seed, qm);
+  return check_launch("rt_queue_kernel");
+}
+
+int render_rt_queue(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
+  QueueMap qm;
+  qm.ncam = s.nrender;
+  qm.per_item = std::max(1, s.settings.queue_item / 32);
+  qm.item_base[0] = 0;
+  for (int32_t c = 0; c < s.nrender; ++c) {
+    const int32_t W = s.cam_res[c][0], H = s.cam_res[c][1];
+    const bool any = s.render_rgb[c] || s.render_depth[c] || s.render_seg[c];
+    qm.wtiles_x[c] = (W + 7) / 8;
+    qm.wtiles[c] = any ? qm.wtiles_x[c] * ((H + 3) / 4) : 0;
+    qm.item_base[c + 1] = qm.item_base[c] + (qm.wtiles[c] + qm.per_item - 1) / qm.per_item;
+  }
+  qm.items_per_world = qm.item_base[s.nrender];
+  const int64_t total = (int64_t)qm.items_per_world * s.nworld;
+  if (total == 0) return MJPBR_OK;
+  if (total > INT32_MAX) return set_error(MJPBR_ERR_ARG, "render queue: %lld work items exceed the counter", (long long)total);
+  qm.total = (int32_t)total;
+  const bool mesh = s.nmesh > 0 && s.blas_root != nullptr;
+  const bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
+  if (mesh && tex) return launch_queue_variant<true, true>(s, seed, qm, stream);
+  if (mesh) return launch_queue_variant<true, false>(s, seed, qm, stream);
+  if (tex) return launch_queue_variant<false, true>(s, seed, qm, stream);
+  return launch_queue_variant<false, false>(s, seed, qm, stream);
+}
+
 }  // namespace
 
+// True when the queue schedule's per-warp world blocks fit the shared memory of the resident CTAs.
+bool rt_queue_fits(const MjpbrScene& s) {
+  return (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes() <= kQueueSmemLimit;
+}
+
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
+  if (s.settings.schedule == MJPBR_SCHEDULE_QUEUE) {
+    if (!s.work_counter) return set_error(MJPBR_ERR_ARG, "the queue schedule needs the work_counter scratch");
+    if (!rt_queue_fits(s)) {
+      return set_error(MJPBR_ERR_ARG, "queue schedule: 8 world blocks of %d floats do not fit shared memory; use the grid schedule",
+                       s.world_block_floats);
+    }
+    return render_rt_queue(s, seed, stream);
+  }
   TileMap tm;
   tm.ncam = s.nrender;
   if (s.settings.render_order == MJPBR_ORDER_ROW) {

@@ -181,6 +181,10 @@ class PbrRenderContext:
   ray_origin: torch.Tensor | None = None
   ray_direction: torch.Tensor | None = None
   ray_res: list[tuple[int, int]] | None = None
+  # real-time tier schedule (MJPBR_SCHEDULE_GRID 0 / MJPBR_SCHEDULE_QUEUE 1) and the queue's work
+  # item size in pixels; set by create_render_context or mujoco_warp_pbr_gb300.autotune
+  schedule: int = 0
+  queue_item: int = 64
   # accepted for compatibility with the reference's signature; the GB300 kernels choose their own
   block_dim: int | None = None
   max_registers: int | None = None

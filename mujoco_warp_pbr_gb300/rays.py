@@ -87,3 +87,28 @@ def set_camera_rays(rc: Any, camera_rays: Any) -> None:
   rc.ray_origin.copy_(torch.from_numpy(origin))
   rc.ray_direction.copy_(torch.from_numpy(direction))
   rc.ray_res = [list(r) for r in cam_res]
+
+
+def pinhole_rays(width: int, height: int, fovy_deg: float) -> np.ndarray:
+  """(height, width, 2, 3) camera-frame rays of a pinhole camera through the pixel centres."""
+  h = np.tan(np.radians(fovy_deg) / 2.0)
+  u = (np.arange(width) + 0.5) / width - 0.5
+  v = (np.arange(height) + 0.5) / height - 0.5
+  d = np.stack(np.broadcast_arrays(u[None, :] * 2.0 * h * width / height, -v[:, None] * 2.0 * h, -np.ones((1, 1))), axis=-1)
+  d /= np.linalg.norm(d, axis=-1, keepdims=True)
+  return np.stack([np.zeros_like(d), d], axis=2).astype(np.float32)
+
+
+def fisheye_rays(width: int, height: int, fov_deg: float = 180.0) -> np.ndarray:
+  """(height, width, 2, 3) rays of an equidistant fisheye: the angle from the optical axis grows
+  linearly with the distance from the image centre, reaching fov / 2 on the inscribed circle;
+  pixels outside that circle have no ray (zero direction)."""
+  u = (np.arange(width) + 0.5) / width * 2.0 - 1.0
+  v = 1.0 - (np.arange(height) + 0.5) / height * 2.0
+  x, y = np.meshgrid(u * width / max(width, height), v * height / max(width, height))
+  r = np.hypot(x, y)
+  theta = r * np.radians(fov_deg) / 2.0
+  phi = np.arctan2(y, x)
+  d = np.stack([np.sin(theta) * np.cos(phi), np.sin(theta) * np.sin(phi), -np.cos(theta)], -1)
+  d[r > 1.0] = 0.0
+  return np.stack([np.zeros_like(d), d], axis=2).astype(np.float32)

@@ -139,6 +139,8 @@ def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
   st.update(
     {
       "render_order": int(rc.render_order),
+      "schedule": int(rc.schedule),
+      "queue_item": int(rc.queue_item),
       "samples_per_axis": int(rc.samples_per_pixel),
       "tone_mapper": int(rc.tone_mapper),
       "render_hdr": int(bool(rc.render_hdr)),

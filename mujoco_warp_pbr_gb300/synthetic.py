@@ -493,6 +493,77 @@ def path_scene(seed: int = 0, nworld: int = 1024, res: int = 128, spp: int = 2, 
   return SyntheticScene(name=f"path_{nworld}x{res}_spp{spp}", mjm=mjm, mjd=mjd, nworld=nworld, options=options, per_world=pw, seed=seed)
 
 
+def batched_scene(seed: int = 0, nworld: int = 2048, res: tuple[int, ...] = (64, 128, 256), fisheye: int = 2, nprim: int = 16) -> SyntheticScene:
+  """Batched uneven workload: the primitive scene with `nprim` primitives and one camera per entry
+  of `res` (square images, all looking at the scene from different places); camera `fisheye`
+  renders per-pixel rays of a 180 degree equidistant fisheye, the others per-pixel pinhole rays.
+  Per-world enable masks (alpha 0) leave between 2 and nprim primitives visible, uniformly."""
+  from mujoco_warp_pbr_gb300 import rays
+
+  rng = np.random.default_rng(seed)
+  b = Builder()
+  b.geom(GEOM_PLANE, (3.0, 3.0, 0.1), rgba=(0.6, 0.6, 0.6, 1.0))
+  for t, size in _random_primitives(rng, nprim):
+    b.geom(t, size)
+  b.light(LIGHT_DIRECTIONAL, pos=(0, 0, 4), dir=(0.3, 0.2, -1.0), diffuse=(0.7, 0.7, 0.7), castshadow=True)
+  b.light(LIGHT_POINT, pos=(0.5, -0.5, 2.0), diffuse=(0.5, 0.5, 0.5), range=10.0, bulbradius=0.05, castshadow=True)
+  eyes = [(0.0, -3.2, 2.2), (2.6, -1.8, 1.6), (0.0, 0.0, 3.0), (-2.4, -2.0, 1.8)]
+  for i, r in enumerate(res):
+    b.camera(eyes[i % len(eyes)], (0.0, 0.0, 0.25) if i % len(eyes) != 2 else (0.0, 0.3, 0.0), fovy=45.0, resolution=(r, r))
+  mjm, mjd0 = b.build()
+  ngeom = mjm.ngeom
+  xpos = np.broadcast_to(mjd0.geom_xpos, (nworld, ngeom, 3)).copy()
+  xmat = np.broadcast_to(mjd0.geom_xmat, (nworld, ngeom, 9)).copy()
+  xpos[:, 1:, :2] = rng.uniform(-1.0, 1.0, (nworld, ngeom - 1, 2))
+  xpos[:, 1:, 2] = rng.uniform(0.1, 0.8, (nworld, ngeom - 1))
+  xmat[:, 1:] = quat_to_mat(random_quats(rng, (nworld, ngeom - 1)))
+  mjd = HostData(
+    geom_xpos=xpos.astype(np.float32),
+    geom_xmat=xmat.astype(np.float32),
+    cam_xpos=np.broadcast_to(mjd0.cam_xpos, (nworld, mjm.ncam, 3)).astype(np.float32),
+    cam_xmat=np.broadcast_to(mjd0.cam_xmat, (nworld, mjm.ncam, 9)).astype(np.float32),
+    light_xpos=np.broadcast_to(mjd0.light_xpos, (nworld, mjm.nlight, 3)).astype(np.float32),
+    light_xdir=np.broadcast_to(mjd0.light_xdir, (nworld, mjm.nlight, 3)).astype(np.float32),
+  )
+  rgba = np.concatenate([rng.uniform(0.0, 1.0, (nworld, ngeom, 3)), np.ones((nworld, ngeom, 1))], axis=-1)
+  rgba[:, 0, :3] = 0.6
+  # enable masks: k ~ U{2..nprim} visible primitives per world
+  visible = rng.integers(2, nprim + 1, nworld)
+  order = np.argsort(rng.uniform(size=(nworld, nprim)), axis=1)
+  hidden = order >= visible[:, None]
+  rgba[:, 1:, 3] = np.where(hidden, 0.0, 1.0)
+  roughness = rng.uniform(0.05, 1.0, (nworld, ngeom))
+  metallic = (rng.uniform(0.0, 1.0, (nworld, ngeom)) < 0.3).astype(np.float64)
+  metallic[:, 0] = 0.0
+  roughness[:, 0] = 0.9
+  grey = 0.5
+  exposure = 1.0 / (1.2 * 2.0**14.96578428466209)
+  srgb_grey = 1.055 * grey ** (1 / 2.4) - 0.055
+  bundle = [rays.fisheye_rays(r, r) if i == fisheye else rays.pinhole_rays(r, r, 45.0) for i, r in enumerate(res)]
+  return SyntheticScene(
+    name=f"batched_{nworld}x{'-'.join(map(str, res))}",
+    mjm=mjm,
+    mjd=mjd,
+    nworld=nworld,
+    options={
+      "cam_res": [(r, r) for r in res],
+      "render_rgb": True,
+      "render_depth": True,
+      "render_seg": True,
+      "shadow_samples": 4,
+      "background_color": (srgb_grey, srgb_grey, srgb_grey, 1.0),
+      "camera_rays": bundle,
+    },
+    per_world={
+      "geom_rgba": rgba.astype(np.float32),
+      "geom_roughness": roughness.astype(np.float32),
+      "geom_metallic": metallic.astype(np.float32),
+      "ambient_radiance": np.full((1, 3), grey / exposure, np.float32),
+    },
+    seed=seed,
+  )
+
+
 def procedural_env(rng: np.random.Generator, width: int = 1024) -> np.ndarray:
   """Log-normal radiance (mu 0, sigma 1) smoothed, plus a Gaussian sun lobe of peak 1e3."""
   h = width // 2
