@@ -88,6 +88,28 @@ enum MjpbrTexFormat { MJPBR_TEX_RGBA8 = 0, MJPBR_TEX_RGBA16F = 1 };
 typedef struct mjpbr_f32b { const float* ptr; int32_t nbatch; int32_t pad_; } mjpbr_f32b;
 typedef struct mjpbr_i32b { const int32_t* ptr; int32_t nbatch; int32_t pad_; } mjpbr_i32b;
 
+/* One 3x3 convolution layer of the learned denoiser (stride 1, zero padding), NHWC BF16
+ * activations, FP32 accumulation on the tensor cores. Input channels are `in` (c_in of them)
+ * followed, when c_in2 > 0, by `in2` (nimg, height / 2, width / 2, c_in2) upsampled x2 (nearest):
+ * the U-Net's skip concatenation. weight: (c_out, 9, c_in + c_in2), taps row-major (dy, dx).
+ * Epilogue: + bias, ReLU if relu, zeroed where mask <= 0 if mask (a ReLU derivative), stored as
+ * BF16 to out and/or FP32 to out_f32. Channel counts are multiples of 16, c_out <= 256; width is
+ * a power-of-two multiple of 16 up to 128 or a multiple of 128, height * width a multiple of 128
+ * (128 / min(width, 128) rows per 128-pixel tile). */
+typedef struct MjpbrConv {
+  const uint16_t* in;
+  const uint16_t* in2;
+  const uint16_t* weight;
+  const float* bias;
+  uint16_t* out;
+  float* out_f32;
+  const uint16_t* mask;
+  int32_t* error_word;
+  int32_t nimg, height, width, c_in, c_in2, c_out;
+  int32_t relu;
+  int32_t pad_;
+} MjpbrConv;
+
 /* One mipmapped 2D texture inside MjpbrScene.tex_data (RGBA, row-major levels). */
 typedef struct MjpbrTexture {
   int32_t format;   /* MjpbrTexFormat */
@@ -329,6 +351,10 @@ int mjpbr_render(const MjpbrScene* scene, uint32_t seed, void* stream);
  * denoiser; no counterpart in the reference. */
 int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                     void* stream);
+
+/* Forward 3x3 convolution (see MjpbrConv); also the input-gradient pass with the flipped,
+ * transposed weights. No counterpart in the reference (its denoiser is the a-trous filter). */
+int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream);
 
 /* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
  * caller: the per-world blocks and the path tracer's work counter live in static device memory of

@@ -169,6 +169,11 @@ int mjpbr_prefilter_env(const MjpbrTexture* radiance, const uint8_t* data, int32
   return prefilter_launch(radiance, data, levels, height, width, nsample, stack, static_cast<cudaStream_t>(stream));
 }
 
+int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream) {
+  if (!conv) return set_error(MJPBR_ERR_ARG, "conv is NULL");
+  return conv3x3_launch(*conv, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                     void* stream) {
   return gemm_bf16_launch(a, b, d, m, n, k, error_word, static_cast<cudaStream_t>(stream));

@@ -1,0 +1,97 @@
+"""3x3 convolution layers of the learned denoiser (tcgen05 implicit GEMM) against a float64 CPU
+convolution of the same BF16 values: every tile geometry (image widths 16 to 256), the skip
+concatenation with a half-resolution upsampled input, bias, ReLU, the ReLU-derivative mask and
+the FP32 output."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+
+def conv_ref(x, w, bias=None, x2=None, relu=False, mask=None):
+  """x (n, h, w, c1), x2 (n, h/2, w/2, c2) or None, w (cout, 9, c1 + c2): float64 NHWC result."""
+  if x2 is not None:
+    up = np.repeat(np.repeat(x2, 2, axis=1), 2, axis=2)
+    x = np.concatenate([x, up], axis=-1)
+  n, h, wd, c = x.shape
+  xp = np.zeros((n, h + 2, wd + 2, c))
+  xp[:, 1:-1, 1:-1] = x
+  out = np.zeros((n, h, wd, w.shape[0]))
+  for tap in range(9):
+    dy, dx = divmod(tap, 3)
+    out += np.einsum("nhwc,oc->nhwo", xp[:, dy : dy + h, dx : dx + wd], w[:, tap, :])
+  if bias is not None:
+    out += bias
+  if relu:
+    out = np.maximum(out, 0.0)
+  if mask is not None:
+    out = np.where(mask > 0, out, 0.0)
+  return out
+
+
+def test_conv_argument_errors_without_a_gpu():
+  from mujoco_warp_pbr_gb300 import _lib
+
+  lib = _lib.load()
+  c = _lib.Conv(in_=16, weight=16, out=16, nimg=1, height=8, width=24, c_in=16, c_out=16)
+  assert lib.mjpbr_conv3x3_bf16(ctypes.byref(c), None) == _lib.ERR_ARG
+  assert b"width 24" in lib.mjpbr_last_error()
+  c = _lib.Conv(in_=16, weight=16, out=16, nimg=1, height=8, width=16, c_in=24, c_out=16)
+  assert lib.mjpbr_conv3x3_bf16(ctypes.byref(c), None) == _lib.ERR_ARG
+  assert b"multiples of 16" in lib.mjpbr_last_error()
+  c = _lib.Conv(in_=16, weight=16, out=16, nimg=1, height=4, width=16, c_in=16, c_out=16)
+  assert lib.mjpbr_conv3x3_bf16(ctypes.byref(c), None) == _lib.ERR_ARG
+  assert b"height 4" in lib.mjpbr_last_error()
+
+
+CASES = [
+  # nimg, h, w, c1, c2, cout, bias, relu, mask
+  (2, 16, 16, 16, 0, 32, False, False, False),
+  (1, 8, 128, 32, 0, 48, True, True, False),
+  (2, 32, 32, 32, 16, 64, True, True, False),
+  (1, 4, 256, 16, 0, 16, False, False, True),
+  (3, 16, 64, 48, 96, 160, True, False, True),
+  (1, 16, 16, 96, 0, 256, True, True, False),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("nimg,h,w,c1,c2,cout,use_bias,relu,use_mask", CASES)
+def test_conv3x3_matches_cpu(nimg, h, w, c1, c2, cout, use_bias, relu, use_mask):
+  from mujoco_warp_pbr_gb300 import _lib
+
+  g = torch.Generator().manual_seed(nimg * 1000 + h * 10 + w + c1 + c2 + cout)
+  x = (torch.rand((nimg, h, w, c1), generator=g) * 2 - 1).to(torch.bfloat16)
+  x2 = (torch.rand((nimg, h // 2, w // 2, c2), generator=g) * 2 - 1).to(torch.bfloat16) if c2 else None
+  wt = ((torch.rand((cout, 9, c1 + c2), generator=g) * 2 - 1) / np.sqrt(9 * (c1 + c2))).to(torch.bfloat16)
+  bias = (torch.rand(cout, generator=g) - 0.5) if use_bias else None
+  mask = (torch.rand((nimg, h, w, cout), generator=g) - 0.3).to(torch.bfloat16) if use_mask else None
+  ref = conv_ref(
+    x.float().numpy().astype(np.float64),
+    wt.float().numpy().astype(np.float64),
+    None if bias is None else bias.numpy().astype(np.float64),
+    None if x2 is None else x2.float().numpy().astype(np.float64),
+    relu,
+    None if mask is None else mask.float().numpy(),
+  )
+  dev = {k: (v.cuda() if v is not None else None) for k, v in {"x": x, "x2": x2, "w": wt, "b": bias, "m": mask}.items()}
+  out = torch.zeros((nimg, h, w, cout), dtype=torch.bfloat16, device="cuda")
+  out32 = torch.zeros((nimg, h, w, cout), dtype=torch.float32, device="cuda")
+  err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+  def ptr(t):
+    return t.data_ptr() if t is not None else None
+
+  c = _lib.Conv(
+    in_=ptr(dev["x"]), in2=ptr(dev["x2"]), weight=ptr(dev["w"]), bias=ptr(dev["b"]), out=ptr(out), out_f32=ptr(out32),
+    mask=ptr(dev["m"]), error_word=ptr(err), nimg=nimg, height=h, width=w, c_in=c1, c_in2=c2, c_out=cout, relu=int(relu),
+  )
+  _lib.call("mjpbr_conv3x3_bf16", ctypes.byref(c), torch.cuda.current_stream().cuda_stream)
+  torch.cuda.synchronize()
+  assert int(err.item()) == 0
+  np.testing.assert_allclose(out32.cpu().numpy(), ref, rtol=1e-4, atol=1e-4)
+  np.testing.assert_allclose(out.float().cpu().numpy(), ref, rtol=1e-2, atol=1e-2)
