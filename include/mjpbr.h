@@ -110,6 +110,21 @@ typedef struct MjpbrConv {
   int32_t pad_;
 } MjpbrConv;
 
+/* Weight and bias gradients of a 3x3 convolution layer (same tensors and constraints as
+ * MjpbrConv): grad_weight (c_out, 9, c_in + c_in2) += sum over pixels of grad_out (x) the shifted
+ * input, grad_bias (c_out) += sum of grad_out; FP32, accumulated into the existing values. */
+typedef struct MjpbrConvGrad {
+  const uint16_t* in;
+  const uint16_t* in2;
+  const uint16_t* grad_out;
+  float* grad_weight;
+  float* grad_bias;
+  int32_t* error_word;
+  int32_t nimg, height, width, c_in, c_in2, c_out;
+  int32_t tiles_per_cta; /* 128-pixel tiles each CTA accumulates before its atomic reduction (0: 64) */
+  int32_t pad_;
+} MjpbrConvGrad;
+
 /* One mipmapped 2D texture inside MjpbrScene.tex_data (RGBA, row-major levels). */
 typedef struct MjpbrTexture {
   int32_t format;   /* MjpbrTexFormat */
@@ -355,6 +370,9 @@ int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, i
 /* Forward 3x3 convolution (see MjpbrConv); also the input-gradient pass with the flipped,
  * transposed weights. No counterpart in the reference (its denoiser is the a-trous filter). */
 int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream);
+
+/* Weight / bias gradients of a 3x3 convolution (see MjpbrConvGrad), on the tensor cores. */
+int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream);
 
 /* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
  * caller: the per-world blocks and the path tracer's work counter live in static device memory of

@@ -270,6 +270,27 @@ class Conv(ctypes.Structure):
   ]
 
 
+class ConvGrad(ctypes.Structure):
+  """MjpbrConvGrad: weight / bias gradients of a 3x3 convolution layer."""
+
+  _fields_ = [
+    ("in_", c_vp),
+    ("in2", c_vp),
+    ("grad_out", c_vp),
+    ("grad_weight", c_vp),
+    ("grad_bias", c_vp),
+    ("error_word", c_vp),
+    ("nimg", c_i32),
+    ("height", c_i32),
+    ("width", c_i32),
+    ("c_in", c_i32),
+    ("c_in2", c_i32),
+    ("c_out", c_i32),
+    ("tiles_per_cta", c_i32),
+    ("pad_", c_i32),
+  ]
+
+
 # name -> (restype, argtypes)
 _SIGNATURES = {
   "mjpbr_abi_version": (ctypes.c_int, []),
@@ -281,6 +302,7 @@ _SIGNATURES = {
   "mjpbr_refit_render_static": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),
   "mjpbr_gemm_bf16": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp]),
   "mjpbr_conv3x3_bf16": (ctypes.c_int, [ctypes.POINTER(Conv), c_vp]),
+  "mjpbr_conv3x3_wgrad_bf16": (ctypes.c_int, [ctypes.POINTER(ConvGrad), c_vp]),
   "mjpbr_get_rgb": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),
   "mjpbr_get_depth": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_f32, c_vp, c_i32, c_vp]),
   "mjpbr_get_segmentation": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),

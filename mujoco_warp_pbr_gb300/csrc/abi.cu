@@ -174,6 +174,11 @@ int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream) {
   return conv3x3_launch(*conv, static_cast<cudaStream_t>(stream));
 }
 
+int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream) {
+  if (!grad) return set_error(MJPBR_ERR_ARG, "grad is NULL");
+  return conv3x3_wgrad_launch(*grad, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                     void* stream) {
   return gemm_bf16_launch(a, b, d, m, n, k, error_word, static_cast<cudaStream_t>(stream));

@@ -26,6 +26,7 @@ int prefilter_launch(const MjpbrTexture* radiance, const uint8_t* data, int32_t 
                      int32_t nsample, uint16_t* stack, cudaStream_t stream);
 int denoise_launch(const MjpbrScene& s, cudaStream_t stream);
 int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream);
+int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream);
 int gemm_bf16_launch(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                      cudaStream_t stream);
 

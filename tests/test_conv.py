@@ -95,3 +95,57 @@ def test_conv3x3_matches_cpu(nimg, h, w, c1, c2, cout, use_bias, relu, use_mask)
   assert int(err.item()) == 0
   np.testing.assert_allclose(out32.cpu().numpy(), ref, rtol=1e-4, atol=1e-4)
   np.testing.assert_allclose(out.float().cpu().numpy(), ref, rtol=1e-2, atol=1e-2)
+
+
+def wgrad_ref(x, dy, x2=None):
+  if x2 is not None:
+    up = np.repeat(np.repeat(x2, 2, axis=1), 2, axis=2)
+    x = np.concatenate([x, up], axis=-1)
+  n, h, w, c = x.shape
+  xp = np.zeros((n, h + 2, w + 2, c))
+  xp[:, 1:-1, 1:-1] = x
+  gw = np.zeros((dy.shape[-1], 9, c))
+  for tap in range(9):
+    ty, tx = divmod(tap, 3)
+    gw[:, tap, :] = np.einsum("nhwo,nhwc->oc", dy, xp[:, ty : ty + h, tx : tx + w])
+  return gw, dy.sum(axis=(0, 1, 2))
+
+
+WGRAD_CASES = [
+  # nimg, h, w, c1, c2, cout, tiles_per_cta
+  (2, 16, 16, 16, 0, 32, 0),
+  (1, 8, 128, 32, 0, 48, 3),
+  (2, 32, 32, 32, 16, 64, 5),
+  (1, 4, 256, 16, 0, 16, 1),
+  (3, 16, 64, 48, 96, 96, 0),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("nimg,h,w,c1,c2,cout,per_cta", WGRAD_CASES)
+def test_conv3x3_wgrad_matches_cpu(nimg, h, w, c1, c2, cout, per_cta):
+  from mujoco_warp_pbr_gb300 import _lib
+
+  g = torch.Generator().manual_seed(nimg * 100 + h + w * 3 + c1 + c2 + cout)
+  x = (torch.rand((nimg, h, w, c1), generator=g) * 2 - 1).to(torch.bfloat16)
+  x2 = (torch.rand((nimg, h // 2, w // 2, c2), generator=g) * 2 - 1).to(torch.bfloat16) if c2 else None
+  dy = (torch.rand((nimg, h, w, cout), generator=g) * 2 - 1).to(torch.bfloat16)
+  ref_w, ref_b = wgrad_ref(
+    x.float().numpy().astype(np.float64), dy.float().numpy().astype(np.float64), None if x2 is None else x2.float().numpy().astype(np.float64)
+  )
+  gw = torch.full((cout, 9, c1 + c2), 0.5, dtype=torch.float32, device="cuda")  # accumulates into existing values
+  gb = torch.full((cout,), 0.25, dtype=torch.float32, device="cuda")
+  err = torch.zeros(1, dtype=torch.int32, device="cuda")
+  dx, dx2, ddy = x.cuda(), (x2.cuda() if x2 is not None else None), dy.cuda()
+  c = _lib.ConvGrad(
+    in_=dx.data_ptr(), in2=dx2.data_ptr() if dx2 is not None else None, grad_out=ddy.data_ptr(), grad_weight=gw.data_ptr(),
+    grad_bias=gb.data_ptr(), error_word=err.data_ptr(), nimg=nimg, height=h, width=w, c_in=c1, c_in2=c2, c_out=cout,
+    tiles_per_cta=per_cta,
+  )
+  _lib.call("mjpbr_conv3x3_wgrad_bf16", ctypes.byref(c), torch.cuda.current_stream().cuda_stream)
+  torch.cuda.synchronize()
+  assert int(err.item()) == 0
+  scale = np.sqrt(nimg * h * w)
+  np.testing.assert_allclose(gw.cpu().numpy(), ref_w + 0.5, rtol=1e-4, atol=1e-4 * scale)
+  np.testing.assert_allclose(gb.cpu().numpy(), ref_b + 0.25, rtol=1e-4, atol=1e-4 * scale)
