@@ -374,6 +374,41 @@ int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream);
 /* Weight / bias gradients of a 3x3 convolution (see MjpbrConvGrad), on the tensor cores. */
 int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream);
 
+/* ---- Learned denoiser building blocks (no counterpart in the reference). NHWC layouts, one
+ * image per world of camera `cam`; BF16 as raw 16-bit values. ---- */
+/* Network input (nworld, H, W, 16) BF16: log(1 + demodulated radiance), albedo, normal,
+ * log(1 + depth), zeros; from denoise_buffers[0] and aov_guide written by a denoising render. */
+int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, uint16_t* x0, void* stream);
+/* Demodulated training target (nworld, H, W, 4) FP32 from the FP64 sum of converged HDR frames
+ * (laid out like hdr_data) times inv_n, with the denoising render's albedo and emission. */
+int mjpbr_kpcn_target(const MjpbrScene* scene, int32_t cam, const double* hdr_sum, double inv_n, float* target, void* stream);
+/* acc[i] += src[i] in FP64. */
+int mjpbr_accumulate_f64(const float* src, double* acc, int64_t n, void* stream);
+/* 2 x 2 average pooling of BF16 (nimg, h, w, c). */
+int mjpbr_avgpool2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, void* stream);
+/* Softmax of 25 of the 32 FP32 logits per pixel, the 5 x 5 kernel applied to the radiance (float4
+ * records); weights (nimg, h, w, 25) may be NULL (inference); out (nimg, h, w, 4), w = 0. */
+int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
+                     void* stream);
+/* L1 and relative-MSE loss of out against target (float4 records): gradient, and the two sums
+ * added to sums[0..1]. */
+int mjpbr_kpcn_loss(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
+                    void* stream);
+/* Backward of mjpbr_kpcn_apply: BF16 logit gradients (nimg, h, w, 32). */
+int mjpbr_kpcn_apply_grad(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,
+                          int32_t h, int32_t w, void* stream);
+/* Gradient of a skip concatenation (FP32 (nimg, h, w, c1 + c2)): skip part to dskip (FP32), the
+ * upsampled part pooled (sum of 2 x 2) and masked by low > 0 into dlow (BF16, half resolution). */
+int mjpbr_split_concat_grad(const float* dcat, const uint16_t* low, float* dskip, uint16_t* dlow, int32_t nimg, int32_t h, int32_t w,
+                            int32_t c1, int32_t c2, void* stream);
+/* dact = (dskip + average-pool gradient of dpool) masked by act > 0 (dskip may be NULL). */
+int mjpbr_unpool_add_grad(const float* dskip, const float* dpool, const uint16_t* act, uint16_t* dact, int32_t nimg, int32_t h,
+                          int32_t w, int32_t c, void* stream);
+/* Adam step on FP32 parameters (gradient zeroed); refreshes the BF16 copy and, if flip, the
+ * (c_in, 9, c_out) tap-reversed copy of a convolution weight. */
+int mjpbr_adam(float* param, float* grad, float* m, float* v, uint16_t* copy, uint16_t* flip, int64_t n, int32_t cout, int32_t cin,
+               float lr, float beta1, float beta2, float eps, int32_t step, void* stream);
+
 /* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
  * caller: the per-world blocks and the path tracer's work counter live in static device memory of
  * the library (scene->world_blocks and scene->work_counter are ignored). For hosts that cannot

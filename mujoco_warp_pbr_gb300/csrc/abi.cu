@@ -179,6 +179,54 @@ int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream) {
   return conv3x3_wgrad_launch(*grad, static_cast<cudaStream_t>(stream));
 }
 
+int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, uint16_t* x0, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return kpcn_features_launch(*scene, cam, x0, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_kpcn_target(const MjpbrScene* scene, int32_t cam, const double* hdr_sum, double inv_n, float* target, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return kpcn_target_launch(*scene, cam, hdr_sum, inv_n, target, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_accumulate_f64(const float* src, double* acc, int64_t n, void* stream) {
+  return accumulate_f64_launch(src, acc, n, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_avgpool2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, void* stream) {
+  return avgpool2_launch(in, out, nimg, h, w, c, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
+                     void* stream) {
+  return kpcn_apply_launch(logits, radiance, weights, out, nimg, h, w, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_kpcn_loss(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
+                    void* stream) {
+  return kpcn_loss_launch(out, target, grad, sums, npix, w_l1, w_rel, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_kpcn_apply_grad(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,
+                          int32_t h, int32_t w, void* stream) {
+  return kpcn_apply_grad_launch(grad, weights, radiance, grad_logits, nimg, h, w, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_split_concat_grad(const float* dcat, const uint16_t* low, float* dskip, uint16_t* dlow, int32_t nimg, int32_t h, int32_t w,
+                            int32_t c1, int32_t c2, void* stream) {
+  return split_concat_grad_launch(dcat, low, dskip, dlow, nimg, h, w, c1, c2, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_unpool_add_grad(const float* dskip, const float* dpool, const uint16_t* act, uint16_t* dact, int32_t nimg, int32_t h,
+                          int32_t w, int32_t c, void* stream) {
+  return unpool_add_grad_launch(dskip, dpool, act, dact, nimg, h, w, c, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_adam(float* param, float* grad, float* m, float* v, uint16_t* copy, uint16_t* flip, int64_t n, int32_t cout, int32_t cin,
+               float lr, float beta1, float beta2, float eps, int32_t step, void* stream) {
+  return adam_launch(param, grad, m, v, copy, flip, n, cout, cin, lr, beta1, beta2, eps, step, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                     void* stream) {
   return gemm_bf16_launch(a, b, d, m, n, k, error_word, static_cast<cudaStream_t>(stream));

@@ -27,6 +27,22 @@ int prefilter_launch(const MjpbrTexture* radiance, const uint8_t* data, int32_t 
 int denoise_launch(const MjpbrScene& s, cudaStream_t stream);
 int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream);
 int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream);
+int kpcn_features_launch(const MjpbrScene& s, int32_t cam, uint16_t* x0, cudaStream_t st);
+int kpcn_target_launch(const MjpbrScene& s, int32_t cam, const double* hdr_sum, double inv_n, float* target, cudaStream_t st);
+int accumulate_f64_launch(const float* src, double* acc, int64_t n, cudaStream_t st);
+int avgpool2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st);
+int kpcn_apply_launch(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
+                      cudaStream_t st);
+int kpcn_loss_launch(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
+                     cudaStream_t st);
+int kpcn_apply_grad_launch(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,
+                           int32_t h, int32_t w, cudaStream_t st);
+int split_concat_grad_launch(const float* dcat, const uint16_t* low, float* dskip, uint16_t* dlow, int32_t nimg, int32_t h, int32_t w,
+                             int32_t c1, int32_t c2, cudaStream_t st);
+int unpool_add_grad_launch(const float* dskip, const float* dpool, const uint16_t* act, uint16_t* dact, int32_t nimg, int32_t h,
+                           int32_t w, int32_t c, cudaStream_t st);
+int adam_launch(float* param, float* grad, float* m, float* v, uint16_t* copy, uint16_t* flip, int64_t n, int32_t cout, int32_t cin,
+                float lr, float beta1, float beta2, float eps, int32_t step, cudaStream_t st);
 int gemm_bf16_launch(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                      cudaStream_t stream);
 
