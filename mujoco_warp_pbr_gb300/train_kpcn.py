@@ -1,0 +1,202 @@
+"""Training and evaluation of the learned denoiser on pairs the path tracer renders itself.
+
+A pair is one world's 128 x 128 image of a seeded path-traced scene (synthetic.path_scene: the
+primitive scene with emissive quads, per-world materials and emission): the network input and the
+noisy demodulated radiance from a denoising render at 1-4 spp, and the converged target: many
+path-traced passes with other seeds, their HDR summed in FP64 on the device
+(mjpbr_accumulate_f64) and demodulated with the noisy render's albedo and emission
+(mjpbr_kpcn_target).
+
+    python -m mujoco_warp_pbr_gb300.train_kpcn --out weights.npz [--crops 2048 --target-spp 1024]
+
+prints one JSON line: training time and loss curve, and on held-out scenes the relative MSE
+(mean((x - ref)^2 / (ref^2 + 0.01)) on linear HDR) against 4096-spp references of the learned
+denoiser at 2 spp, the a-trous filter (5 iterations) at 16 spp and plain path tracing at 16 spp,
+with the Mpix/s of each pipeline (render + denoise) measured with CUDA events.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+import mujoco_warp_pbr_gb300 as mjpbr
+from mujoco_warp_pbr_gb300 import _lib
+from mujoco_warp_pbr_gb300 import kpcn as kpcn_lib
+from mujoco_warp_pbr_gb300 import synthetic
+from mujoco_warp_pbr_gb300.render import scene as scene_descriptor
+
+
+@dataclass
+class Frame:
+  """A seeded batch of worlds on the device, with one context per sample count."""
+
+  sc: synthetic.SyntheticScene
+  m: object
+  d: object
+
+  def context(self, **opts):
+    options = {**self.sc.options, **opts}
+    rc = mjpbr.create_render_context(self.sc.mjm, self.sc.nworld, data=self.sc.mjd, **options)
+    synthetic.apply_per_world(self.sc, self.m, rc)
+    return rc
+
+
+def make_frame(seed: int, nworld: int, res: int) -> Frame:
+  sc = synthetic.path_scene(seed=seed, nworld=nworld, res=res, spp=2)
+  m = mjpbr.put_model(sc.mjm)
+  d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=nworld)
+  return Frame(sc, m, d)
+
+
+def converged_hdr(fr: Frame, spp: int, per_pass: int = 256, seed0: int = 1_000_003) -> torch.Tensor:
+  """FP64 sum over passes of the HDR (nworld, npix, 3) and the pass count (mean = sum / passes)."""
+  rc = fr.context(path_samples=min(per_pass, spp), render_hdr=True)
+  passes = max(1, spp // per_pass)
+  acc = torch.zeros(rc.hdr_data.shape, dtype=torch.float64, device=rc.device)
+  mjpbr.refit_bvh(fr.m, fr.d, rc)
+  stream = torch.cuda.current_stream().cuda_stream
+  for k in range(passes):
+    mjpbr.render(fr.m, fr.d, rc, seed=seed0 + 7919 * k)
+    _lib.call("mjpbr_accumulate_f64", rc.hdr_data.data_ptr(), acc.data_ptr(), rc.hdr_data.numel(), stream)
+  return acc / passes
+
+
+def noisy_pair(fr: Frame, spp: int, seed: int, gt_hdr: torch.Tensor | None):
+  """(x0, radiance, target or None, rc) of a denoising render at spp."""
+  rc = fr.context(path_samples=spp, denoise=True, render_hdr=True)
+  mjpbr.refit_bvh(fr.m, fr.d, rc)
+  mjpbr.render(fr.m, fr.d, rc, seed=seed, denoise=False)
+  s = scene_descriptor(fr.m, fr.d, rc)
+  n = fr.sc.nworld
+  w, h = rc.base.cam_res[0]
+  stream = torch.cuda.current_stream().cuda_stream
+  x0 = torch.zeros((n, h, w, kpcn_lib.FEATURES), dtype=torch.bfloat16, device=rc.device)
+  _lib.call("mjpbr_kpcn_features", ctypes.byref(s), 0, x0.data_ptr(), stream)
+  radiance = rc.denoise_buffers[0].view(n, h, w, 4).clone()
+  target = None
+  if gt_hdr is not None:
+    hsum = gt_hdr.contiguous()
+    target = torch.zeros((n, h, w, 4), dtype=torch.float32, device=rc.device)
+    _lib.call("mjpbr_kpcn_target", ctypes.byref(s), 0, hsum.data_ptr(), ctypes.c_double(1.0), target.data_ptr(), stream)
+  return x0, radiance, target, rc
+
+
+def make_dataset(crops: int, frame_worlds: int, res: int, target_spp: int, seed0: int = 100):
+  xs, rs, ts = [], [], []
+  nframes = (crops + frame_worlds - 1) // frame_worlds
+  for f in range(nframes):
+    fr = make_frame(seed0 + f, frame_worlds, res)
+    gt = converged_hdr(fr, target_spp)
+    spp = 1 + f % 4  # 1-4 spp inputs
+    x0, rad, tgt, _ = noisy_pair(fr, spp, seed=17 + f, gt_hdr=gt)
+    xs.append(x0)
+    rs.append(rad)
+    ts.append(tgt)
+  return torch.cat(xs)[:crops], torch.cat(rs)[:crops], torch.cat(ts)[:crops]
+
+
+def train(net: kpcn_lib.KPCN, data, steps: int, batch: int, lr: float, seed: int = 0) -> list[float]:
+  x0, rad, tgt = data
+  n = x0.shape[0]
+  g = torch.Generator(device="cpu").manual_seed(seed)
+  losses = []
+  for step in range(steps):
+    idx = torch.randint(0, n, (batch,), generator=g).to(x0.device)
+    lr_t = lr * 0.5 * (1.0 + np.cos(np.pi * step / steps))
+    sums = net.train_step(x0[idx].contiguous(), rad[idx].contiguous(), tgt[idx].contiguous(), lr_t)
+    if step % 50 == 0 or step == steps - 1:
+      losses.append(float(sums.sum().item()))
+  return losses
+
+
+def rel_mse(x: torch.Tensor, ref: torch.Tensor) -> float:
+  x, ref = x.double(), ref.double()
+  return float(((x - ref) ** 2 / (ref * ref + 1.0e-2)).mean().item())
+
+
+def timed(fn, reps: int = 3) -> float:
+  fn()
+  torch.cuda.synchronize()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record()
+  for _ in range(reps):
+    fn()
+  e1.record()
+  torch.cuda.synchronize()
+  return e0.elapsed_time(e1) / reps
+
+
+def evaluate(net: kpcn_lib.KPCN, nworld: int, res: int, ref_spp: int, seed: int = 9000) -> dict:
+  """relMSE against ref_spp references and Mpix/s of the three pipelines on a held-out frame."""
+  fr = make_frame(seed, nworld, res)
+  ref = converged_hdr(fr, ref_spp).float()
+  npix = nworld * res * res
+  out = {"ref_spp": ref_spp, "nworld": nworld, "res": res}
+  # learned denoiser at 2 spp
+  rc2 = fr.context(path_samples=2, denoise=True, render_hdr=True)
+  mjpbr.refit_bvh(fr.m, fr.d, rc2)
+
+  def learned():
+    mjpbr.render(fr.m, fr.d, rc2, seed=5, denoise=False)
+    net.denoise(fr.m, fr.d, rc2)
+
+  ms = timed(learned)
+  out["learned_2spp"] = {"rel_mse": rel_mse(rc2.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  # a-trous at 16 spp, 5 iterations
+  rc16 = fr.context(path_samples=16, denoise=True, denoise_iterations=5, render_hdr=True)
+  mjpbr.refit_bvh(fr.m, fr.d, rc16)
+  ms = timed(lambda: mjpbr.render(fr.m, fr.d, rc16, seed=5))
+  out["atrous_16spp"] = {"rel_mse": rel_mse(rc16.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  # a-trous at 2 spp and plain 16 / 2 spp for context
+  rca = fr.context(path_samples=2, denoise=True, denoise_iterations=5, render_hdr=True)
+  mjpbr.refit_bvh(fr.m, fr.d, rca)
+  ms = timed(lambda: mjpbr.render(fr.m, fr.d, rca, seed=5))
+  out["atrous_2spp"] = {"rel_mse": rel_mse(rca.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  for spp in (2, 16):
+    rcp = fr.context(path_samples=spp, render_hdr=True)
+    mjpbr.refit_bvh(fr.m, fr.d, rcp)
+    ms = timed(lambda rcp=rcp: mjpbr.render(fr.m, fr.d, rcp, seed=5))
+    out[f"plain_{spp}spp"] = {"rel_mse": rel_mse(rcp.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  out["speedup_learned2_vs_atrous16"] = out["atrous_16spp"]["ms"] / out["learned_2spp"]["ms"]
+  return out
+
+
+def main() -> None:
+  p = argparse.ArgumentParser()
+  p.add_argument("--out", default="kpcn_weights.npz")
+  p.add_argument("--crops", type=int, default=2048)
+  p.add_argument("--frame-worlds", type=int, default=256)
+  p.add_argument("--res", type=int, default=128)
+  p.add_argument("--target-spp", type=int, default=1024)
+  p.add_argument("--steps", type=int, default=2000)
+  p.add_argument("--batch", type=int, default=16)
+  p.add_argument("--lr", type=float, default=1e-3)
+  p.add_argument("--eval-worlds", type=int, default=64)
+  p.add_argument("--eval-ref-spp", type=int, default=4096)
+  p.add_argument("--init", default=None, help="weights to start from")
+  args = p.parse_args()
+  t0 = time.time()
+  data = make_dataset(args.crops, args.frame_worlds, args.res, args.target_spp)
+  torch.cuda.synchronize()
+  t_data = time.time() - t0
+  net = kpcn_lib.KPCN.load(args.init) if args.init else kpcn_lib.KPCN("cuda", seed=0)
+  t1 = time.time()
+  losses = train(net, data, args.steps, args.batch, args.lr)
+  torch.cuda.synchronize()
+  t_train = time.time() - t1
+  assert int(net.error.item()) == 0
+  net.save(args.out)
+  del data
+  ev = evaluate(net, args.eval_worlds, args.res, args.eval_ref_spp)
+  print(json.dumps({"data_s": t_data, "train_s": t_train, "steps": args.steps, "batch": args.batch, "crops": args.crops, "target_spp": args.target_spp, "losses": losses, "eval": ev}))
+
+
+if __name__ == "__main__":
+  main()
