@@ -87,6 +87,8 @@ class Net:
   def __init__(self, params: dict[str, tuple[np.ndarray, np.ndarray]], bf16: bool = True):
     self.p = {k: (np.asarray(w, np.float64), np.asarray(b, np.float64)) for k, (w, b) in params.items()}
     self.q = round_bf16 if bf16 else (lambda x: x)
+    # gradients the GPU stores as BF16 (the inputs of its input- and weight-gradient convolutions)
+    self.qg = self.q
     if bf16:
       self.p = {k: (round_bf16(w), b) for k, (w, b) in self.p.items()}
 
@@ -131,36 +133,40 @@ class Net:
     dlog = np.zeros(a["logits"].shape)
     dlog[..., :TAPS] = wts * (gk - np.sum(wts * gk, -1, keepdims=True))
 
+    qg = self.qg
+    dlog = qg(dlog)
+
     def back(name, x, dy, mask=None):
       dx, dw, db = conv_backward(x, self.p[name][0], dy)
       g[name] = (dw, db)
-      return dx * (mask > 0) if mask is not None else dx
+      return qg(dx * (mask > 0)) if mask is not None else dx
 
     d = back("head", a["v0"], dlog, a["v0"])
     d = back("d0b", a["u0"], d, a["u0"])
     dcat = back("d0a", np.concatenate([a["s0"], up(a["v1"])], -1), d)
     c0 = a["s0"].shape[-1]
     dskip0 = dcat[..., :c0]
-    d = pool(dcat[..., c0:]) * 4.0 * (a["v1"] > 0)
+    d = qg(pool(dcat[..., c0:]) * 4.0 * (a["v1"] > 0))
     d = back("d1b", a["u1"], d, a["u1"])
     dcat = back("d1a", np.concatenate([a["s1"], up(a["v2"])], -1), d)
     c1 = a["s1"].shape[-1]
     dskip1 = dcat[..., :c1]
-    d = pool(dcat[..., c1:]) * 4.0 * (a["v2"] > 0)
+    d = qg(pool(dcat[..., c1:]) * 4.0 * (a["v2"] > 0))
     d = back("d2b", a["u2"], d, a["u2"])
     dcat = back("d2a", np.concatenate([a["s2"], up(a["b3"])], -1), d)
     c2 = a["s2"].shape[-1]
     dskip2 = dcat[..., :c2]
-    d = pool(dcat[..., c2:]) * 4.0 * (a["b3"] > 0)
+    d = qg(pool(dcat[..., c2:]) * 4.0 * (a["b3"] > 0))
     d = back("e3b", a["a3"], d, a["a3"])
     dp = back("e3a", a["p3"], d)
-    d = (dskip2 + up(dp) * 0.25) * (a["s2"] > 0)
+    d = qg((dskip2 + up(dp) * 0.25) * (a["s2"] > 0))
     d = back("e2b", a["a2"], d, a["a2"])
     dp = back("e2a", a["p2"], d)
-    d = (dskip1 + up(dp) * 0.25) * (a["s1"] > 0)
+    d = qg((dskip1 + up(dp) * 0.25) * (a["s1"] > 0))
     d = back("e1b", a["a1"], d, a["a1"])
     dp = back("e1a", a["p1"], d)
-    d = (dskip0 + up(dp) * 0.25) * (a["s0"] > 0)
+    d = qg((dskip0 + up(dp) * 0.25) * (a["s0"] > 0))
+    self.ds0 = d
     d = back("e0b", a["a0"], d, a["a0"])
     back("e0a", a["x0"], d)
     return g

@@ -74,11 +74,28 @@ def _gpu_net(params):
   return net
 
 
-@pytest.mark.gpu
-@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
-def test_gpu_forward_and_gradients_match_oracle():
-  params = _params(3)
-  x0, rad, tgt = _inputs(4, n=2)
+# (layer, forward inputs, incoming gradient, outgoing gradient, ReLU mask of the outgoing one)
+BACKWARD_CHAIN = [
+  ("head", ("v0",), "dlogits", "dv0", "v0"),
+  ("d0b", ("u0",), "dv0", "du0", "u0"),
+  ("d0a", ("s0", "v1"), "du0", "dcat0", None),
+  ("d1b", ("u1",), "dv1", "du1", "u1"),
+  ("d1a", ("s1", "v2"), "du1", "dcat1", None),
+  ("d2b", ("u2",), "dv2", "du2", "u2"),
+  ("d2a", ("s2", "b3"), "du2", "dcat2", None),
+  ("e3b", ("a3",), "db3", "da3", "a3"),
+  ("e3a", ("p3",), "da3", "dp3", None),
+  ("e2b", ("a2",), "ds2", "da2", "a2"),
+  ("e2a", ("p2",), "da2", "dp2", None),
+  ("e1b", ("a1",), "ds1", "da1", "a1"),
+  ("e1a", ("p1",), "da1", "dp1", None),
+  ("e0b", ("a0",), "ds0", "da0", "a0"),
+  ("e0a", ("x0",), "da0", None, None),
+]
+
+
+def _gpu_step(params, n=2):
+  x0, rad, tgt = _inputs(4, n=n)
   net = _gpu_net(params)
   x0_d = torch.as_tensor(x0, dtype=torch.float32).to(torch.bfloat16).cuda()
   rad_d = torch.as_tensor(rad, dtype=torch.float32).cuda()
@@ -89,20 +106,73 @@ def test_gpu_forward_and_gradients_match_oracle():
   net.backward(x0_d, rad_d)
   torch.cuda.synchronize()
   assert int(net.error.item()) == 0
+  ws = {k: v.float().cpu().numpy().astype(np.float64) for k, v in net.workspace(n, 64, 128).items()}
+  ws["x0"] = x0_d.float().cpu().numpy().astype(np.float64)
+  return net, ws, out.cpu().numpy(), (x0, rad, tgt)
 
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+def test_gpu_backward_steps_match_oracle_on_their_own_inputs():
+  """Every backward operation of the GPU network, recomputed in float64 from the tensors the GPU
+  itself fed it: weight and bias gradients (tensor-core wgrad), input gradients (tensor-core
+  dgrad), their ReLU masks and BF16 rounding, the skip / pooling gradient routing and the kernel
+  softmax backward."""
+  params = _params(3)
+  net, ws, _, (_, rad, _) = _gpu_step(params)
+  # kernel softmax backward
+  lg = ws["logits"][..., : kpcn.TAPS]
+  e = np.exp(lg - lg.max(-1, keepdims=True))
+  wts = e / e.sum(-1, keepdims=True)
+  _, _, taps = ko.apply_kernel(ws["logits"], rad)
+  gk = np.stack([np.sum(ws["gout"][..., :3] * t, -1) for t in taps], -1)
+  dlog = wts * (gk - np.sum(wts * gk, -1, keepdims=True))
+  np.testing.assert_allclose(ws["dlogits"][..., : kpcn.TAPS], ko.round_bf16(dlog), rtol=1e-2, atol=1e-2 * np.abs(dlog).max())
+  for name, ins, dy, dx_name, mask in BACKWARD_CHAIN:
+    x = ws[ins[0]] if len(ins) == 1 else np.concatenate([ws[ins[0]], ko.up(ws[ins[1]])], -1)
+    dx, dw, db = ko.conv_backward(x, ko.round_bf16(params[name][0]), ws[dy])
+    layer = net.layers[name]
+    for got, ref, what in ((layer.gw.cpu().numpy(), dw, "weight"), (layer.gb.cpu().numpy(), db, "bias")):
+      err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-12)
+      assert err < 2e-3, f"{name}: {what} gradient relative error {err:.3g} on the GPU's own inputs"
+    if dx_name is None:
+      continue
+    if mask is not None:
+      ref = ko.round_bf16(dx * (ws[mask] > 0))
+      np.testing.assert_allclose(ws[dx_name], ref, rtol=2e-2, atol=1e-2 * np.abs(ref).max(), err_msg=name)
+    else:
+      np.testing.assert_allclose(ws[dx_name], dx, rtol=1e-3, atol=1e-4 * np.abs(dx).max(), err_msg=name)
+  # gradient routing through the concatenations and poolings
+  for dcat, skip, low, dskip, dlow in (("dcat0", "s0", "v1", "dskip0", "dv1"), ("dcat1", "s1", "v2", "dskip1", "dv2"), ("dcat2", "s2", "b3", "dskip2", "db3")):
+    c1 = ws[skip].shape[-1]
+    np.testing.assert_array_equal(ws[dskip], ws[dcat][..., :c1])
+    ref = ko.round_bf16(ko.pool(ws[dcat][..., c1:]) * 4.0 * (ws[low] > 0))
+    np.testing.assert_allclose(ws[dlow], ref, rtol=1e-2, atol=1e-3 * np.abs(ref).max())
+  for dskip, dp, act, out in (("dskip2", "dp3", "s2", "ds2"), ("dskip1", "dp2", "s1", "ds1"), ("dskip0", "dp1", "s0", "ds0")):
+    ref = ko.round_bf16((ws[dskip] + ko.up(ws[dp]) * 0.25) * (ws[act] > 0))
+    np.testing.assert_allclose(ws[out], ref, rtol=1e-2, atol=1e-3 * np.abs(ref).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+def test_gpu_forward_and_gradients_match_oracle():
+  """End to end against the float64 oracle with the same BF16 weights and storage points: the
+  output within BF16 precision, every layer's gradient pointing the same way (cosine similarity;
+  BF16 rounding differences compound through the 15 layers, so elementwise equality is not
+  expected)."""
+  params = _params(3)
+  net, ws, out, (x0, rad, tgt) = _gpu_step(params)
   ref = ko.Net(params, bf16=True)
   ref_out = ref.forward(ko.round_bf16(x0), rad)
-  np.testing.assert_allclose(out.cpu().numpy()[..., :3], ref_out, rtol=2e-2, atol=2e-2)
-  _, gout = ko.loss(out.cpu().numpy()[..., :3].astype(np.float64), tgt)
+  np.testing.assert_allclose(out[..., :3], ref_out, rtol=2e-2, atol=2e-2)
+  _, gout = ko.loss(out[..., :3].astype(np.float64), tgt)
   g = ref.backward(gout)
   for name, layer in net.layers.items():
-    gw = layer.gw.cpu().numpy()
-    gb = layer.gb.cpu().numpy()
-    rw, rb = g[name]
-    err_w = np.linalg.norm(gw - rw) / max(np.linalg.norm(rw), 1e-12)
-    err_b = np.linalg.norm(gb - rb) / max(np.linalg.norm(rb), 1e-12)
-    assert err_w < 0.05, f"{name}: weight gradient relative error {err_w:.3g}"
-    assert err_b < 0.05 or np.linalg.norm(rb) < 1e-9, f"{name}: bias gradient relative error {err_b:.3g}"
+    gw = layer.gw.cpu().numpy().ravel()
+    rw = g[name][0].ravel()
+    cos = float(gw @ rw / (np.linalg.norm(gw) * np.linalg.norm(rw)))
+    ratio = float(np.linalg.norm(gw) / np.linalg.norm(rw))
+    assert cos > 0.95 and 0.8 < ratio < 1.25, f"{name}: cosine {cos:.4f}, norm ratio {ratio:.3f}"
 
 
 @pytest.mark.gpu
