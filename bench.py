@@ -449,9 +449,29 @@ def run(args) -> None:
     }
     if args.workload == "mesh_ibl" and not args.no_path_tier:
       line["path_tier"] = path_tier(dev, max(3, args.steps // 2))
+      if not args.no_learned:
+        line["learned_denoiser"] = learned_denoiser(args)
     print(json.dumps(line))
   if world_size > 1:
     dist.destroy_process_group()
+
+
+WEIGHTS = ROOT / "mujoco_warp_pbr_gb300" / "weights" / "kpcn_path.npz"
+
+
+def learned_denoiser(args) -> dict | None:
+  """Learned denoiser at 2 spp against the a-trous filter at 16 spp (and plain path tracing) on a
+  held-out path-traced frame: relative MSE against a converged reference and Mpix/s of each
+  pipeline (render + denoise), from the committed trained weights."""
+  if not WEIGHTS.exists():
+    return None
+  from mujoco_warp_pbr_gb300 import kpcn
+  from mujoco_warp_pbr_gb300 import train_kpcn
+
+  net = kpcn.KPCN.load(WEIGHTS)
+  out = train_kpcn.evaluate(net, nworld=args.learned_worlds, res=128, ref_spp=args.learned_ref_spp)
+  out["weights"] = str(WEIGHTS.relative_to(ROOT))
+  return out
 
 
 def run_batched(args) -> None:
@@ -576,6 +596,9 @@ def main() -> None:
   p.add_argument("--workload", choices=["mesh_ibl", "primitives", "path", "batched"], default="mesh_ibl")
   p.add_argument("--spp", type=int, default=2)
   p.add_argument("--no-path-tier", action="store_true")
+  p.add_argument("--no-learned", action="store_true")
+  p.add_argument("--learned-worlds", type=int, default=256)
+  p.add_argument("--learned-ref-spp", type=int, default=1024)
   p.add_argument("--nworld", type=int, default=None)
   p.add_argument("--res", type=int, default=None)
   p.add_argument("--seed", type=int, default=0)

@@ -377,7 +377,8 @@ int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream);
 /* ---- Learned denoiser building blocks (no counterpart in the reference). NHWC layouts, one
  * image per world of camera `cam`; BF16 as raw 16-bit values. ---- */
 /* Network input (nworld, H, W, 16) BF16: log(1 + demodulated radiance), albedo, normal,
- * log(1 + depth), zeros; from denoise_buffers[0] and aov_guide written by a denoising render. */
+ * log(1 + depth), log(1 + standard deviation of the mean's luminance), zeros; from
+ * denoise_buffers[0] and aov_guide written by a denoising render. */
 int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, uint16_t* x0, void* stream);
 /* Demodulated training target (nworld, H, W, 4) FP32 from the FP64 sum of converged HDR frames
  * (laid out like hdr_data) times inv_n, with the denoising render's albedo and emission. */
@@ -391,9 +392,13 @@ int mjpbr_avgpool2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t
 int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
                      void* stream);
 /* L1 and relative-MSE loss of out against target (float4 records): gradient, and the two sums
- * added to sums[0..1]. */
-int mjpbr_kpcn_loss(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
-                    void* stream);
+ * added to sums[0..1]. With scale and offset (float4 records, see mjpbr_kpcn_remod; may be NULL)
+ * both are first mapped to HDR as offset + x * scale. */
+int mjpbr_kpcn_loss(const float* out, const float* target, const float* scale, const float* offset, float* grad, float* sums,
+                    int64_t npix, float w_l1, float w_rel, void* stream);
+/* The per-pixel HDR mapping of the demodulated radiance of camera `cam` (nworld, H, W, 4) each:
+ * scale = max(albedo, 0.01) / exposure, offset = exposed first-hit emission / exposure. */
+int mjpbr_kpcn_remod(const MjpbrScene* scene, int32_t cam, float* scale, float* offset, void* stream);
 /* Backward of mjpbr_kpcn_apply: BF16 logit gradients (nimg, h, w, 32). */
 int mjpbr_kpcn_apply_grad(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,
                           int32_t h, int32_t w, void* stream);

@@ -308,7 +308,8 @@ _SIGNATURES = {
   "mjpbr_accumulate_f64": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int64, c_vp]),
   "mjpbr_avgpool2_bf16": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp]),
   "mjpbr_kpcn_apply": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp]),
-  "mjpbr_kpcn_loss": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_vp]),
+  "mjpbr_kpcn_loss": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_vp]),
+  "mjpbr_kpcn_remod": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_vp, c_vp]),
   "mjpbr_kpcn_apply_grad": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp]),
   "mjpbr_split_concat_grad": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp]),
   "mjpbr_unpool_add_grad": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp]),

@@ -202,9 +202,14 @@ int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights,
   return kpcn_apply_launch(logits, radiance, weights, out, nimg, h, w, static_cast<cudaStream_t>(stream));
 }
 
-int mjpbr_kpcn_loss(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
-                    void* stream) {
-  return kpcn_loss_launch(out, target, grad, sums, npix, w_l1, w_rel, static_cast<cudaStream_t>(stream));
+int mjpbr_kpcn_loss(const float* out, const float* target, const float* scale, const float* offset, float* grad, float* sums,
+                    int64_t npix, float w_l1, float w_rel, void* stream) {
+  return kpcn_loss_launch(out, target, scale, offset, grad, sums, npix, w_l1, w_rel, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_kpcn_remod(const MjpbrScene* scene, int32_t cam, float* scale, float* offset, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  return kpcn_remod_launch(*scene, cam, scale, offset, static_cast<cudaStream_t>(stream));
 }
 
 int mjpbr_kpcn_apply_grad(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,

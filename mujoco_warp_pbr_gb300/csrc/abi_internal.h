@@ -33,8 +33,9 @@ int accumulate_f64_launch(const float* src, double* acc, int64_t n, cudaStream_t
 int avgpool2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st);
 int kpcn_apply_launch(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
                       cudaStream_t st);
-int kpcn_loss_launch(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
-                     cudaStream_t st);
+int kpcn_loss_launch(const float* out, const float* target, const float* scale, const float* offset, float* grad, float* sums,
+                     int64_t npix, float w_l1, float w_rel, cudaStream_t st);
+int kpcn_remod_launch(const MjpbrScene& s, int32_t cam, float* scale, float* offset, cudaStream_t st);
 int kpcn_apply_grad_launch(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,
                            int32_t h, int32_t w, cudaStream_t st);
 int split_concat_grad_launch(const float* dcat, const uint16_t* low, float* dskip, uint16_t* dlow, int32_t nimg, int32_t h, int32_t w,

@@ -21,7 +21,7 @@ namespace {
 constexpr int kKernel = 5;                    // predicted kernel edge
 constexpr int kTaps = kKernel * kKernel;      // 25 weights per pixel
 constexpr int kLogits = 32;                   // logit channels (25 used)
-constexpr int kFeatures = 16;                 // network input channels (10 used)
+constexpr int kFeatures = 16;                 // network input channels (11 used)
 
 __device__ __forceinline__ uint16_t bf16_bits(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
 __device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
@@ -31,7 +31,7 @@ struct CamImage {
 };
 
 // Network input of camera image (world w): log(1 + demodulated radiance), first-hit albedo,
-// normal, log(1 + depth), zeros.
+// normal, log(1 + depth), log(1 + standard deviation of the mean's luminance), zeros.
 __global__ void features_kernel(const __grid_constant__ MjpbrScene s, CamImage c, uint16_t* __restrict__ x0) {
   const int64_t npix = (int64_t)c.width * c.height;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -41,7 +41,8 @@ __global__ void features_kernel(const __grid_constant__ MjpbrScene s, CamImage c
   const float4 r = reinterpret_cast<const float4*>(s.denoise_buffers[0])[adr];
   const Guide g = unpack_guide(reinterpret_cast<const uint4*>(s.aov_guide)[adr]);
   float f[kFeatures] = {log1pf(fmaxf(r.x, 0.0f)), log1pf(fmaxf(r.y, 0.0f)), log1pf(fmaxf(r.z, 0.0f)), g.albedo.x, g.albedo.y,
-                        g.albedo.z, g.normal.x, g.normal.y, g.normal.z, log1pf(fmaxf(g.depth, 0.0f)), 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                        g.albedo.z, g.normal.x, g.normal.y, g.normal.z, log1pf(fmaxf(g.depth, 0.0f)), log1pf(sqrtf(fmaxf(r.w, 0.0f))),
+                        0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   uint32_t o[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) o[k] = (uint32_t)bf16_bits(f[2 * k]) | ((uint32_t)bf16_bits(f[2 * k + 1]) << 16);
@@ -122,23 +123,31 @@ __global__ void apply_kernel(const float* __restrict__ logits, const float4* __r
 }
 
 // Loss = w_l1 * mean|o - t| + w_rel * mean((o - t)^2 / (t^2 + 0.01)) over pixels and channels
-// (t clamped at 0); its gradient with respect to the output; the two sums into sums[0..1].
-__global__ void loss_kernel(const float4* __restrict__ out, const float4* __restrict__ target, float4* __restrict__ grad,
-                            float* __restrict__ sums, int64_t npix, float w_l1, float w_rel) {
+// (t clamped at 0); its gradient with respect to the output; the two sums into sums[0..1]. With
+// scale / offset (float4 records, may be NULL) both are first mapped to HDR, x -> offset + x *
+// scale (the remodulation by albedo and emission over exposure), so that the loss is the relative
+// error of the final image.
+__global__ void loss_kernel(const float4* __restrict__ out, const float4* __restrict__ target, const float4* __restrict__ scale,
+                            const float4* __restrict__ offset, float4* __restrict__ grad, float* __restrict__ sums, int64_t npix,
+                            float w_l1, float w_rel) {
   __shared__ float part[2][256];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float l1 = 0.0f, rel = 0.0f;
   if (i < npix) {
     const float4 o = out[i], t = target[i];
+    const float4 sc = scale ? scale[i] : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    const float4 of = offset ? offset[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float inv = 1.0f / (3.0f * (float)npix);
     const float ov[3] = {o.x, o.y, o.z}, tv[3] = {fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f), fmaxf(t.z, 0.0f)};
+    const float sv[3] = {sc.x, sc.y, sc.z}, fv[3] = {of.x, of.y, of.z};
     float g[3];
     for (int c = 0; c < 3; ++c) {
-      const float d = ov[c] - tv[c];
-      const float den = tv[c] * tv[c] + 0.01f;
+      const float oh = fv[c] + ov[c] * sv[c], th = fv[c] + tv[c] * sv[c];
+      const float d = oh - th;
+      const float den = th * th + 0.01f;
       l1 += fabsf(d);
       rel += d * d / den;
-      g[c] = (w_l1 * (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) + w_rel * 2.0f * d / den) * inv;
+      g[c] = (w_l1 * (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) + w_rel * 2.0f * d / den) * inv * sv[c];
     }
     grad[i] = make_float4(g[0], g[1], g[2], 0.0f);
   }
@@ -156,6 +165,22 @@ __global__ void loss_kernel(const float4* __restrict__ out, const float4* __rest
     atomicAdd(sums, part[0][0]);
     atomicAdd(sums + 1, part[1][0]);
   }
+}
+
+// The HDR mapping of the demodulated radiance of camera image (world w): scale = max(albedo,
+// 0.01) / exposure, offset = exposed emission / exposure (float4 records, w = 0).
+__global__ void remod_kernel(const __grid_constant__ MjpbrScene s, CamImage c, float4* __restrict__ scale, float4* __restrict__ offset) {
+  const int64_t npix = (int64_t)c.width * c.height;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix * s.nworld) return;
+  const int64_t w = i / npix, pid = i - w * npix;
+  const int64_t adr = w * s.rgb_stride + c.adr + pid;
+  const Guide g = unpack_guide(reinterpret_cast<const uint4*>(s.aov_guide)[adr]);
+  const float inv_exposure = 1.0f / bf(s.exposure, (int32_t)w, 1, 0);
+  scale[i] = make_float4(fmaxf(g.albedo.x, kMinAlbedo) * inv_exposure, fmaxf(g.albedo.y, kMinAlbedo) * inv_exposure,
+                         fmaxf(g.albedo.z, kMinAlbedo) * inv_exposure, 0.0f);
+  offset[i] = make_float4(s.aov_emission[adr * 3] * inv_exposure, s.aov_emission[adr * 3 + 1] * inv_exposure,
+                          s.aov_emission[adr * 3 + 2] * inv_exposure, 0.0f);
 }
 
 // Backward of apply_kernel: d logit_k = w_k (g_k - sum_j w_j g_j), g_k = grad . radiance(tap k);
@@ -307,12 +332,22 @@ int kpcn_apply_launch(const float* logits, const float* radiance, float* weights
   return check_launch("apply_kernel");
 }
 
-int kpcn_loss_launch(const float* out, const float* target, float* grad, float* sums, int64_t npix, float w_l1, float w_rel,
-                     cudaStream_t st) {
+int kpcn_loss_launch(const float* out, const float* target, const float* scale, const float* offset, float* grad, float* sums,
+                     int64_t npix, float w_l1, float w_rel, cudaStream_t st) {
   if (!out || !target || !grad || !sums) return set_error(MJPBR_ERR_ARG, "kpcn loss: bad arguments");
   loss_kernel<<<blocks(npix, 256), 256, 0, st>>>(reinterpret_cast<const float4*>(out), reinterpret_cast<const float4*>(target),
+                                                 reinterpret_cast<const float4*>(scale), reinterpret_cast<const float4*>(offset),
                                                  reinterpret_cast<float4*>(grad), sums, npix, w_l1, w_rel);
   return check_launch("loss_kernel");
+}
+
+int kpcn_remod_launch(const MjpbrScene& s, int32_t cam, float* scale, float* offset, cudaStream_t st) {
+  CamImage c;
+  if (int rc = cam_image(s, cam, &c)) return rc;
+  if (!scale || !offset || !s.aov_guide || !s.aov_emission) return set_error(MJPBR_ERR_ARG, "kpcn remod: missing buffers");
+  const int64_t n = (int64_t)s.nworld * c.width * c.height;
+  remod_kernel<<<blocks(n, 256), 256, 0, st>>>(s, c, reinterpret_cast<float4*>(scale), reinterpret_cast<float4*>(offset));
+  return check_launch("remod_kernel");
 }
 
 int kpcn_apply_grad_launch(const float* grad, const float* weights, const float* radiance, uint16_t* grad_logits, int32_t nimg,

@@ -2,8 +2,8 @@
 
 A 4-level U-Net (channel widths 32 / 48 / 64 / 96, two 3 x 3 convolutions per level, 2 x 2
 average pooling down, nearest upsampling and skip concatenation up) reads 10 feature channels per
-pixel (log of the noisy demodulated radiance, first-hit albedo, normal and log depth; padded to
-16) and predicts 25 logits per pixel; their softmax is a 5 x 5 kernel applied to the noisy
+pixel (log of the noisy demodulated radiance, first-hit albedo, normal, log depth and the log of
+the per-pixel noise estimate; padded to 16) and predicts 25 logits per pixel; their softmax is a 5 x 5 kernel applied to the noisy
 demodulated radiance, which the a-trous filter's last pass then remodulates, tone maps and
 encodes. Weights and activations are BF16, accumulation FP32; every convolution (forward, input
 gradient and weight gradient) runs on the tensor cores through the library (conv.cu), the other
@@ -282,13 +282,17 @@ class KPCN:
     dg("e0b", ws["ds0"], ws["da0"], mask=ws["a0"])
     wg("e0a", x0, ws["da0"])
 
-  def loss_grad(self, target: torch.Tensor, w_l1: float = 1.0, w_rel: float = 1.0) -> torch.Tensor:
-    """Loss of ws['out'] against target (n, h, w, 4): writes ws['gout']; returns the device
-    sums (L1, relative MSE) over pixels and channels."""
+  def loss_grad(self, target: torch.Tensor, scale: torch.Tensor | None = None, offset: torch.Tensor | None = None, w_l1: float = 1.0, w_rel: float = 1.0) -> torch.Tensor:
+    """Loss of ws['out'] against target (n, h, w, 4), in HDR when scale / offset map the
+    demodulated radiance there (mjpbr_kpcn_remod): writes ws['gout']; returns the device sums
+    (L1, relative MSE) over pixels and channels."""
     n, h, w, _ = target.shape
     ws = self.workspace(n, h, w)
     ws["sums"].zero_()
-    _lib.call("mjpbr_kpcn_loss", _ptr(ws["out"]), _ptr(target), _ptr(ws["gout"]), _ptr(ws["sums"]), n * h * w, w_l1, w_rel, self._stream())
+    _lib.call(
+      "mjpbr_kpcn_loss", _ptr(ws["out"]), _ptr(target), _ptr(scale), _ptr(offset), _ptr(ws["gout"]), _ptr(ws["sums"]), n * h * w, w_l1, w_rel,
+      self._stream(),
+    )
     return ws["sums"]
 
   def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1.0e-8) -> None:
@@ -300,9 +304,9 @@ class KPCN:
       _lib.call("mjpbr_adam", _ptr(l.w), _ptr(l.gw), _ptr(l.mw), _ptr(l.vw), _ptr(l.w16), _ptr(l.flip16), l.w.numel(), s.c_out, cin, lr, beta1, beta2, eps, self.step_count, st)
       _lib.call("mjpbr_adam", _ptr(l.b), _ptr(l.gb), _ptr(l.mb), _ptr(l.vb), None, None, l.b.numel(), 0, 0, lr, beta1, beta2, eps, self.step_count, st)
 
-  def train_step(self, x0: torch.Tensor, radiance: torch.Tensor, target: torch.Tensor, lr: float) -> torch.Tensor:
+  def train_step(self, x0: torch.Tensor, radiance: torch.Tensor, target: torch.Tensor, lr: float, scale: torch.Tensor | None = None, offset: torch.Tensor | None = None) -> torch.Tensor:
     self.forward(x0, radiance, train=True)
-    sums = self.loss_grad(target)
+    sums = self.loss_grad(target, scale, offset)
     self.backward(x0, radiance)
     self.adam(lr)
     return sums
@@ -343,3 +347,56 @@ class KPCN:
     finish.denoise_buffers[0] = rc.denoise_buffers[1].data_ptr()
     finish.denoise_iterations = 0
     _lib.call("mjpbr_denoise_atrous", ctypes.byref(finish), st)
+
+
+def forward_flops(nimg: int, h: int, w: int) -> int:
+  """Multiply-add FLOPs (2 per MAC) of the network's convolutions for a batch."""
+  total = 0
+  for s in layer_specs():
+    px = nimg * (h >> s.level) * (w >> s.level)
+    total += 2 * 9 * (s.c_in + s.c_in2) * s.c_out * px
+  return total
+
+
+def _bench() -> None:
+  """python -m mujoco_warp_pbr_gb300.kpcn [nimg] [size] [reps]: times the network's forward pass
+  (and one training step) on random inputs with CUDA events; prints one JSON line with the
+  convolution TFLOP/s."""
+  import json
+  import sys
+
+  nimg = int(sys.argv[1]) if len(sys.argv) > 1 else 256
+  size = int(sys.argv[2]) if len(sys.argv) > 2 else 128
+  reps = int(sys.argv[3]) if len(sys.argv) > 3 else 5
+  net = KPCN("cuda", seed=0)
+  g = torch.Generator(device="cuda").manual_seed(0)
+  x0 = torch.rand((nimg, size, size, FEATURES), generator=g, device="cuda").to(torch.bfloat16)
+  rad = torch.rand((nimg, size, size, 4), generator=g, device="cuda")
+  tgt = torch.rand((nimg, size, size, 4), generator=g, device="cuda")
+  for _ in range(2):
+    net.forward(x0, rad)
+  torch.cuda.synchronize()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record()
+  for _ in range(reps):
+    net.forward(x0, rad)
+  e1.record()
+  torch.cuda.synchronize()
+  fwd_ms = e0.elapsed_time(e1) / reps
+  net.train_step(x0, rad, tgt, 1e-4)
+  torch.cuda.synchronize()
+  e0.record()
+  for _ in range(reps):
+    net.train_step(x0, rad, tgt, 1e-4)
+  e1.record()
+  torch.cuda.synchronize()
+  train_ms = e0.elapsed_time(e1) / reps
+  flops = forward_flops(nimg, size, size)
+  print(json.dumps({
+    "nimg": nimg, "size": size, "forward_ms": fwd_ms, "forward_tflops": flops / fwd_ms / 1e9, "mpix_s": nimg * size * size / fwd_ms / 1e3,
+    "train_step_ms": train_ms, "train_tflops": 3 * flops / train_ms / 1e9, "error": int(net.error.item()),
+  }))
+
+
+if __name__ == "__main__":
+  _bench()

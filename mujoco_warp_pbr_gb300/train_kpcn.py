@@ -85,32 +85,37 @@ def noisy_pair(fr: Frame, spp: int, seed: int, gt_hdr: torch.Tensor | None):
     hsum = gt_hdr.contiguous()
     target = torch.zeros((n, h, w, 4), dtype=torch.float32, device=rc.device)
     _lib.call("mjpbr_kpcn_target", ctypes.byref(s), 0, hsum.data_ptr(), ctypes.c_double(1.0), target.data_ptr(), stream)
-  return x0, radiance, target, rc
+  scale = torch.zeros((n, h, w, 4), dtype=torch.float32, device=rc.device)
+  offset = torch.zeros((n, h, w, 4), dtype=torch.float32, device=rc.device)
+  _lib.call("mjpbr_kpcn_remod", ctypes.byref(s), 0, scale.data_ptr(), offset.data_ptr(), stream)
+  return x0, radiance, target, (scale, offset), rc
 
 
-def make_dataset(crops: int, frame_worlds: int, res: int, target_spp: int, seed0: int = 100):
-  xs, rs, ts = [], [], []
+def make_dataset(crops: int, frame_worlds: int, res: int, target_spp: int, spp: tuple[int, ...] = (2,), seed0: int = 100):
+  """(x0, radiance, target, scale, offset) of `crops` world images, input sample counts cycling
+  through spp frame by frame."""
+  parts: list[list[torch.Tensor]] = [[], [], [], [], []]
   nframes = (crops + frame_worlds - 1) // frame_worlds
   for f in range(nframes):
     fr = make_frame(seed0 + f, frame_worlds, res)
     gt = converged_hdr(fr, target_spp)
-    spp = 1 + f % 4  # 1-4 spp inputs
-    x0, rad, tgt, _ = noisy_pair(fr, spp, seed=17 + f, gt_hdr=gt)
-    xs.append(x0)
-    rs.append(rad)
-    ts.append(tgt)
-  return torch.cat(xs)[:crops], torch.cat(rs)[:crops], torch.cat(ts)[:crops]
+    x0, rad, tgt, (scale, offset), _ = noisy_pair(fr, spp[f % len(spp)], seed=17 + f, gt_hdr=gt)
+    for p, t in zip(parts, (x0, rad, tgt, scale, offset)):
+      p.append(t)
+  return tuple(torch.cat(p)[:crops] for p in parts)
 
 
-def train(net: kpcn_lib.KPCN, data, steps: int, batch: int, lr: float, seed: int = 0) -> list[float]:
-  x0, rad, tgt = data
+def train(net: kpcn_lib.KPCN, data, steps: int, batch: int, lr: float, seed: int = 0, warmup: int = 100) -> list[float]:
+  """Adam with a linear warm-up and cosine decay of the learning rate; the loss is the relative
+  error of the remodulated HDR image."""
+  x0, rad, tgt, scale, offset = data
   n = x0.shape[0]
   g = torch.Generator(device="cpu").manual_seed(seed)
   losses = []
   for step in range(steps):
     idx = torch.randint(0, n, (batch,), generator=g).to(x0.device)
-    lr_t = lr * 0.5 * (1.0 + np.cos(np.pi * step / steps))
-    sums = net.train_step(x0[idx].contiguous(), rad[idx].contiguous(), tgt[idx].contiguous(), lr_t)
+    lr_t = lr * min(1.0, (step + 1) / warmup) * 0.5 * (1.0 + np.cos(np.pi * step / steps))
+    sums = net.train_step(x0[idx].contiguous(), rad[idx].contiguous(), tgt[idx].contiguous(), lr_t, scale[idx].contiguous(), offset[idx].contiguous())
     if step % 50 == 0 or step == steps - 1:
       losses.append(float(sums.sum().item()))
   return losses
@@ -181,9 +186,10 @@ def main() -> None:
   p.add_argument("--eval-worlds", type=int, default=64)
   p.add_argument("--eval-ref-spp", type=int, default=4096)
   p.add_argument("--init", default=None, help="weights to start from")
+  p.add_argument("--spp", default="2", help="input sample counts, comma separated, cycled per frame")
   args = p.parse_args()
   t0 = time.time()
-  data = make_dataset(args.crops, args.frame_worlds, args.res, args.target_spp)
+  data = make_dataset(args.crops, args.frame_worlds, args.res, args.target_spp, tuple(int(v) for v in args.spp.split(",")))
   torch.cuda.synchronize()
   t_data = time.time() - t0
   net = kpcn_lib.KPCN.load(args.init) if args.init else kpcn_lib.KPCN("cuda", seed=0)
@@ -195,7 +201,7 @@ def main() -> None:
   net.save(args.out)
   del data
   ev = evaluate(net, args.eval_worlds, args.res, args.eval_ref_spp)
-  print(json.dumps({"data_s": t_data, "train_s": t_train, "steps": args.steps, "batch": args.batch, "crops": args.crops, "target_spp": args.target_spp, "losses": losses, "eval": ev}))
+  print(json.dumps({"data_s": t_data, "train_s": t_train, "steps": args.steps, "batch": args.batch, "crops": args.crops, "target_spp": args.target_spp, "spp": args.spp, "losses": losses, "eval": ev}))
 
 
 if __name__ == "__main__":
