@@ -391,7 +391,8 @@ int mjpbr_avgpool2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t
  * records); weights (nimg, h, w, 25) may be NULL (inference); out (nimg, h, w, 4), w = 0. */
 int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
                      void* stream);
-/* L1 and relative-MSE loss of out against target (float4 records): gradient, and the two sums
+/* Relative L1 (|d| / sqrt(t^2 + 0.01)) and relative-MSE loss of out against target (float4
+ * records): gradient, and the two sums
  * added to sums[0..1]. With scale and offset (float4 records, see mjpbr_kpcn_remod; may be NULL)
  * both are first mapped to HDR as offset + x * scale. */
 int mjpbr_kpcn_loss(const float* out, const float* target, const float* scale, const float* offset, float* grad, float* sums,

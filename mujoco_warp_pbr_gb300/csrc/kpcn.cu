@@ -122,8 +122,9 @@ __global__ void apply_kernel(const float* __restrict__ logits, const float4* __r
   out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
 
-// Loss = w_l1 * mean|o - t| + w_rel * mean((o - t)^2 / (t^2 + 0.01)) over pixels and channels
-// (t clamped at 0); its gradient with respect to the output; the two sums into sums[0..1]. With
+// Loss = w_l1 * mean(|o - t| / sqrt(t^2 + 0.01)) + w_rel * mean((o - t)^2 / (t^2 + 0.01)) over
+// pixels and channels (t clamped at 0): relative L1 and relative MSE, both independent of the
+// image's scale; its gradient with respect to the output; the two sums into sums[0..1]. With
 // scale / offset (float4 records, may be NULL) both are first mapped to HDR, x -> offset + x *
 // scale (the remodulation by albedo and emission over exposure), so that the loss is the relative
 // error of the final image.
@@ -145,9 +146,10 @@ __global__ void loss_kernel(const float4* __restrict__ out, const float4* __rest
       const float oh = fv[c] + ov[c] * sv[c], th = fv[c] + tv[c] * sv[c];
       const float d = oh - th;
       const float den = th * th + 0.01f;
-      l1 += fabsf(d);
+      const float rden = rsqrtf(den);
+      l1 += fabsf(d) * rden;
       rel += d * d / den;
-      g[c] = (w_l1 * (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) + w_rel * 2.0f * d / den) * inv * sv[c];
+      g[c] = (w_l1 * (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * rden + w_rel * 2.0f * d / den) * inv * sv[c];
     }
     grad[i] = make_float4(g[0], g[1], g[2], 0.0f);
   }

@@ -7,7 +7,10 @@ path-traced passes with other seeds, their HDR summed in FP64 on the device
 (mjpbr_accumulate_f64) and demodulated with the noisy render's albedo and emission
 (mjpbr_kpcn_target).
 
-    python -m mujoco_warp_pbr_gb300.train_kpcn --out weights.npz [--crops 2048 --target-spp 1024]
+    python -m mujoco_warp_pbr_gb300.train_kpcn --out weights.npz [--crops 6144 --target-spp 1024 --steps 8000]
+
+The committed weights (weights/kpcn_path.npz) came from --crops 6144 --frame-worlds 256
+--target-spp 1024 --steps 8000 --batch 16 --lr 1e-3 --spp 2 --loss-space demod.
 
 prints one JSON line: training time and loss curve, and on held-out scenes the relative MSE
 (mean((x - ref)^2 / (ref^2 + 0.01)) on linear HDR) against 4096-spp references of the learned
@@ -107,7 +110,7 @@ def make_dataset(crops: int, frame_worlds: int, res: int, target_spp: int, spp: 
 
 def train(net: kpcn_lib.KPCN, data, steps: int, batch: int, lr: float, seed: int = 0, warmup: int = 100) -> list[float]:
   """Adam with a linear warm-up and cosine decay of the learning rate; the loss is the relative
-  error of the remodulated HDR image."""
+  error of the remodulated HDR image (of the demodulated radiance when scale is None)."""
   x0, rad, tgt, scale, offset = data
   n = x0.shape[0]
   g = torch.Generator(device="cpu").manual_seed(seed)
@@ -115,7 +118,8 @@ def train(net: kpcn_lib.KPCN, data, steps: int, batch: int, lr: float, seed: int
   for step in range(steps):
     idx = torch.randint(0, n, (batch,), generator=g).to(x0.device)
     lr_t = lr * min(1.0, (step + 1) / warmup) * 0.5 * (1.0 + np.cos(np.pi * step / steps))
-    sums = net.train_step(x0[idx].contiguous(), rad[idx].contiguous(), tgt[idx].contiguous(), lr_t, scale[idx].contiguous(), offset[idx].contiguous())
+    remod = (scale[idx].contiguous(), offset[idx].contiguous()) if scale is not None else (None, None)
+    sums = net.train_step(x0[idx].contiguous(), rad[idx].contiguous(), tgt[idx].contiguous(), lr_t, *remod)
     if step % 50 == 0 or step == steps - 1:
       losses.append(float(sums.sum().item()))
   return losses
@@ -176,17 +180,18 @@ def evaluate(net: kpcn_lib.KPCN, nworld: int, res: int, ref_spp: int, seed: int 
 def main() -> None:
   p = argparse.ArgumentParser()
   p.add_argument("--out", default="kpcn_weights.npz")
-  p.add_argument("--crops", type=int, default=2048)
+  p.add_argument("--crops", type=int, default=6144)
   p.add_argument("--frame-worlds", type=int, default=256)
   p.add_argument("--res", type=int, default=128)
   p.add_argument("--target-spp", type=int, default=1024)
-  p.add_argument("--steps", type=int, default=2000)
+  p.add_argument("--steps", type=int, default=8000)
   p.add_argument("--batch", type=int, default=16)
   p.add_argument("--lr", type=float, default=1e-3)
   p.add_argument("--eval-worlds", type=int, default=64)
   p.add_argument("--eval-ref-spp", type=int, default=4096)
   p.add_argument("--init", default=None, help="weights to start from")
   p.add_argument("--spp", default="2", help="input sample counts, comma separated, cycled per frame")
+  p.add_argument("--loss-space", choices=["demod", "hdr"], default="demod", help="relative losses on the demodulated radiance or the remodulated HDR")
   args = p.parse_args()
   t0 = time.time()
   data = make_dataset(args.crops, args.frame_worlds, args.res, args.target_spp, tuple(int(v) for v in args.spp.split(",")))
@@ -194,6 +199,8 @@ def main() -> None:
   t_data = time.time() - t0
   net = kpcn_lib.KPCN.load(args.init) if args.init else kpcn_lib.KPCN("cuda", seed=0)
   t1 = time.time()
+  if args.loss_space == "demod":
+    data = data[:3] + (None, None)
   losses = train(net, data, args.steps, args.batch, args.lr)
   torch.cuda.synchronize()
   t_train = time.time() - t1
@@ -201,7 +208,7 @@ def main() -> None:
   net.save(args.out)
   del data
   ev = evaluate(net, args.eval_worlds, args.res, args.eval_ref_spp)
-  print(json.dumps({"data_s": t_data, "train_s": t_train, "steps": args.steps, "batch": args.batch, "crops": args.crops, "target_spp": args.target_spp, "spp": args.spp, "losses": losses, "eval": ev}))
+  print(json.dumps({"data_s": t_data, "train_s": t_train, "steps": args.steps, "batch": args.batch, "crops": args.crops, "target_spp": args.target_spp, "spp": args.spp, "loss_space": args.loss_space, "losses": losses, "eval": ev}))
 
 
 if __name__ == "__main__":

@@ -3,7 +3,7 @@
 Mirrors mujoco_warp_pbr_gb300/kpcn.py layer by layer: 3 x 3 convolutions with zero padding, ReLU,
 2 x 2 average pooling, nearest upsampling with skip concatenation, a 32-channel head whose first 25
 logits are a softmax 5 x 5 kernel applied to the radiance (borders clamped), the L1 + relative-MSE
-loss, and the backward pass of all of these. Activations can be rounded to BF16 after every layer
+loss (relative L1 + relative MSE), and the backward pass of all of these. Activations can be rounded to BF16 after every layer
 (as the GPU stores them) so that GPU gradients are compared with the same quantisation; without
 rounding it is the exact float64 reference that finite differences pin. Only tests/ use it.
 """
@@ -76,8 +76,8 @@ def loss(out, target, w_l1=1.0, w_rel=1.0):
   d = out - t
   den = t * t + 0.01
   n = d.size
-  value = w_l1 * np.abs(d).sum() / n + w_rel * (d * d / den).sum() / n
-  grad = (w_l1 * np.sign(d) + w_rel * 2.0 * d / den) / n
+  value = w_l1 * (np.abs(d) / np.sqrt(den)).sum() / n + w_rel * (d * d / den).sum() / n
+  grad = (w_l1 * np.sign(d) / np.sqrt(den) + w_rel * 2.0 * d / den) / n
   return value, grad
 
 
