@@ -474,6 +474,75 @@ def learned_denoiser(args) -> dict | None:
   return out
 
 
+def run_large(args) -> None:
+  """Large path-traced run: 8192 worlds x 2 cameras x 256², 2 spp, depth 4, four HDR environments,
+  the learned denoiser (BF16, 512 worlds at a time); every step is one CUDA-graph replay of pose
+  copy -> refit_bvh -> path tracer -> network -> finish pass."""
+  import torch
+
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import kpcn
+  from mujoco_warp_pbr_gb300 import synthetic
+
+  sc = synthetic.large_path_scene(seed=args.seed, nworld=args.nworld, res=args.res)
+  torch.cuda.set_device(0)
+  dev = torch.device("cuda", 0)
+  m = mjpbr.put_model(sc.mjm, device=dev)
+  d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld, device=dev)
+  opts = {**sc.options, "denoise": True, "render_hdr": False}
+  rc = mjpbr.create_render_context(sc.mjm, sc.nworld, data=sc.mjd, device=dev, **opts)
+  synthetic.apply_per_world(sc, m, rc)
+  net = kpcn.KPCN.load(WEIGHTS, device=dev)
+  poses = d.geom_xpos.clone()
+  poses[:, 1:, 2] += 0.01
+  graph = mjpbr.capture_frame(m, d, rc, seed=7, step=lambda: d.geom_xpos.copy_(poses), denoiser=lambda: net.denoise(m, d, rc, chunk=args.chunk))
+  stream = torch.cuda.current_stream(dev)
+  for _ in range(args.warmup):
+    graph.replay()
+  torch.cuda.synchronize()
+  assert mjpbr.check_errors(rc) == 0 and int(net.error.item()) == 0
+  npix = sc.nworld * sum(w * h for w, h in rc.base.cam_res)
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  with ClockSampler(0) as clocks:
+    e0.record(stream)
+    for _ in range(args.steps):
+      graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+  ms = e0.elapsed_time(e1) / args.steps
+  out_host = torch.empty(rc.base.rgb_data.shape, dtype=rc.base.rgb_data.dtype).pin_memory()
+  host_poses = poses.cpu().pin_memory()
+  e0.record(stream)
+  for _ in range(args.steps):
+    poses.copy_(host_poses, non_blocking=True)
+    graph.replay()
+    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+  e1.record(stream)
+  torch.cuda.synchronize()
+  e2e_ms = e0.elapsed_time(e1) / args.steps
+  print(json.dumps({
+    "metric": PATH_METRIC,
+    "value": npix / ms / 1e3,
+    "unit": UNIT,
+    "n_gpus": 1,
+    "steps": args.steps,
+    "warmup": args.warmup,
+    "ms_per_step": ms,
+    "higher_is_better": True,
+    "scaling": "weak",
+    "vs_baseline": None,
+    "dtype": "f32 path tracing, bf16 network",
+    "data": "synthetic (seeded scenes; no dataset)",
+    "config": {"workload": sc.name, "nworld": sc.nworld, "cameras": 2, "cam_res": [args.res, args.res], "spp": 2, "max_depth": 4,
+               "rr_depth": 2, "envs": 4, "denoiser": "learned (KPCN, BF16)", "chunk_worlds": args.chunk, "graph": "one CUDA graph per frame",
+               "l2": "frame working set far above L2"},
+    "e2e": {"value": npix / e2e_ms / 1e3, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4), "d2h_bytes_per_step": int(out_host.numel() * 4)},
+    "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
+    "gpu_launches": None,
+    "clocks": clocks.summary(),
+  }))
+
+
 def run_batched(args) -> None:
   """Batched uneven workload: autotuned launch shape, and every step is one CUDA-graph replay of
   step (copy of the next poses) -> refit_bvh -> render."""
@@ -593,7 +662,8 @@ def main() -> None:
   p.add_argument("--steps", type=int, default=20)
   p.add_argument("--warmup", type=int, default=3)
   p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-  p.add_argument("--workload", choices=["mesh_ibl", "primitives", "path", "batched"], default="mesh_ibl")
+  p.add_argument("--workload", choices=["mesh_ibl", "primitives", "path", "batched", "large_path"], default="mesh_ibl")
+  p.add_argument("--chunk", type=int, default=512)
   p.add_argument("--spp", type=int, default=2)
   p.add_argument("--no-path-tier", action="store_true")
   p.add_argument("--no-learned", action="store_true")
@@ -606,14 +676,16 @@ def main() -> None:
   p.add_argument("--no-cpu-baseline", action="store_true")
   args = p.parse_args()
   if args.nworld is None:
-    args.nworld = {"mesh_ibl": 4096, "path": 1024, "batched": 2048}.get(args.workload, 16)
+    args.nworld = {"mesh_ibl": 4096, "path": 1024, "batched": 2048, "large_path": 8192}.get(args.workload, 16)
   if args.res is None:
-    args.res = 128 if args.workload in ("mesh_ibl", "path") else 64
+    args.res = {"mesh_ibl": 128, "path": 128, "large_path": 256}.get(args.workload, 64)
   args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
   if args.impl == "reference":
     run_reference(args)
   elif args.workload == "batched":
     run_batched(args)
+  elif args.workload == "large_path":
+    run_large(args)
   else:
     run(args)
 

@@ -376,10 +376,10 @@ int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream);
 
 /* ---- Learned denoiser building blocks (no counterpart in the reference). NHWC layouts, one
  * image per world of camera `cam`; BF16 as raw 16-bit values. ---- */
-/* Network input (nworld, H, W, 16) BF16: log(1 + demodulated radiance), albedo, normal,
- * log(1 + depth), log(1 + standard deviation of the mean's luminance), zeros; from
- * denoise_buffers[0] and aov_guide written by a denoising render. */
-int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, uint16_t* x0, void* stream);
+/* Network input (nw, H, W, 16) BF16 of worlds [w0, w0 + nw): log(1 + demodulated radiance),
+ * albedo, normal, log(1 + depth), log(1 + standard deviation of the mean's luminance), zeros;
+ * from denoise_buffers[0] and aov_guide written by a denoising render. */
+int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, int32_t w0, int32_t nw, uint16_t* x0, void* stream);
 /* Demodulated training target (nworld, H, W, 4) FP32 from the FP64 sum of converged HDR frames
  * (laid out like hdr_data) times inv_n, with the denoising render's albedo and emission. */
 int mjpbr_kpcn_target(const MjpbrScene* scene, int32_t cam, const double* hdr_sum, double inv_n, float* target, void* stream);

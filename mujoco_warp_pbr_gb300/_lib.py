@@ -303,7 +303,7 @@ _SIGNATURES = {
   "mjpbr_gemm_bf16": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp]),
   "mjpbr_conv3x3_bf16": (ctypes.c_int, [ctypes.POINTER(Conv), c_vp]),
   "mjpbr_conv3x3_wgrad_bf16": (ctypes.c_int, [ctypes.POINTER(ConvGrad), c_vp]),
-  "mjpbr_kpcn_features": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_vp]),
+  "mjpbr_kpcn_features": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_i32, c_i32, c_vp, c_vp]),
   "mjpbr_kpcn_target": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, ctypes.c_double, c_vp, c_vp]),
   "mjpbr_accumulate_f64": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int64, c_vp]),
   "mjpbr_avgpool2_bf16": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp]),

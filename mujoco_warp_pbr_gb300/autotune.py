@@ -112,11 +112,15 @@ def autotune(m: Any, d: Any, rc: PbrRenderContext, frames: int = 3, candidates: 
   return {"best": best.describe(), "ms": {k.describe(): v for k, v in timings.items()}}
 
 
-def capture_frame(m: Any, d: Any, rc: PbrRenderContext, seed: int = 0, step: Callable[[], None] | None = None, warmup: int = 2) -> torch.cuda.CUDAGraph:
+def capture_frame(
+  m: Any, d: Any, rc: PbrRenderContext, seed: int = 0, step: Callable[[], None] | None = None, warmup: int = 2,
+  denoiser: Callable[[], None] | None = None,
+) -> torch.cuda.CUDAGraph:
   """One CUDA graph of a frame: step() (e.g. the physics step, or a copy of the next poses), the
-  BVH refit, the render and, for a denoised path-traced context, the filter. The seed is part of
+  BVH refit, the render and, for a denoised path-traced context, the filter: the a-trous passes,
+  or denoiser() (e.g. the learned denoiser's kpcn.KPCN.denoise) when given. The seed is part of
   the graph. Arrays replaced by assignment after capture are not seen by the graph: capture again.
-  The first calls (warm-up, outside the capture) configure the kernels."""
+  The first calls (warm-up, outside the capture) configure the kernels and allocate workspaces."""
   s = scene_descriptor(m, d, rc)
   current = torch.cuda.current_stream(rc.device)
   side = torch.cuda.Stream(rc.device)
@@ -127,7 +131,9 @@ def capture_frame(m: Any, d: Any, rc: PbrRenderContext, seed: int = 0, step: Cal
       step()
     _lib.call("mjpbr_refit_bvh", s, stream)
     _lib.call("mjpbr_render", s, int(seed) & 0xFFFFFFFF, stream)
-    if rc.tier == 1 and rc.denoise:
+    if denoiser is not None:
+      denoiser()
+    elif rc.tier == 1 and rc.denoise:
       _lib.call("mjpbr_denoise_atrous", s, stream)
 
   with torch.cuda.stream(side):

@@ -179,9 +179,9 @@ int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream) {
   return conv3x3_wgrad_launch(*grad, static_cast<cudaStream_t>(stream));
 }
 
-int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, uint16_t* x0, void* stream) {
+int mjpbr_kpcn_features(const MjpbrScene* scene, int32_t cam, int32_t w0, int32_t nw, uint16_t* x0, void* stream) {
   if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
-  return kpcn_features_launch(*scene, cam, x0, static_cast<cudaStream_t>(stream));
+  return kpcn_features_launch(*scene, cam, w0, nw, x0, static_cast<cudaStream_t>(stream));
 }
 
 int mjpbr_kpcn_target(const MjpbrScene* scene, int32_t cam, const double* hdr_sum, double inv_n, float* target, void* stream) {

@@ -27,7 +27,7 @@ int prefilter_launch(const MjpbrTexture* radiance, const uint8_t* data, int32_t 
 int denoise_launch(const MjpbrScene& s, cudaStream_t stream);
 int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream);
 int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream);
-int kpcn_features_launch(const MjpbrScene& s, int32_t cam, uint16_t* x0, cudaStream_t st);
+int kpcn_features_launch(const MjpbrScene& s, int32_t cam, int32_t w0, int32_t nw, uint16_t* x0, cudaStream_t st);
 int kpcn_target_launch(const MjpbrScene& s, int32_t cam, const double* hdr_sum, double inv_n, float* target, cudaStream_t st);
 int accumulate_f64_launch(const float* src, double* acc, int64_t n, cudaStream_t st);
 int avgpool2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st);

@@ -32,11 +32,11 @@ struct CamImage {
 
 // Network input of camera image (world w): log(1 + demodulated radiance), first-hit albedo,
 // normal, log(1 + depth), log(1 + standard deviation of the mean's luminance), zeros.
-__global__ void features_kernel(const __grid_constant__ MjpbrScene s, CamImage c, uint16_t* __restrict__ x0) {
+__global__ void features_kernel(const __grid_constant__ MjpbrScene s, CamImage c, int32_t w0, int32_t nw, uint16_t* __restrict__ x0) {
   const int64_t npix = (int64_t)c.width * c.height;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npix * s.nworld) return;
-  const int64_t w = i / npix, pid = i - w * npix;
+  if (i >= npix * nw) return;
+  const int64_t w = w0 + i / npix, pid = i % npix;
   const int64_t adr = w * s.rgb_stride + c.adr + pid;
   const float4 r = reinterpret_cast<const float4*>(s.denoise_buffers[0])[adr];
   const Guide g = unpack_guide(reinterpret_cast<const uint4*>(s.aov_guide)[adr]);
@@ -293,12 +293,13 @@ int cam_image(const MjpbrScene& s, int32_t cam, CamImage* c) {
 
 }  // namespace
 
-int kpcn_features_launch(const MjpbrScene& s, int32_t cam, uint16_t* x0, cudaStream_t st) {
+int kpcn_features_launch(const MjpbrScene& s, int32_t cam, int32_t w0, int32_t nw, uint16_t* x0, cudaStream_t st) {
   CamImage c;
   if (int rc = cam_image(s, cam, &c)) return rc;
   if (!x0 || !s.denoise_buffers[0] || !s.aov_guide) return set_error(MJPBR_ERR_ARG, "kpcn features: missing buffers");
-  const int64_t n = (int64_t)s.nworld * c.width * c.height;
-  features_kernel<<<blocks(n, 256), 256, 0, st>>>(s, c, x0);
+  if (w0 < 0 || nw < 1 || w0 + nw > s.nworld) return set_error(MJPBR_ERR_ARG, "kpcn features: worlds [%d, %d) outside [0, %d)", w0, w0 + nw, s.nworld);
+  const int64_t n = (int64_t)nw * c.width * c.height;
+  features_kernel<<<blocks(n, 256), 256, 0, st>>>(s, c, w0, nw, x0);
   return check_launch("features_kernel");
 }
 

@@ -140,31 +140,49 @@ class KPCN:
     return net
 
   # ---------------------------------------------------------------- workspace
-  def workspace(self, nimg: int, h: int, w: int) -> dict[str, torch.Tensor]:
+  def workspace(self, nimg: int, h: int, w: int, backward: bool = False) -> dict[str, torch.Tensor]:
+    """Activation buffers of a batch shape (allocated once); the gradient buffers are added the
+    first time a backward pass needs them, so inference holds only the forward activations."""
     key = (nimg, h, w)
-    if key in self._ws:
-      return self._ws[key]
-    if not supported(w, h):
-      raise ValueError(f"the learned denoiser needs images whose 4 levels tile into 128 pixels, got {w}x{h}")
-    dev, bf, f32 = self.device, torch.bfloat16, torch.float32
-    w0, w1, w2, w3 = WIDTHS
-
-    def t(level: int, c: int, dtype=bf) -> torch.Tensor:
-      return torch.zeros((nimg, h >> level, w >> level, c), dtype=dtype, device=dev)
-
-    ws = {
-      "a0": t(0, w0), "s0": t(0, w0), "p1": t(1, w0), "a1": t(1, w1), "s1": t(1, w1), "p2": t(2, w1), "a2": t(2, w2),
-      "s2": t(2, w2), "p3": t(3, w2), "a3": t(3, w3), "b3": t(3, w3), "u2": t(2, w2), "v2": t(2, w2), "u1": t(1, w1),
-      "v1": t(1, w1), "u0": t(0, w0), "v0": t(0, w0), "logits": t(0, LOGITS, f32), "kweights": t(0, TAPS, f32),
-      "out": t(0, 4, f32), "gout": t(0, 4, f32), "dlogits": t(0, LOGITS), "dv0": t(0, w0), "du0": t(0, w0),
-      "dcat0": t(0, w0 + w1, f32), "dskip0": t(0, w0, f32), "dv1": t(1, w1), "du1": t(1, w1), "dcat1": t(1, w1 + w2, f32),
-      "dskip1": t(1, w1, f32), "dv2": t(2, w2), "du2": t(2, w2), "dcat2": t(2, w2 + w3, f32), "dskip2": t(2, w2, f32),
-      "db3": t(3, w3), "da3": t(3, w3), "dp3": t(3, w2, f32), "ds2": t(2, w2), "da2": t(2, w2), "dp2": t(2, w1, f32),
-      "ds1": t(1, w1), "da1": t(1, w1), "dp1": t(1, w0, f32), "ds0": t(0, w0), "da0": t(0, w0),
-      "sums": torch.zeros(2, dtype=f32, device=dev),
-    }
-    self._ws[key] = ws
+    ws = self._ws.get(key)
+    if ws is None:
+      if not supported(w, h):
+        raise ValueError(f"the learned denoiser needs images whose 4 levels tile into 128 pixels, got {w}x{h}")
+      ws = self._ws[key] = self._alloc(nimg, h, w, self._FORWARD)
+    if backward and "dlogits" not in ws:
+      ws.update(self._alloc(nimg, h, w, self._BACKWARD))
     return ws
+
+  _FORWARD = {
+    # name: (level, channels, fp32)
+    "a0": (0, 0, False), "s0": (0, 0, False), "p1": (1, 0, False), "a1": (1, 1, False), "s1": (1, 1, False), "p2": (2, 1, False),
+    "a2": (2, 2, False), "s2": (2, 2, False), "p3": (3, 2, False), "a3": (3, 3, False), "b3": (3, 3, False), "u2": (2, 2, False),
+    "v2": (2, 2, False), "u1": (1, 1, False), "v1": (1, 1, False), "u0": (0, 0, False), "v0": (0, 0, False),
+    "logits": (0, "logits", True), "out": (0, "rgba", True),
+  }
+  _BACKWARD = {
+    "kweights": (0, "taps", True), "gout": (0, "rgba", True), "dlogits": (0, "logits", False), "dv0": (0, 0, False), "du0": (0, 0, False), "dcat0": (0, (0, 1), True),
+    "dskip0": (0, 0, True), "dv1": (1, 1, False), "du1": (1, 1, False), "dcat1": (1, (1, 2), True), "dskip1": (1, 1, True),
+    "dv2": (2, 2, False), "du2": (2, 2, False), "dcat2": (2, (2, 3), True), "dskip2": (2, 2, True), "db3": (3, 3, False),
+    "da3": (3, 3, False), "dp3": (3, 2, True), "ds2": (2, 2, False), "da2": (2, 2, False), "dp2": (2, 1, True), "ds1": (1, 1, False),
+    "da1": (1, 1, False), "dp1": (1, 0, True), "ds0": (0, 0, False), "da0": (0, 0, False),
+  }
+
+  def _alloc(self, nimg: int, h: int, w: int, spec: dict) -> dict[str, torch.Tensor]:
+    named = {"logits": LOGITS, "taps": TAPS, "rgba": 4}
+    out = {}
+    for name, (level, ch, f32) in spec.items():
+      if isinstance(ch, tuple):
+        c = WIDTHS[ch[0]] + WIDTHS[ch[1]]
+      elif isinstance(ch, str):
+        c = named[ch]
+      else:
+        c = WIDTHS[ch]
+      dtype = torch.float32 if f32 else torch.bfloat16
+      out[name] = torch.zeros((nimg, h >> level, w >> level, c), dtype=dtype, device=self.device)
+    if "gout" in out:
+      out["sums"] = torch.zeros(2, dtype=torch.float32, device=self.device)
+    return out
 
   # ---------------------------------------------------------------- primitives
   def _stream(self) -> int:
@@ -212,7 +230,7 @@ class KPCN:
     """x0 (n, h, w, 16) BF16 features, radiance (n, h, w, 4) FP32 noisy demodulated radiance;
     returns the filtered demodulated radiance (n, h, w, 4) (a view of the workspace)."""
     n, h, w, _ = x0.shape
-    ws = self.workspace(n, h, w)
+    ws = self.workspace(n, h, w, backward=train)
     c = self._conv
     c("e0a", x0, ws["a0"])
     c("e0b", ws["a0"], ws["s0"])
@@ -241,7 +259,7 @@ class KPCN:
   def backward(self, x0: torch.Tensor, radiance: torch.Tensor) -> None:
     """Accumulates the parameter gradients of the loss whose output gradient is in ws['gout']."""
     n, h, w, _ = x0.shape
-    ws = self.workspace(n, h, w)
+    ws = self.workspace(n, h, w, backward=True)
     w0, w1, w2, w3 = WIDTHS
     st = self._stream()
     _lib.call("mjpbr_kpcn_apply_grad", _ptr(ws["gout"]), _ptr(ws["kweights"]), _ptr(radiance), _ptr(ws["dlogits"]), n, h, w, st)
@@ -287,7 +305,7 @@ class KPCN:
     demodulated radiance there (mjpbr_kpcn_remod): writes ws['gout']; returns the device sums
     (L1, relative MSE) over pixels and channels."""
     n, h, w, _ = target.shape
-    ws = self.workspace(n, h, w)
+    ws = self.workspace(n, h, w, backward=True)
     ws["sums"].zero_()
     _lib.call(
       "mjpbr_kpcn_loss", _ptr(ws["out"]), _ptr(target), _ptr(scale), _ptr(offset), _ptr(ws["gout"]), _ptr(ws["sums"]), n * h * w, w_l1, w_rel,
@@ -317,11 +335,12 @@ class KPCN:
       l.gb.zero_()
 
   # ---------------------------------------------------------------- rendering
-  def denoise(self, m: Any, d: Any, rc: Any) -> None:
+  def denoise(self, m: Any, d: Any, rc: Any, chunk: int = 512) -> None:
     """Filters a denoising path-traced frame (rendered with render(..., denoise=False)) into the
-    context's RGB (and HDR) outputs with the network, every RGB camera in turn. Raises ValueError
-    for camera sizes the convolution tiles do not cover (the a-trous filter, render(...,
-    denoise=True), handles those)."""
+    context's RGB (and HDR) outputs with the network, every RGB camera in turn, `chunk` worlds at a
+    time (the activations of a chunk are the only network memory). Raises ValueError for camera
+    sizes the convolution tiles do not cover (the a-trous filter, render(..., denoise=True),
+    handles those). Capturable in a CUDA graph after one call outside the capture."""
     from mujoco_warp_pbr_gb300.render import scene
 
     s = scene(m, d, rc)
@@ -332,21 +351,26 @@ class KPCN:
     for cam, (width, height) in enumerate(rc.base.cam_res):
       if not rc.base.render_rgb[cam]:
         continue
-      ws = self.workspace(n, height, width)
-      if "x0" not in ws:
-        ws["x0"] = torch.zeros((n, height, width, FEATURES), dtype=torch.bfloat16, device=self.device)
-        ws["radiance"] = torch.zeros((n, height, width, 4), dtype=torch.float32, device=self.device)
       adr = rc.base.rgb_adr[cam]
-      _lib.call("mjpbr_kpcn_features", ctypes.byref(s), cam, _ptr(ws["x0"]), st)
-      ws["radiance"].view(n, -1, 4).copy_(src[:, adr : adr + width * height])
-      out = self.forward(ws["x0"], ws["radiance"])
-      dst[:, adr : adr + width * height].copy_(out.view(n, -1, 4))
+      for w0 in range(0, n, chunk):
+        nw = min(chunk, n - w0)
+        ws = self.workspace(nw, height, width)
+        if "x0" not in ws:
+          ws["x0"] = torch.zeros((nw, height, width, FEATURES), dtype=torch.bfloat16, device=self.device)
+          ws["radiance"] = torch.zeros((nw, height, width, 4), dtype=torch.float32, device=self.device)
+        _lib.call("mjpbr_kpcn_features", ctypes.byref(s), cam, w0, nw, _ptr(ws["x0"]), st)
+        ws["radiance"].view(nw, -1, 4).copy_(src[w0 : w0 + nw, adr : adr + width * height])
+        out = self.forward(ws["x0"], ws["radiance"])
+        dst[w0 : w0 + nw, adr : adr + width * height].copy_(out.view(nw, -1, 4))
     # the a-trous filter's finish pass without filtering remodulates, tone maps and writes the
     # outputs from the network's filtered radiance
-    finish = _lib.Scene.from_buffer_copy(s)
-    finish.denoise_buffers[0] = rc.denoise_buffers[1].data_ptr()
-    finish.denoise_iterations = 0
-    _lib.call("mjpbr_denoise_atrous", ctypes.byref(finish), st)
+    finish = rc._host_cache.get("kpcn_finish")
+    if finish is None or finish[0] is not s:
+      fs = _lib.Scene.from_buffer_copy(s)
+      fs.denoise_buffers[0] = rc.denoise_buffers[1].data_ptr()
+      fs.denoise_iterations = 0
+      finish = rc._host_cache["kpcn_finish"] = (s, fs)
+    _lib.call("mjpbr_denoise_atrous", ctypes.byref(finish[1]), st)
 
 
 def forward_flops(nimg: int, h: int, w: int) -> int:

@@ -440,7 +440,7 @@ def primitive_scene(seed: int = 0, nworld: int = 16, res: int = 64, shadow_sampl
   )
 
 
-def path_scene(seed: int = 0, nworld: int = 1024, res: int = 128, spp: int = 2, nquad: int = 3) -> SyntheticScene:
+def path_scene(seed: int = 0, nworld: int = 1024, res: int = 128, spp: int = 2, nquad: int = 3, ncam: int = 1) -> SyntheticScene:
   """Path-traced tier: the primitive scene plus emissive quads (thin boxes whose material emission,
   display-relative radiance, is drawn per world from U(1, 20)), next-event estimation over the
   lights, max depth 4, Russian roulette after bounce 2, `spp` jittered samples per pixel."""
@@ -458,6 +458,8 @@ def path_scene(seed: int = 0, nworld: int = 1024, res: int = 128, spp: int = 2, 
   b.light(LIGHT_DIRECTIONAL, pos=(0, 0, 4), dir=(0.3, 0.2, -1.0), diffuse=(0.7, 0.7, 0.7), castshadow=True)
   b.light(LIGHT_POINT, pos=(0.5, -0.5, 2.0), diffuse=(0.5, 0.5, 0.5), range=10.0, bulbradius=0.05, castshadow=True)
   b.camera((0.0, -3.2, 2.2), (0.0, 0.0, 0.25), fovy=45.0, resolution=(res, res))
+  if ncam > 1:
+    b.camera((2.8, 1.6, 1.8), (0.0, 0.0, 0.3), fovy=50.0, resolution=(res, res))
   mjm, mjd0 = b.build()
   ngeom, nprim = mjm.ngeom, 9
   xpos = np.broadcast_to(mjd0.geom_xpos, (nworld, ngeom, 3)).copy()
@@ -467,8 +469,8 @@ def path_scene(seed: int = 0, nworld: int = 1024, res: int = 128, spp: int = 2, 
   mjd = HostData(
     geom_xpos=xpos.astype(np.float32),
     geom_xmat=xmat.astype(np.float32),
-    cam_xpos=base.mjd.cam_xpos,
-    cam_xmat=base.mjd.cam_xmat,
+    cam_xpos=np.broadcast_to(mjd0.cam_xpos, (nworld, mjm.ncam, 3)).astype(np.float32),
+    cam_xmat=np.broadcast_to(mjd0.cam_xmat, (nworld, mjm.ncam, 9)).astype(np.float32),
     light_xpos=base.mjd.light_xpos,
     light_xdir=base.mjd.light_xdir,
   )
@@ -562,6 +564,19 @@ def batched_scene(seed: int = 0, nworld: int = 2048, res: tuple[int, ...] = (64,
     },
     seed=seed,
   )
+
+
+def large_path_scene(seed: int = 0, nworld: int = 8192, res: int = 256, nenv: int = 4, env_width: int = 512) -> SyntheticScene:
+  """Large path-traced run: the path scene with two cameras per world at res x res, per-world
+  materials and emission, and `nenv` procedural HDR environments chosen per world (env_id
+  uniform) with random rotation; 2 spp, depth 4."""
+  sc = path_scene(seed=seed, nworld=nworld, res=res, spp=2, ncam=2)
+  rng = np.random.default_rng(seed + 104729)
+  sc.options["envmap"] = [procedural_env(np.random.default_rng(seed + 31 * k), env_width) for k in range(nenv)]
+  sc.options["cam_res"] = [(res, res), (res, res)]
+  sc.per_world["env_id"] = rng.integers(0, nenv, nworld).astype(np.int32)
+  sc.per_world["env_yaw"] = rng.uniform(0.0, 2 * math.pi, nworld).astype(np.float32)
+  return dataclasses.replace(sc, name=f"large_path_{nworld}x2x{res}_spp2")
 
 
 def procedural_env(rng: np.random.Generator, width: int = 1024) -> np.ndarray:

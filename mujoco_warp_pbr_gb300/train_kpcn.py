@@ -81,7 +81,7 @@ def noisy_pair(fr: Frame, spp: int, seed: int, gt_hdr: torch.Tensor | None):
   w, h = rc.base.cam_res[0]
   stream = torch.cuda.current_stream().cuda_stream
   x0 = torch.zeros((n, h, w, kpcn_lib.FEATURES), dtype=torch.bfloat16, device=rc.device)
-  _lib.call("mjpbr_kpcn_features", ctypes.byref(s), 0, x0.data_ptr(), stream)
+  _lib.call("mjpbr_kpcn_features", ctypes.byref(s), 0, 0, n, x0.data_ptr(), stream)
   radiance = rc.denoise_buffers[0].view(n, h, w, 4).clone()
   target = None
   if gt_hdr is not None:

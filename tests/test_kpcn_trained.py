@@ -23,3 +23,36 @@ def test_trained_network_beats_the_filter_without_it():
   assert learned < 0.5 * atrous2, ev
   assert learned < 0.1 * plain2, ev
   assert learned < 1.1 * atrous16, ev
+
+
+def test_learned_denoiser_in_a_captured_frame_matches_eager():
+  """The learned denoiser captured with the frame (capture_frame(..., denoiser=...)) replays to
+  the eager images; worlds processed in chunks give the same images as one batch."""
+  from pathlib import Path
+
+  import numpy as np
+
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import kpcn, synthetic
+
+  sc = synthetic.path_scene(seed=77, nworld=6, res=128, spp=2)
+  m = mjpbr.put_model(sc.mjm)
+  d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld)
+  rc = mjpbr.create_render_context(sc.mjm, sc.nworld, data=sc.mjd, **{**sc.options, "denoise": True})
+  synthetic.apply_per_world(sc, m, rc)
+  net = kpcn.KPCN.load(Path(kpcn.__file__).resolve().parent / "weights" / "kpcn_path.npz")
+  mjpbr.refit_bvh(m, d, rc)
+  mjpbr.render(m, d, rc, seed=4, denoise=False)
+  net.denoise(m, d, rc)
+  torch.cuda.synchronize()
+  eager = rc.base.rgb_data.cpu().numpy().copy()
+  mjpbr.render(m, d, rc, seed=4, denoise=False)
+  net.denoise(m, d, rc, chunk=4)
+  torch.cuda.synchronize()
+  np.testing.assert_array_equal(rc.base.rgb_data.cpu().numpy(), eager)
+  graph = mjpbr.capture_frame(m, d, rc, seed=4, denoiser=lambda: net.denoise(m, d, rc))
+  rc.base.rgb_data.zero_()
+  graph.replay()
+  torch.cuda.synchronize()
+  assert mjpbr.check_errors(rc) == 0 and int(net.error.item()) == 0
+  np.testing.assert_array_equal(rc.base.rgb_data.cpu().numpy(), eager)
