@@ -184,18 +184,19 @@ MJ_DEV M3 cam_mat(const float* c) {
 struct RtCtx {
   const MjpbrScene* s;
   const float* blk;
-  const BlockLayout* L;  // in shared memory (one per CTA)
+  BlockLayout L;
   int32_t w;
   float exposure;
   V3 ambient;
   int32_t env;
   float env_yaw, env_scale;
+  int32_t err;
   Stack st;
 };
 
 // MuJoCo reflectance of a slot's material (material.py:543-550), 0 without a material.
 MJ_DEV float mirror_reflectance(const RtCtx& c, int32_t slot) {
-  int32_t matid = __float_as_int(c.blk[c.L->geom_off + slot * kGeomFloats + 18]);
+  int32_t matid = __float_as_int(c.blk[c.L.geom_off + slot * kGeomFloats + 18]);
   if (matid < 0 || !c.s->mat_reflectance.ptr) return 0.0f;
   return bf(c.s->mat_reflectance, c.w, c.s->nmat, matid);
 }
@@ -244,8 +245,9 @@ MJ_DEV void stage_world_block(const MjpbrScene& s, int32_t w, float* blk, int32_
 MJ_DEV void init_ctx(RtCtx& c, const MjpbrScene& s, const float* blk, const BlockLayout& L, int32_t w, bool tex) {
   c.s = &s;
   c.blk = blk;
-  c.L = &L;
+  c.L = L;
   c.w = w;
+  c.err = 0;
   c.exposure = bf(s.exposure, w, 1, 0);
   c.ambient = bv3(s.ambient_radiance, w, 1, 0);
   c.env = 0;

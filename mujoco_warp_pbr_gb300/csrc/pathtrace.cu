@@ -52,7 +52,7 @@ struct PixelAcc {
 template <bool kMesh, bool kTex>
 struct Pt {
   static MJ_DEV Hit trace(RtCtx& c, V3 o, V3 d, float max_dist, bool any) {
-    return trace_ray<kMesh>(*c.s, c.st, c.blk, *c.L, Ray{o, d}, max_dist, c.s->settings.cull_backfaces != 0, any, c.s->error_word);
+    return trace_ray<kMesh>(*c.s, c.st, c.blk, c.L, Ray{o, d}, max_dist, c.s->settings.cull_backfaces != 0, any, &c.err);
   }
 
   static __device__ __noinline__ V3 environment(const RtCtx& c, V3 d) {
@@ -129,8 +129,7 @@ struct Pt {
     }
     const V3 point = ps.o + ps.d * hit.dist;
     V3 normal;
-    Surface sf = eval_surface<kMesh, kTex>(s, c.blk, *c.L, c.w, hit, hit.slot, point, ps.d, 0.0f);
-    normal = sf.shading;
+    Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, point, ps.d, 0.0f, &normal);
     if (st.has_transparency) {
       if (pt_rand(seed, ps.sample, ps.depth + ps.passes, 0) >= sf.alpha && ps.passes < 4 * st.max_layers) {
         ps.o = point + ps.d * kRayOffset;
@@ -171,16 +170,16 @@ struct Pt {
     if (ps.depth == 0 && camera_ray) ps.albedo = lb.diffuse_color + spec_weight;
 
     // next-event estimation: MuJoCo lights, then the headlight (no shadow, display-relative)
-    const int32_t nl = c.L->nlight + (st.headlight_active ? 1 : 0);
+    const int32_t nl = c.L.nlight + (st.headlight_active ? 1 : 0);
     V3 direct = v3(0.0f);
 #pragma unroll 1
     for (int32_t li = 0; li < nl; ++li) {
       Light light;
       float u0 = 0.0f, u1 = 0.0f;
-      if (li < c.L->nlight) {
-        light = load_light(c.blk + c.L->light_off + li * kLightFloats);
+      if (li < c.L.nlight) {
+        light = load_light(c.blk + c.L.light_off + li * kLightFloats);
         if (!light.active) continue;
-        light_rand2(seed, ps.sample, ps.depth, c.L->nlight, li, &u0, &u1);
+        light_rand2(seed, ps.sample, ps.depth, c.L.nlight, li, &u0, &u1);
       } else {
         light = make_headlight(st, head_dir, c.exposure);
       }
@@ -256,8 +255,7 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
   extern __shared__ __align__(16) float smem[];
   __shared__ int32_t s_tile, s_next;
   float* blk = smem;
-  __shared__ BlockLayout L;
-  if (threadIdx.x == 0) L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const MjpbrSettings& st = s.settings;
   const int lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
@@ -268,6 +266,7 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
     c.st.t = reinterpret_cast<float*>(stack_base + kThreads * kStackDepth) + threadIdx.x;
     c.st.stride = kThreads;
   }
+  int32_t err = 0;
   for (;;) {
     if (threadIdx.x == 0) s_tile = atomicAdd(s.work_counter, 1);
     __syncthreads();
@@ -396,8 +395,10 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
         s.rgb_data[adr] = encode_display(display_transform(hdr * c.exposure, st.tone_mapper));
       }
     }
+    err |= c.err;
     __syncthreads();  // every lane done with this tile's block before the next one is staged
   }
+  if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
 int g_sm_count = 0;

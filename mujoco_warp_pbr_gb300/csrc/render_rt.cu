@@ -31,7 +31,7 @@ template <bool kMesh, bool kTex>
 struct Rt {
   static MJ_DEV bool occluded(RtCtx& c, V3 o, V3 d, float max_dist) {
     Ray r{o, d};
-    return trace_ray<kMesh>(*c.s, c.st, c.blk, *c.L, r, max_dist, c.s->settings.cull_backfaces != 0, true, c.s->error_word).geom != -1;
+    return trace_ray<kMesh>(*c.s, c.st, c.blk, c.L, r, max_dist, c.s->settings.cull_backfaces != 0, true, &c.err).geom != -1;
   }
 
   // Fraction of the light reaching the point (render.py:81-127).
@@ -111,13 +111,13 @@ struct Rt {
     V3 radiance = cmul(irradiance, lb.diffuse_color) * ao + cmul(prefiltered, cmul(lb.spec_albedo, lb.energy_comp)) * spec_ao;
     // MuJoCo lights, then the headlight (a directional light along the view, no shadow, its
     // illuminance display-relative), through one shade_light call site.
-    const int32_t nl = c.L->nlight + (st.headlight_active ? 1 : 0);
+    const int32_t nl = c.L.nlight + (st.headlight_active ? 1 : 0);
 #pragma unroll 1
     for (int32_t li = 0; li < nl; ++li) {
       Light light;
-      int32_t count = c.L->nlight, index = li;
-      if (li < c.L->nlight) {
-        light = load_light(c.blk + c.L->light_off + li * kLightFloats);
+      int32_t count = c.L.nlight, index = li;
+      if (li < c.L.nlight) {
+        light = load_light(c.blk + c.L.light_off + li * kLightFloats);
         if (!light.active) continue;
       } else {
         light = make_headlight(st, head_dir, c.exposure);
@@ -162,7 +162,7 @@ struct Rt {
 #pragma unroll 1
     for (int32_t iter = 0; iter < 2 * nlayer; ++iter) {
       Ray ray{so, sd};
-      Hit hit = trace_ray<kMesh>(s, c.st, c.blk, *c.L, ray, smax, cull, false, s.error_word);
+      Hit hit = trace_ray<kMesh>(s, c.st, c.blk, c.L, ray, smax, cull, false, &c.err);
       if (!mirror_seg && layer == 0) *first = hit;
       bool cont = false;
       if (hit.geom == -1) {
@@ -172,8 +172,7 @@ struct Rt {
         V3 point = so + sd * hit.dist;
         float cone = mirror_seg ? sfoot + spread * hit.dist : footprint + spread * (travelled + hit.dist);
         V3 normal;
-        Surface sf = eval_surface<kMesh, kTex>(s, c.blk, *c.L, c.w, hit, hit.slot, point, sd, cone);
-        normal = sf.shading;
+        Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, point, sd, cone, &normal);
         if (!mirror_seg && layer == 0) {
           *albedo = sf.base_color;
           *gnormal = normal;
@@ -246,8 +245,9 @@ MJ_DEV void render_pixel(const MjpbrScene& s, uint32_t seed, const float* blk, c
     float max_dist, depth_z;
     primary_ray(s, p, 1, 0, 0, &dcam, &ocam, &max_dist, &depth_z);
     Ray ray{cpos + mul(R, ocam), mul(R, dcam)};
-    Hit hit = trace_ray<kMesh>(s, c.st, blk, L, ray, max_dist, cull, false, s.error_word);
+    Hit hit = trace_ray<kMesh>(s, c.st, blk, L, ray, max_dist, cull, false, &c.err);
     write_geometry(s, w, p, hit, depth_z);
+    if (c.err && s.error_word) atomicOr(s.error_word, c.err);
     return;
   }
 
@@ -294,6 +294,7 @@ MJ_DEV void render_pixel(const MjpbrScene& s, uint32_t seed, const float* blk, c
     s.hdr_data[adr * 3 + 2] = hdr.z * inv_nn;
   }
   s.rgb_data[adr] = encode_display(display * inv_nn);
+  if (c.err && s.error_word) atomicOr(s.error_word, c.err);
 }
 
 MJ_DEV Stack thread_stack(float* stacks) {
@@ -312,10 +313,9 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   extern __shared__ __align__(16) float smem[];
   float* blk = smem;
   const int32_t w = blockIdx.y;
-  __shared__ BlockLayout L;
   stage_world_block(s, w, blk, kThreads);
-  if (threadIdx.x == 0) L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   __syncthreads();
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const int32_t tile = blockIdx.x;
   int32_t cam = 0;
   while (cam + 1 < tm.ncam && tile >= tm.tile_base[cam + 1]) ++cam;
@@ -361,9 +361,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_queue_kernel
   const unsigned full = 0xffffffffu;
   float* blk = smem + warp * s.world_block_floats;
   const Stack stack = thread_stack(smem + (kThreads / 32) * s.world_block_floats);
-  __shared__ BlockLayout L;
-  if (threadIdx.x == 0) L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-  __syncthreads();
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   int32_t staged = -1;
   for (;;) {
     int32_t item = 0;

@@ -53,7 +53,6 @@ struct Surface {
   float reflectance;
   V3 emissive;
   float occlusion;
-  V3 shading;  // viewer-facing shading normal, world frame
 };
 
 struct Lobes {

@@ -162,8 +162,8 @@ MJ_DEV float4 fetch_role(const MjpbrScene& s, int32_t tex_id, const TexFrame& f,
 
 // Surface and viewer-facing shading normal (world frame) at a hit (material.py:301-503).
 template <bool kMesh, bool kTex>
-__device__ __noinline__ Surface eval_surface(const MjpbrScene& s, const float* blk, const BlockLayout& L, int32_t w, const Hit hit,
-                            int32_t slot, V3 point, V3 dir, float footprint) {
+__device__ __noinline__ Surface eval_surface(const MjpbrScene& s, const float* blk, const BlockLayout& L, int32_t w, const Hit& hit,
+                            int32_t slot, V3 point, V3 dir, float footprint, V3* shading_world) {
   Surface sf;
   sf.occlusion = 1.0f;
   sf.emissive = v3(0.0f);
@@ -317,7 +317,7 @@ __device__ __noinline__ Surface eval_surface(const MjpbrScene& s, const float* b
     float kernel = fminf(2.0f * kSpecularAaVariance * dn * dn, kSpecularAaThreshold);
     sf.roughness = widen_roughness(sf.roughness, kernel);
   }
-  sf.shading = normalize(mul(fr.mat, shading));
+  *shading_world = normalize(mul(fr.mat, shading));
   return sf;
 }
 

@@ -47,8 +47,8 @@ MJ_DEV void push(const Stack& st, int& sp, int32_t code, float t, int32_t* err) 
     st.code[sp * st.stride] = code;
     st.t[sp * st.stride] = t;
     ++sp;
-  } else if (err) {
-    atomicOr(err, kErrStackOverflow);  // the scene's device error word (rare: a stack overflow)
+  } else {
+    *err |= kErrStackOverflow;
   }
 }
 
