@@ -90,8 +90,9 @@ typedef struct mjpbr_i32b { const int32_t* ptr; int32_t nbatch; int32_t pad_; } 
 
 /* One 3x3 convolution layer of the learned denoiser (stride 1, zero padding), NHWC BF16
  * activations, FP32 accumulation on the tensor cores. Input channels are `in` (c_in of them)
- * followed, when c_in2 > 0, by `in2` (nimg, height / 2, width / 2, c_in2) upsampled x2 (nearest):
- * the U-Net's skip concatenation. weight: (c_out, 9, c_in + c_in2), taps row-major (dy, dx).
+ * followed, when c_in2 > 0, by `in2`: (nimg, height, width, c_in2) when in2_full, else
+ * (nimg, height / 2, width / 2, c_in2) upsampled x2 (nearest) while staging: the U-Net's skip
+ * concatenation (mjpbr_upsample2_bf16 makes the full-resolution copy). weight: (c_out, 9, c_in + c_in2), taps row-major (dy, dx).
  * Epilogue: + bias, ReLU if relu, zeroed where mask <= 0 if mask (a ReLU derivative), stored as
  * BF16 to out and/or FP32 to out_f32. Channel counts are multiples of 16, c_out <= 256; width is
  * a power-of-two multiple of 16 up to 128 or a multiple of 128, height * width a multiple of 128
@@ -107,7 +108,7 @@ typedef struct MjpbrConv {
   int32_t* error_word;
   int32_t nimg, height, width, c_in, c_in2, c_out;
   int32_t relu;
-  int32_t pad_;
+  int32_t in2_full; /* 1: in2 has the output resolution; 0: half of it, upsampled x2 */
 } MjpbrConv;
 
 /* Weight and bias gradients of a 3x3 convolution layer (same tensors and constraints as
@@ -387,6 +388,8 @@ int mjpbr_kpcn_target(const MjpbrScene* scene, int32_t cam, const double* hdr_su
 int mjpbr_accumulate_f64(const float* src, double* acc, int64_t n, void* stream);
 /* 2 x 2 average pooling of BF16 (nimg, h, w, c). */
 int mjpbr_avgpool2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, void* stream);
+/* x2 nearest upsampling of BF16 (nimg, h, w, c) to (nimg, 2 h, 2 w, c); c a multiple of 8. */
+int mjpbr_upsample2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, void* stream);
 /* Softmax of 25 of the 32 FP32 logits per pixel, the 5 x 5 kernel applied to the radiance (float4
  * records); weights (nimg, h, w, 25) may be NULL (inference); out (nimg, h, w, 4), w = 0. */
 int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,

@@ -266,7 +266,7 @@ class Conv(ctypes.Structure):
     ("c_in2", c_i32),
     ("c_out", c_i32),
     ("relu", c_i32),
-    ("pad_", c_i32),
+    ("in2_full", c_i32),
   ]
 
 
@@ -307,6 +307,7 @@ _SIGNATURES = {
   "mjpbr_kpcn_target": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, ctypes.c_double, c_vp, c_vp]),
   "mjpbr_accumulate_f64": (ctypes.c_int, [c_vp, c_vp, ctypes.c_int64, c_vp]),
   "mjpbr_avgpool2_bf16": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp]),
+  "mjpbr_upsample2_bf16": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp]),
   "mjpbr_kpcn_apply": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp]),
   "mjpbr_kpcn_loss": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_vp]),
   "mjpbr_kpcn_remod": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_vp, c_vp]),

@@ -197,6 +197,10 @@ int mjpbr_avgpool2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t
   return avgpool2_launch(in, out, nimg, h, w, c, static_cast<cudaStream_t>(stream));
 }
 
+int mjpbr_upsample2_bf16(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, void* stream) {
+  return upsample2_launch(in, out, nimg, h, w, c, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_kpcn_apply(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
                      void* stream) {
   return kpcn_apply_launch(logits, radiance, weights, out, nimg, h, w, static_cast<cudaStream_t>(stream));

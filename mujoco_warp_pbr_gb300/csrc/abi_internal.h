@@ -31,6 +31,7 @@ int kpcn_features_launch(const MjpbrScene& s, int32_t cam, int32_t w0, int32_t n
 int kpcn_target_launch(const MjpbrScene& s, int32_t cam, const double* hdr_sum, double inv_n, float* target, cudaStream_t st);
 int accumulate_f64_launch(const float* src, double* acc, int64_t n, cudaStream_t st);
 int avgpool2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st);
+int upsample2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st);
 int kpcn_apply_launch(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,
                       cudaStream_t st);
 int kpcn_loss_launch(const float* out, const float* target, const float* scale, const float* offset, float* grad, float* sums,

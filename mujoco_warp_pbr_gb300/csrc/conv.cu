@@ -1,26 +1,26 @@
 // 3x3 convolutions of the learned denoiser as implicit GEMMs on the 5th-generation tensor cores.
 //
-// A CTA of 128 threads computes one tile of 128 output pixels (a run of one image row, or
-// 128 / width whole rows) times all output channels: D (128 x c_out, FP32 in tensor memory) =
-// sum over the 9 taps and the input channels of A_tap (128 x c_in) * W_tap^T. The input channels
-// are processed 16 at a time. For each 16-channel chunk the threads stage into shared memory,
-// in the K-major core-matrix layout, three copies of the tile's input rows plus a one-row halo
-// above and below, shifted by -1, 0 and +1 pixel (the dx of the taps; zero outside the image), so
-// that the A operand of tap (dy, dx) is one descriptor: copy dx, starting dy rows down, with a
-// uniform 16-byte row stride across the whole tile (the rows are stored with pitch = tile row
-// length, so consecutive output pixels, also across image rows, are consecutive operand rows).
-// One elected thread then issues the chunk's 9 tcgen05.mma instructions (K = 16 each) and commits
-// them to an mbarrier; the buffer is restaged after they completed. Two CTAs per SM overlap one
-// CTA's staging with the other's MMAs. The epilogue reads the accumulator rows out of tensor
-// memory (tcgen05.ld), adds the bias, applies ReLU and / or a ReLU-derivative mask and stores
-// BF16 (and optionally FP32) NHWC.
+// A tile is 128 output pixels (a run of one image row, or 128 / width whole rows) times all
+// output channels: D (128 x c_out, FP32 in tensor memory) = sum over the 9 taps and the input
+// channels of A_tap (128 x c_in) * W_tap^T, 16 input channels (one K = 16 MMA) at a time. The
+// input rows of a tile plus a one-row halo above and below are staged in shared memory in the
+// K-major core-matrix layout (8 pixels x 16 bytes), so that the A operand of tap (dy, dx) is one
+// descriptor with a uniform 16-byte row stride.
 //
-// The U-Net's skip concatenation is read in place: channels past c_in come from the half-
-// resolution tensor in2, upsampled x2 (nearest) while staging.
+// conv3x3_ws_kernel (the default, further below) is a persistent warp-specialised kernel whose
+// operands arrive by TMA. conv3x3_kernel, directly below, is the first version: one CTA per tile
+// staging three dx-shifted copies of its rows with plain loads (MJPBR_CONV_PIPELINE=0 selects it,
+// as do batches of more than 2^31 pixels).
+//
+// The U-Net's skip concatenation is read in place: channels past c_in come from in2, either at
+// the output resolution (in2_full) or at half of it, upsampled x2 (nearest) while staging.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
+#include <cstring>
 
 #include "abi_internal.h"
 #include "common.cuh"
@@ -44,6 +44,7 @@ __device__ __forceinline__ uint4 load_px(const MjpbrConv& p, int32_t img, int32_
   if (ch < p.c_in) {
     return __ldg(reinterpret_cast<const uint4*>(p.in + (((int64_t)img * p.height + iy) * p.width + ix) * p.c_in + ch));
   }
+  if (p.in2_full) return __ldg(reinterpret_cast<const uint4*>(p.in2 + (((int64_t)img * p.height + iy) * p.width + ix) * p.c_in2 + (ch - p.c_in)));
   const int32_t h2 = p.height >> 1, w2 = p.width >> 1;
   return __ldg(reinterpret_cast<const uint4*>(p.in2 + (((int64_t)img * h2 + (iy >> 1)) * w2 + (ix >> 1)) * p.c_in2 + (ch - p.c_in)));
 }
@@ -174,7 +175,419 @@ __global__ void __launch_bounds__(kConvThreads, 2) conv3x3_kernel(const __grid_c
   if (warp == 0) umma::tmem_free(tmem, ncols);
 }
 
+// ---- warp-specialised variant: persistent CTAs of six warps. Warp 4 loads operands with the
+// tensor memory accelerator (TMA) into up to kMaxStages stage buffers, warp 5 issues the MMAs,
+// warps 0-3 run the epilogue; two accumulators in tensor memory let a tile's epilogue overlap
+// the next tile's MMAs. The roles hand over through mbarriers:
+//   full[s]   the TMA loads of the stage in buffer s landed (expect-tx arrival by the loader)
+//   ready[s]  its operands are complete (in2 upsampled into the planes): loader, one arrival
+//   empty[s]  its MMAs completed (tcgen05.commit)
+//   acc_full[b] / acc_empty[b]  accumulator b holds a finished tile / was read (128 arrivals)
+//
+// Operand layout of a stage (G 16-channel chunks): one 5-D TMA box per copy covering all 2G
+// channel groups, so each group is a plane of (rows + 2) x spitch pixels x 16 bytes. A tile of
+// one image row (width >= 128) is staged once with its halo columns (spitch = pitch + 2) and the
+// dx shift of a tap is a one-pixel (16-byte) offset of the A descriptor; tiles of several short
+// rows stage three dx-shifted copies (spitch = pitch), since a shifted start would wrap from one
+// image row into the next. Outside the image the TMA reads zeros. A stage holds chunks of `in`
+// or of the half-resolution in2, which is loaded as one box per stage covering the tile's
+// footprint and upsampled x2 (nearest) into the planes by the loader warp; a full-resolution in2
+// (in2_full) is staged like `in`.
+//
+// Weights are resident (one TMA box of all taps and channel groups) when they fit, else loaded
+// per stage. Every wait is bounded; a wait that gives up raises the CTA's abort flag, which ends
+// the other roles' loops, and the error word records kErrWaitTimeout.
+
+constexpr int kWsThreads = 192;
+constexpr int kMaxStages = 4;
+
+struct WsGeom {
+  ConvGeom g;
+  int32_t ntiles;
+  int32_t single;    // tile = (part of) one image row: one staged copy with halo columns
+  int32_t spitch;    // staged pixels per row
+  int32_t plane;     // bytes of one channel-group plane: (rows + 2) x spitch x 16
+  int32_t group;     // 16-channel chunks per stage (G)
+  int32_t abuf;      // bytes of one stage's A region: copies x 2G planes (multiple of 128)
+  int32_t s2w, s2h;  // in2 box: pixels, rows
+  int32_t s2plane;   // bytes of one in2 group plane
+  int32_t s2buf;     // bytes of one stage's in2 boxes (multiple of 128); 0 without in2
+  int32_t bstage;    // bytes of one stage's weights; 0 when resident
+  int32_t resident;  // weights resident: 9 x (cin / 8) x c_out x 16 bytes at b_off
+  int32_t s2_off, b_off;
+  int32_t nstage;
+  int32_t acc_cols;  // tensor-memory columns of one accumulator
+};
+
+struct StageInfo {
+  int32_t in2;  // chunks of in2 (else of in)
+  int32_t cs;   // first chunk, in chunks of the concatenated input
+  int32_t nc;   // chunks
+};
+
+__device__ __forceinline__ StageInfo stage_info(int32_t s, int32_t nci, int32_t nchunk, int32_t G) {
+  const int32_t nsp_in = (nci + G - 1) / G;
+  StageInfo st;
+  st.in2 = s >= nsp_in;
+  st.cs = st.in2 ? nci + (s - nsp_in) * G : s * G;
+  st.nc = min(G, (st.in2 ? nchunk : nci) - st.cs);
+  return st;
+}
+
+// Bounded wait that also gives up once another role raised the abort flag.
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int32_t* abort_flag) {
+  for (uint32_t i = 0; i < umma::kWaitLimit; ++i) {
+    if (umma::mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 255u && *abort_flag) return false;
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void tile_origin(const ConvGeom& g, int32_t tile, int32_t& img, int32_t& y0, int32_t& x0) {
+  img = tile / g.tiles_per_img;
+  const int32_t t = tile - img * g.tiles_per_img;
+  y0 = (t / g.tiles_per_row) * g.rows;
+  x0 = (t % g.tiles_per_row) * g.pitch;
+}
+
+// Upsamples the in2 boxes of one stage (2 nc group planes; rows from (y0 - 1) >> 1, pixels from
+// x0 / 2 - 1) into its operand planes: staged row j, pixel xs holds input (y0 - 1 + j,
+// x0 + xs - 1) of the single copy, or (y0 - 1 + j, x + dx - 1) of copy dx at x.
+__device__ __forceinline__ void ws_expand(const WsGeom& wg, uint8_t* smem, int32_t buf, int32_t nc, int32_t y0, int32_t lane) {
+  const int32_t P = wg.g.pitch, R = wg.g.rows;
+  const int32_t r0 = (y0 - 1) >> 1;
+  const uint8_t* src0 = smem + wg.s2_off + buf * wg.s2buf;
+  uint8_t* dst0 = smem + buf * wg.abuf;
+  if (wg.single) {
+    const int32_t hw = P + 2;
+    const int32_t n = 2 * nc * 3 * hw;
+    for (int32_t e = lane; e < n; e += 32) {
+      const int32_t pl = e / (3 * hw);
+      const int32_t r = e - pl * 3 * hw;
+      const int32_t j = r / hw, xs = r - j * hw;
+      const int32_t sr = ((y0 - 1 + j) >> 1) - r0, sc = (xs + 1) >> 1;
+      *reinterpret_cast<uint4*>(dst0 + pl * wg.plane + (j * hw + xs) * 16) =
+          *reinterpret_cast<const uint4*>(src0 + pl * wg.s2plane + (sr * wg.s2w + sc) * 16);
+    }
+  } else {
+    const int32_t per_plane = (R + 2) * P;
+    const int32_t n = 3 * 2 * nc * per_plane;
+    const int32_t copy_stride = 2 * wg.group * wg.plane;
+    for (int32_t e = lane; e < n; e += 32) {
+      const int32_t dx = e / (2 * nc * per_plane);
+      const int32_t r1 = e - dx * 2 * nc * per_plane;
+      const int32_t pl = r1 / per_plane;
+      const int32_t r = r1 - pl * per_plane;
+      const int32_t j = r / P, x = r - j * P;
+      const int32_t sr = ((y0 - 1 + j) >> 1) - r0, sc = (x + dx + 1) >> 1;
+      *reinterpret_cast<uint4*>(dst0 + dx * copy_stride + pl * wg.plane + (j * P + x) * 16) =
+          *reinterpret_cast<const uint4*>(src0 + pl * wg.s2plane + (sr * wg.s2w + sc) * 16);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_constant__ MjpbrConv p, const __grid_constant__ WsGeom wg,
+                                                                   const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_in2,
+                                                                   const __grid_constant__ CUtensorMap tm_w) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t full[kMaxStages], ready[kMaxStages], empty[kMaxStages];
+  __shared__ uint64_t acc_full[2], acc_empty[2], wbar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int32_t abort_flag;
+  const ConvGeom& g = wg.g;
+  const int32_t cout = p.c_out;
+  const int32_t nchunk = g.cin / 16;
+  const int32_t nci = p.c_in / 16;
+  const int32_t G = wg.group;
+  const int32_t nsp = (nci + G - 1) / G + (nchunk - nci + G - 1) / G;  // stages per tile
+  const int32_t nst = wg.nstage;
+  const uint32_t s0 = umma::smem_addr(smem);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t ncols = 2u * (uint32_t)wg.acc_cols;
+  if (warp == 0) umma::tmem_alloc(&tmem_slot, ncols);
+  if (tid == 128) {
+    for (int i = 0; i < nst; ++i) {
+      umma::mbar_init(&full[i], 1);
+      umma::mbar_init(&ready[i], 1);
+      umma::mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      umma::mbar_init(&acc_full[i], 1);
+      umma::mbar_init(&acc_empty[i], kTilePx);
+    }
+    umma::mbar_init(&wbar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_in)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_w)) : "memory");
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  volatile int32_t* abort_v = &abort_flag;
+  bool ok = true;
+
+  if (warp == 4) {
+    // ---- loader: TMA loads of stage k, then the in2 upsampling of stage k - 1 ----
+    const uint32_t in_box = (uint32_t)(16 * wg.spitch * (g.rows + 2) * 2 * G);
+    const uint32_t in2_box = (uint32_t)(16 * wg.s2w * wg.s2h * 2 * G);
+    const uint32_t copies = wg.single ? 1u : 3u;
+    if (wg.resident && lane == 0) {
+      umma::mbar_arrive_expect_tx(&wbar, (uint32_t)(9 * 2 * nchunk * cout * 16));
+      umma::tma_load_4d(s0 + wg.b_off, &tm_w, &wbar, 0, 0, 0, 0);
+    }
+    int32_t k = 0, issued = 0, prev_in2 = 0, prev_nc = 0, prev_y0 = 0;
+    for (int32_t tile = blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x) {
+      int32_t img, y0, x0;
+      tile_origin(g, tile, img, y0, x0);
+      for (int32_t sidx = 0; sidx < nsp && ok; ++sidx, ++k) {
+        const StageInfo st = stage_info(sidx, nci, nchunk, G);
+        const int32_t buf = k % nst;
+        if (k >= nst) ok = ws_wait(&empty[buf], ((k / nst) + 1) & 1, abort_v);
+        if (!ok) break;
+        if (lane == 0) {
+          const uint32_t abase = s0 + buf * wg.abuf;
+          const bool half = st.in2 && !p.in2_full;  // in2 box, upsampled below
+          uint32_t bytes = half ? in2_box : copies * in_box;
+          if (!wg.resident) bytes += (uint32_t)wg.bstage;
+          umma::mbar_arrive_expect_tx(&full[buf], bytes);
+          // a full-resolution in2 is staged like `in`, from its own tensor map
+          const CUtensorMap* src = st.in2 ? &tm_in2 : &tm_in;
+          const int32_t grp0 = 2 * (st.in2 ? st.cs - nci : st.cs);
+          if (half) {
+            umma::tma_load_5d(s0 + wg.s2_off + buf * wg.s2buf, &tm_in2, &full[buf], 0, x0 / 2 - 1, (y0 - 1) >> 1, grp0, img);
+          } else if (wg.single) {
+            umma::tma_load_5d(abase, src, &full[buf], 0, x0 - 1, y0 - 1, grp0, img);
+          } else {
+            for (int32_t dx = 0; dx < 3; ++dx) umma::tma_load_5d(abase + dx * 2 * G * wg.plane, src, &full[buf], 0, x0 - 1 + dx, y0 - 1, grp0, img);
+          }
+          if (!wg.resident) umma::tma_load_4d(s0 + wg.b_off + buf * wg.bstage, &tm_w, &full[buf], 0, 0, 2 * st.cs, 0);
+        }
+        issued = k + 1;
+        if (k >= 1) {
+          // stage k - 1: operands complete once its loads landed (and in2 is upsampled)
+          const int32_t pb = (k - 1) % nst;
+          ok = ws_wait(&full[pb], ((k - 1) / nst) & 1, abort_v);
+          if (!ok) break;
+          if (prev_in2) {
+            ws_expand(wg, smem, pb, prev_nc, prev_y0, lane);
+            umma::fence_async_shared();
+          }
+          __syncwarp();
+          if (lane == 0) umma::mbar_arrive(&ready[pb]);
+        }
+        prev_in2 = st.in2 && !p.in2_full;
+        prev_nc = st.nc;
+        prev_y0 = y0;
+      }
+    }
+    if (ok && k >= 1) {
+      const int32_t pb = (k - 1) % nst;
+      ok = ws_wait(&full[pb], ((k - 1) / nst) & 1, abort_v);
+      if (ok) {
+        if (prev_in2) {
+          ws_expand(wg, smem, pb, prev_nc, prev_y0, lane);
+          umma::fence_async_shared();
+        }
+        __syncwarp();
+        if (lane == 0) umma::mbar_arrive(&ready[pb]);
+      }
+    }
+    if (!ok && lane == 0) {
+      // the copies in flight land before the CTA's shared memory is released
+      for (int32_t kk = max(0, issued - nst); kk < issued; ++kk) umma::mbar_wait(&full[kk % nst], (kk / nst) & 1);
+    }
+  } else if (warp == 5) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      const uint32_t idesc = umma::make_idesc_bf16(kTilePx, cout);
+      const uint32_t dy16 = (uint32_t)wg.spitch;
+      const uint32_t dx16 = wg.single ? 1u : (uint32_t)(2 * G * wg.plane) >> 4;
+      const uint32_t achunk16 = (uint32_t)(2 * wg.plane) >> 4;
+      const uint32_t btap16 = (uint32_t)((wg.resident ? 2 * nchunk : 2 * G) * cout);
+      const uint32_t bchunk16 = (uint32_t)(2 * cout);
+      if (wg.resident) ok = ws_wait(&wbar, 0, abort_v);
+      int32_t k = 0, i = 0, last = -1;
+      for (int32_t tile = blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x, ++i) {
+        const int32_t b = i & 1;
+        if (i >= 2) ok = ws_wait(&acc_empty[b], ((i >> 1) + 1) & 1, abort_v);
+        if (!ok) break;
+        umma::fence_after_sync();
+        const uint32_t acc = tmem + (uint32_t)(b * wg.acc_cols);
+        for (int32_t sidx = 0; sidx < nsp; ++sidx, ++k) {
+          const StageInfo st = stage_info(sidx, nci, nchunk, G);
+          const int32_t buf = k % nst;
+          ok = ws_wait(&ready[buf], (k / nst) & 1, abort_v);
+          if (!ok) break;
+          umma::fence_after_sync();
+          const uint64_t a_stage = umma::make_desc(s0 + buf * wg.abuf, wg.plane, 128);
+          const uint64_t b_stage = wg.resident ? umma::make_desc(s0 + wg.b_off, cout * 16, 128) + (uint64_t)(st.cs * bchunk16)
+                                               : umma::make_desc(s0 + wg.b_off + buf * wg.bstage, cout * 16, 128);
+          for (int32_t cc = 0; cc < st.nc; ++cc) {
+            const uint64_t ad = a_stage + cc * achunk16;
+            const uint64_t bd = b_stage + cc * bchunk16;
+#pragma unroll
+            for (int32_t tap = 0; tap < 9; ++tap) {
+              const uint32_t dy = tap / 3, dx = tap % 3;
+              umma::mma_bf16(acc, ad + dy * dy16 + dx * dx16, bd + tap * btap16, idesc, sidx > 0 || cc > 0 || tap > 0);
+            }
+          }
+          umma::commit(&empty[buf]);
+          last = buf;
+        }
+        if (!ok) break;
+        umma::commit(&acc_full[b]);
+      }
+      if (!ok && last >= 0) {
+        // the MMAs in flight complete before their accumulators are released
+        umma::mbar_wait(&empty[last], ((k - 1) / nst) & 1);
+      }
+    }
+  } else {
+    // ---- epilogue: warp w reads accumulator rows (pixels) 32 w .. 32 w + 31 ----
+    const int32_t m = tid;
+    int32_t i = 0;
+    for (int32_t tile = blockIdx.x; tile < wg.ntiles; tile += gridDim.x, ++i) {
+      const int32_t b = i & 1;
+      ok = ws_wait(&acc_full[b], (i >> 1) & 1, abort_v);
+      // tcgen05.ld is warp-collective
+      if (!__all_sync(0xFFFFFFFFu, ok)) {
+        ok = false;
+        *abort_v = 1;
+        break;
+      }
+      umma::fence_after_sync();
+      int32_t img, y0, x0;
+      tile_origin(g, tile, img, y0, x0);
+      const int64_t pix = ((int64_t)img * p.height + y0 + m / g.pitch) * p.width + x0 + m % g.pitch;
+      const uint32_t acc = tmem + (uint32_t)(b * wg.acc_cols) + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+      for (int32_t c0 = 0; c0 < cout; c0 += 16) {
+        float v[16];
+        umma::tmem_load16(acc + c0, v);
+        if (c0 + 16 >= cout) {
+          // the accumulator is free for tile i + 2 once every thread has read its rows
+          umma::fence_before_sync();
+          umma::mbar_arrive(&acc_empty[b]);
+        }
+        if (p.bias) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] += __ldg(p.bias + c0 + j);
+        }
+        if (p.relu) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
+        }
+        if (p.mask) {
+          const uint4* mk = reinterpret_cast<const uint4*>(p.mask + pix * cout + c0);
+          const uint4 m0 = __ldg(mk), m1 = __ldg(mk + 1);
+          const uint32_t wv[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if ((wv[j] & 0x8000u) || !(wv[j] & 0x7FFFu)) v[2 * j] = 0.0f;
+            if ((wv[j] & 0x80000000u) || !(wv[j] & 0x7FFF0000u)) v[2 * j + 1] = 0.0f;
+          }
+        }
+        if (p.out) {
+          uint4* o = reinterpret_cast<uint4*>(p.out + pix * cout + c0);
+          o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]), pack_bf16x2(v[6], v[7]));
+          o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]), pack_bf16x2(v[14], v[15]));
+        }
+        if (p.out_f32) {
+          float4* o = reinterpret_cast<float4*>(p.out_f32 + pix * cout + c0);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        }
+      }
+    }
+  }
+  if (!ok && tid % 32 == 0 && p.error_word) atomicOr(p.error_word, kErrWaitTimeout);
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_free(tmem, ncols);
+}
+
 bool aligned16(const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; }
+
+}  // namespace
+
+namespace {
+
+// shared memory of one CTA of the pipelined kernel: two CTAs per SM
+#ifndef MJPBR_CONV_SMEM_BUDGET
+#define MJPBR_CONV_SMEM_BUDGET (110 * 1024)
+#endif
+constexpr size_t kPipeSmemBudget = MJPBR_CONV_SMEM_BUDGET;
+constexpr size_t kPipeSmemMax = 220 * 1024;
+int g_conv_sms = 0;
+
+int conv_sm_count() {
+  if (g_conv_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_conv_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_conv_sms <= 0) g_conv_sms = 1;
+  }
+  return g_conv_sms;
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess && q == cudaDriverEntryPointSuccess) {
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    }
+  }
+  return fn;
+}
+
+int encode(CUtensorMap* m, const void* base, cuuint32_t rank, const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return set_error(MJPBR_ERR_CUDA, "conv3x3: cuTensorMapEncodeTiled is unavailable");
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(MJPBR_ERR_CUDA, "conv3x3: cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return 0;
+}
+
+// Tensor map of a BF16 NHWC activation as 5-D (8 channels, pixel, row, channel group, image):
+// the channel-group dimension (stride 16 bytes) is outside the pixel dimensions, so one box of
+// groups x 8 channels x bw pixels x bh rows lands as `groups` planes of bh x bw x 16 bytes. Reads
+// outside the tensor return zeros.
+int make_act_map(CUtensorMap* m, const void* base, int32_t ch, int32_t w, int32_t h, int32_t n, int32_t bw, int32_t bh, int32_t groups) {
+  const cuuint64_t dims[5] = {8, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)(ch / 8), (cuuint64_t)n};
+  const cuuint64_t strides[4] = {(cuuint64_t)ch * 2, (cuuint64_t)w * ch * 2, 16, (cuuint64_t)h * w * ch * 2};
+  const cuuint32_t box[5] = {8, (cuuint32_t)bw, (cuuint32_t)bh, (cuuint32_t)groups, 1};
+  return encode(m, base, 5, dims, strides, box);
+}
+
+// Tensor map of the weights [c_out][9 taps][cin] as 4-D (8 channels, output channel, channel
+// group, tap): a box of `groups` channel groups lands as [tap][group][c_out] x 16 bytes, the
+// K-major B operand of every tap.
+int make_weight_map(CUtensorMap* m, const void* base, int32_t cin, int32_t cout, int32_t groups) {
+  const cuuint64_t dims[4] = {8, (cuuint64_t)cout, (cuuint64_t)(cin / 8), 9};
+  const cuuint64_t strides[3] = {(cuuint64_t)9 * cin * 2, 16, (cuuint64_t)cin * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)cout, (cuuint32_t)groups, 9};
+  return encode(m, base, 4, dims, strides, box);
+}
+
+// MJPBR_CONV_PIPELINE=0 selects the one-tile-per-CTA kernel (kept for comparison).
+bool conv_pipeline_enabled() {
+  static int enabled = -1;
+  if (enabled < 0) {
+    const char* v = getenv("MJPBR_CONV_PIPELINE");
+    enabled = (v && v[0] == '0') ? 0 : 1;
+  }
+  return enabled == 1;
+}
 
 }  // namespace
 
@@ -185,7 +598,8 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     return set_error(MJPBR_ERR_ARG, "conv3x3: channels must be multiples of 16 (c_out <= 256), got %d + %d -> %d", c.c_in, c.c_in2,
                      c.c_out);
   }
-  if (c.c_in2 > 0 && (!c.in2 || c.height % 2 || c.width % 2)) return set_error(MJPBR_ERR_ARG, "conv3x3: in2 needs even sizes");
+  if (c.c_in2 > 0 && !c.in2) return set_error(MJPBR_ERR_ARG, "conv3x3: c_in2 > 0 needs in2");
+  if (c.c_in2 > 0 && !c.in2_full && (c.height % 2 || c.width % 2)) return set_error(MJPBR_ERR_ARG, "conv3x3: a half-resolution in2 needs even sizes");
   const int32_t w = c.width;
   const bool row_ok = (w >= 128) ? (w % 128 == 0) : (w >= 16 && 128 % w == 0);
   if (!row_ok) return set_error(MJPBR_ERR_ARG, "conv3x3: width %d is not a power of two in [16, 128] or a multiple of 128", w);
@@ -202,6 +616,80 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
   g.cin = c.c_in + c.c_in2;
   const int64_t tiles = (int64_t)c.nimg * g.tiles_per_img;
   if (tiles > INT32_MAX) return set_error(MJPBR_ERR_ARG, "conv3x3: too many tiles");
+  if (conv_pipeline_enabled() && (int64_t)c.nimg * c.height * c.width <= INT32_MAX) {
+    // warp-specialised persistent variant (32-bit pixel indices)
+    WsGeom wg;
+    wg.g = g;
+    wg.ntiles = (int32_t)tiles;
+    wg.single = g.rows == 1;
+    wg.spitch = wg.single ? g.pitch + 2 : g.pitch;
+    wg.plane = (g.rows + 2) * wg.spitch * 16;
+    wg.s2w = g.pitch / 2 + 2;
+    wg.s2h = wg.single ? 2 : g.rows / 2 + 2;
+    wg.s2plane = wg.s2w * wg.s2h * 16;
+    int acc_cols = 32;
+    while (acc_cols < c.c_out) acc_cols <<= 1;
+    wg.acc_cols = acc_cols;
+    const int32_t nchunk = g.cin / 16, nci = c.c_in / 16;
+    const int32_t copies = wg.single ? 1 : 3;
+    auto round128 = [](size_t v) { return (v + 127) / 128 * 128; };
+    const bool half_in2 = c.c_in2 > 0 && !c.in2_full;
+    const size_t wbytes = (size_t)9 * 2 * nchunk * c.c_out * 16;
+    auto stage_bytes = [&](int32_t G, bool resident) {
+      size_t b = round128((size_t)copies * 2 * G * wg.plane);
+      if (half_in2) b += round128((size_t)2 * G * wg.s2plane);
+      if (!resident) b += (size_t)9 * 2 * G * c.c_out * 16;
+      return b;
+    };
+    // resident weights when they fit beside two one-chunk stages; then the largest stage (in
+    // chunks) of which two fit, then as many stages as fit (at most kMaxStages)
+    const bool resident = wbytes + 2 * stage_bytes(1, true) <= kPipeSmemBudget;
+    const size_t fixed = resident ? wbytes : 0;
+    const int32_t gmax = std::max(nci, nchunk - nci);
+    int32_t G = 1;
+    while (G < gmax && fixed + 2 * stage_bytes(G + 1, resident) <= kPipeSmemBudget) ++G;
+    int32_t nst = 2;
+    while (nst < kMaxStages && fixed + (nst + 1) * stage_bytes(G, resident) <= kPipeSmemBudget) ++nst;
+    wg.group = G;
+    wg.nstage = nst;
+    wg.resident = resident;
+    wg.abuf = (int32_t)round128((size_t)copies * 2 * G * wg.plane);
+    wg.s2buf = half_in2 ? (int32_t)round128((size_t)2 * G * wg.s2plane) : 0;
+    wg.bstage = resident ? 0 : 9 * 2 * G * c.c_out * 16;
+    wg.s2_off = nst * wg.abuf;
+    wg.b_off = wg.s2_off + nst * wg.s2buf;
+    const size_t smem = fixed + (size_t)nst * stage_bytes(G, resident);
+    if (smem > kPipeSmemMax) return set_error(MJPBR_ERR_ARG, "conv3x3: %zu bytes of shared memory needed", smem);
+    static bool ws_smem_set = false;
+    if (!ws_smem_set) {
+      cudaError_t e = cudaFuncSetAttribute(conv3x3_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmemMax);
+      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "conv3x3: %zu bytes of shared memory: %s", kPipeSmemMax, cudaGetErrorString(e));
+      ws_smem_set = true;
+    }
+    CUtensorMap tm_in, tm_in2, tm_w;
+    memset(&tm_in2, 0, sizeof(tm_in2));
+    if (make_act_map(&tm_in, c.in, c.c_in, c.width, c.height, c.nimg, wg.spitch, g.rows + 2, 2 * G) != 0) return MJPBR_ERR_CUDA;
+    if (half_in2 && make_act_map(&tm_in2, c.in2, c.c_in2, c.width / 2, c.height / 2, c.nimg, wg.s2w, wg.s2h, 2 * G) != 0) return MJPBR_ERR_CUDA;
+    if (c.c_in2 > 0 && c.in2_full && make_act_map(&tm_in2, c.in2, c.c_in2, c.width, c.height, c.nimg, wg.spitch, g.rows + 2, 2 * G) != 0) return MJPBR_ERR_CUDA;
+    if (make_weight_map(&tm_w, c.weight, g.cin, c.c_out, resident ? 2 * nchunk : 2 * G) != 0) return MJPBR_ERR_CUDA;
+    // resident CTAs per SM, limited by shared memory (1 KB of it reserved per CTA), registers
+    // and the 512 tensor-memory columns (two accumulators per CTA)
+    static cudaFuncAttributes attr = {};
+    static int smem_per_sm = 0;
+    if (smem_per_sm == 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+      cudaFuncGetAttributes(&attr, conv3x3_ws_kernel);
+    }
+    const int regs = std::max(1, (attr.numRegs + 7) / 8 * 8) * kWsThreads;
+    int per_sm = smem_per_sm / (int)(smem + attr.sharedSizeBytes + 1024);
+    per_sm = std::min({per_sm, 65536 / regs, 512 / (2 * acc_cols)});
+    per_sm = std::max(1, per_sm);
+    const int64_t grid = std::min<int64_t>(tiles, (int64_t)conv_sm_count() * per_sm);
+    conv3x3_ws_kernel<<<(unsigned)grid, kWsThreads, smem, stream>>>(c, wg, tm_in, tm_in2, tm_w);
+    return check_launch("conv3x3_ws_kernel");
+  }
   const size_t smem = (size_t)6 * (g.rows + 2) * g.pitch * 16 + (size_t)18 * c.c_out * 16;
   static size_t smem_set = 0;
   if (smem > smem_set) {

@@ -88,6 +88,18 @@ __global__ void avgpool2_kernel(const uint16_t* __restrict__ in, uint16_t* __res
   out[i] = bf16_bits(0.25f * v);
 }
 
+// One thread per 16-byte group of 8 channels of an output pixel.
+__global__ void upsample2_kernel(const uint4* __restrict__ in, uint4* __restrict__ out, int32_t nimg, int32_t h, int32_t w, int32_t c8) {
+  const int64_t total = (int64_t)nimg * 4 * h * w * c8;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int32_t g = (int32_t)(i % c8);
+  const int64_t pix = i / c8;
+  const int32_t x = (int32_t)(pix % (2 * w)), y = (int32_t)((pix / (2 * w)) % (2 * h));
+  const int64_t n = pix / ((int64_t)4 * w * h);
+  out[i] = __ldg(in + ((n * h + (y >> 1)) * w + (x >> 1)) * c8 + g);
+}
+
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return min(max(v, lo), hi); }
 
 // Softmax of the 25 logits and the kernel applied to the radiance (float4 records, xyz used),
@@ -317,6 +329,14 @@ int accumulate_f64_launch(const float* src, double* acc, int64_t n, cudaStream_t
   if (n == 0) return MJPBR_OK;
   accumulate_f64_kernel<<<blocks(n, 256), 256, 0, st>>>(src, acc, n);
   return check_launch("accumulate_f64_kernel");
+}
+
+int upsample2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st) {
+  if (!in || !out || nimg < 1 || h < 1 || w < 1 || c < 8 || c % 8) return set_error(MJPBR_ERR_ARG, "upsample2: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) return set_error(MJPBR_ERR_ARG, "upsample2: tensors must be 16-byte aligned");
+  const int64_t n = (int64_t)nimg * 4 * h * w * (c / 8);
+  upsample2_kernel<<<blocks(n, 256), 256, 0, st>>>(reinterpret_cast<const uint4*>(in), reinterpret_cast<uint4*>(out), nimg, h, w, c / 8);
+  return check_launch("upsample2_kernel");
 }
 
 int avgpool2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st) {

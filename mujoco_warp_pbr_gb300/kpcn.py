@@ -159,6 +159,8 @@ class KPCN:
     "a2": (2, 2, False), "s2": (2, 2, False), "p3": (3, 2, False), "a3": (3, 3, False), "b3": (3, 3, False), "u2": (2, 2, False),
     "v2": (2, 2, False), "u1": (1, 1, False), "v1": (1, 1, False), "u0": (0, 0, False), "v0": (0, 0, False),
     "logits": (0, "logits", True), "out": (0, "rgba", True),
+    # the decoder's skip inputs upsampled x2 to the level they are concatenated at
+    "up2": (2, 3, False), "up1": (1, 2, False), "up0": (0, 1, False),
   }
   _BACKWARD = {
     "kweights": (0, "taps", True), "gout": (0, "rgba", True), "dlogits": (0, "logits", False), "dv0": (0, 0, False), "du0": (0, 0, False), "dcat0": (0, (0, 1), True),
@@ -189,12 +191,14 @@ class KPCN:
     return torch.cuda.current_stream(self.device).cuda_stream
 
   def _conv(self, name: str, x: torch.Tensor, out: torch.Tensor | None, x2: torch.Tensor | None = None, out_f32: torch.Tensor | None = None) -> None:
+    """x2: the skip input at the resolution of x (already upsampled)."""
     l = self.layers[name]
     s = l.spec
     n, h, w, _ = x.shape
     c = _lib.Conv(
       in_=_ptr(x), in2=_ptr(x2), weight=_ptr(l.w16), bias=_ptr(l.b), out=_ptr(out), out_f32=_ptr(out_f32), mask=None,
       error_word=_ptr(self.error), nimg=n, height=h, width=w, c_in=s.c_in, c_in2=s.c_in2, c_out=s.c_out, relu=int(s.relu),
+      in2_full=1,
     )
     _lib.call("mjpbr_conv3x3_bf16", ctypes.byref(c), self._stream())
 
@@ -225,6 +229,11 @@ class KPCN:
     n, h, w, c = x.shape
     _lib.call("mjpbr_avgpool2_bf16", _ptr(x), _ptr(out), n, h, w, c, self._stream())
 
+  def _up(self, x: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+    n, h, w, c = x.shape
+    _lib.call("mjpbr_upsample2_bf16", _ptr(x), _ptr(out), n, h, w, c, self._stream())
+    return out
+
   # ---------------------------------------------------------------- network
   def forward(self, x0: torch.Tensor, radiance: torch.Tensor, train: bool = False) -> torch.Tensor:
     """x0 (n, h, w, 16) BF16 features, radiance (n, h, w, 4) FP32 noisy demodulated radiance;
@@ -243,11 +252,11 @@ class KPCN:
     self._pool(ws["s2"], ws["p3"])
     c("e3a", ws["p3"], ws["a3"])
     c("e3b", ws["a3"], ws["b3"])
-    c("d2a", ws["s2"], ws["u2"], x2=ws["b3"])
+    c("d2a", ws["s2"], ws["u2"], x2=self._up(ws["b3"], ws["up2"]))
     c("d2b", ws["u2"], ws["v2"])
-    c("d1a", ws["s1"], ws["u1"], x2=ws["v2"])
+    c("d1a", ws["s1"], ws["u1"], x2=self._up(ws["v2"], ws["up1"]))
     c("d1b", ws["u1"], ws["v1"])
-    c("d0a", ws["s0"], ws["u0"], x2=ws["v1"])
+    c("d0a", ws["s0"], ws["u0"], x2=self._up(ws["v1"], ws["up0"]))
     c("d0b", ws["u0"], ws["v0"])
     c("head", ws["v0"], None, out_f32=ws["logits"])
     _lib.call(

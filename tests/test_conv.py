@@ -1,7 +1,7 @@
 """3x3 convolution layers of the learned denoiser (tcgen05 implicit GEMM) against a float64 CPU
 convolution of the same BF16 values: every tile geometry (image widths 16 to 256), the skip
-concatenation with a half-resolution upsampled input, bias, ReLU, the ReLU-derivative mask and
-the FP32 output."""
+concatenation with a half-resolution upsampled input or a full-resolution one, bias, ReLU, the
+ReLU-derivative mask and the FP32 output; and the x2 nearest upsampling."""
 
 import ctypes
 
@@ -12,9 +12,10 @@ torch = pytest.importorskip("torch")
 
 
 def conv_ref(x, w, bias=None, x2=None, relu=False, mask=None):
-  """x (n, h, w, c1), x2 (n, h/2, w/2, c2) or None, w (cout, 9, c1 + c2): float64 NHWC result."""
+  """x (n, h, w, c1), x2 (n, h/2, w/2, c2), (n, h, w, c2) or None, w (cout, 9, c1 + c2): float64
+  NHWC result."""
   if x2 is not None:
-    up = np.repeat(np.repeat(x2, 2, axis=1), 2, axis=2)
+    up = x2 if x2.shape[1] == x.shape[1] else np.repeat(np.repeat(x2, 2, axis=1), 2, axis=2)
     x = np.concatenate([x, up], axis=-1)
   n, h, wd, c = x.shape
   xp = np.zeros((n, h + 2, wd + 2, c))
@@ -55,18 +56,30 @@ CASES = [
   (1, 4, 256, 16, 0, 16, False, False, True),
   (3, 16, 64, 48, 96, 160, True, False, True),
   (1, 16, 16, 96, 0, 256, True, True, False),
+  # more tiles than one wave of persistent CTAs: weights resident (one staged row with halo) and
+  # weights staged per chunk (three shifted copies of two rows)
+  (40, 32, 128, 32, 16, 48, True, True, False),
+  (24, 64, 64, 48, 0, 96, True, False, True),
+]
+# the same with a full-resolution skip input
+FULL_CASES = [
+  (2, 32, 32, 32, 16, 64, True, True, False),
+  (3, 16, 64, 48, 96, 160, True, False, True),
+  (40, 32, 128, 32, 48, 32, True, True, False),
+  (2, 8, 256, 16, 32, 48, False, True, False),
 ]
 
 
 @pytest.mark.gpu
 @pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
-@pytest.mark.parametrize("nimg,h,w,c1,c2,cout,use_bias,relu,use_mask", CASES)
-def test_conv3x3_matches_cpu(nimg, h, w, c1, c2, cout, use_bias, relu, use_mask):
+@pytest.mark.parametrize("nimg,h,w,c1,c2,cout,use_bias,relu,use_mask,full", [c + (False,) for c in CASES] + [c + (True,) for c in FULL_CASES])
+def test_conv3x3_matches_cpu(nimg, h, w, c1, c2, cout, use_bias, relu, use_mask, full):
   from mujoco_warp_pbr_gb300 import _lib
 
   g = torch.Generator().manual_seed(nimg * 1000 + h * 10 + w + c1 + c2 + cout)
   x = (torch.rand((nimg, h, w, c1), generator=g) * 2 - 1).to(torch.bfloat16)
-  x2 = (torch.rand((nimg, h // 2, w // 2, c2), generator=g) * 2 - 1).to(torch.bfloat16) if c2 else None
+  s2 = 1 if full else 2
+  x2 = (torch.rand((nimg, h // s2, w // s2, c2), generator=g) * 2 - 1).to(torch.bfloat16) if c2 else None
   wt = ((torch.rand((cout, 9, c1 + c2), generator=g) * 2 - 1) / np.sqrt(9 * (c1 + c2))).to(torch.bfloat16)
   bias = (torch.rand(cout, generator=g) - 0.5) if use_bias else None
   mask = (torch.rand((nimg, h, w, cout), generator=g) - 0.3).to(torch.bfloat16) if use_mask else None
@@ -89,6 +102,7 @@ def test_conv3x3_matches_cpu(nimg, h, w, c1, c2, cout, use_bias, relu, use_mask)
   c = _lib.Conv(
     in_=ptr(dev["x"]), in2=ptr(dev["x2"]), weight=ptr(dev["w"]), bias=ptr(dev["b"]), out=ptr(out), out_f32=ptr(out32),
     mask=ptr(dev["m"]), error_word=ptr(err), nimg=nimg, height=h, width=w, c_in=c1, c_in2=c2, c_out=cout, relu=int(relu),
+    in2_full=int(full),
   )
   _lib.call("mjpbr_conv3x3_bf16", ctypes.byref(c), torch.cuda.current_stream().cuda_stream)
   torch.cuda.synchronize()
@@ -149,3 +163,18 @@ def test_conv3x3_wgrad_matches_cpu(nimg, h, w, c1, c2, cout, per_cta):
   scale = np.sqrt(nimg * h * w)
   np.testing.assert_allclose(gw.cpu().numpy(), ref_w + 0.5, rtol=1e-4, atol=1e-4 * scale)
   np.testing.assert_allclose(gb.cpu().numpy(), ref_b + 0.25, rtol=1e-4, atol=1e-4 * scale)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+def test_upsample2_is_nearest():
+  from mujoco_warp_pbr_gb300 import _lib
+
+  g = torch.Generator().manual_seed(5)
+  x = torch.randn((3, 5, 7, 24), generator=g).to(torch.bfloat16)
+  out = torch.zeros((3, 10, 14, 24), dtype=torch.bfloat16, device="cuda")
+  xd = x.cuda()
+  _lib.call("mjpbr_upsample2_bf16", xd.data_ptr(), out.data_ptr(), 3, 5, 7, 24, torch.cuda.current_stream().cuda_stream)
+  torch.cuda.synchronize()
+  ref = x.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2)
+  assert torch.equal(out.cpu().view(torch.int16), ref.view(torch.int16))
