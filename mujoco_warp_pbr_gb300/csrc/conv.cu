@@ -180,7 +180,8 @@ __global__ void __launch_bounds__(kConvThreads, 2) conv3x3_kernel(const __grid_c
 // warps 0-3 run the epilogue; two accumulators in tensor memory let a tile's epilogue overlap
 // the next tile's MMAs. The roles hand over through mbarriers:
 //   full[s]   the TMA loads of the stage in buffer s landed (expect-tx arrival by the loader)
-//   ready[s]  its operands are complete (in2 upsampled into the planes): loader, one arrival
+//   ready[s]  the loader is done with it: at once, or after upsampling a half-resolution in2
+//             into its planes (one arrival; the MMA warp waits on full[s] and ready[s])
 //   empty[s]  its MMAs completed (tcgen05.commit)
 //   acc_full[b] / acc_empty[b]  accumulator b holds a finished tile / was read (128 arrivals)
 //
@@ -200,6 +201,7 @@ __global__ void __launch_bounds__(kConvThreads, 2) conv3x3_kernel(const __grid_c
 
 constexpr int kWsThreads = 192;
 constexpr int kMaxStages = 4;
+constexpr int kMaxSlots = 8;  // row-ring slots
 
 struct WsGeom {
   ConvGeom g;
@@ -217,7 +219,38 @@ struct WsGeom {
   int32_t s2_off, b_off;
   int32_t nstage;
   int32_t acc_cols;  // tensor-memory columns of one accumulator
+  // row ring (tiles of one image row, resident weights): each CTA takes a contiguous range of
+  // tiles ordered down the image columns and loads every input row once into a ring of nslot
+  // slots of 2 x (c_in + c_in2) / 16 planes of (pitch + 2) pixels
+  int32_t ring;
+  int32_t nslot;
+  int32_t slot_bytes;
+  int32_t rowplane;  // bytes of one row plane: (pitch + 2) x 16
+  int32_t in2_off;   // offset of the in2 planes in a slot (a multiple of 128)
 };
+
+// The i-th tile of this CTA: strided over the grid, or (ring) the i-th of a contiguous range in
+// column-major order (image, tile column, row). False past the CTA's last tile.
+__device__ __forceinline__ bool cta_tile(const WsGeom& wg, int32_t i, int32_t& img, int32_t& y0, int32_t& x0) {
+  const ConvGeom& g = wg.g;
+  if (wg.ring) {
+    const int32_t t = (int32_t)((int64_t)blockIdx.x * wg.ntiles / gridDim.x) + i;
+    if (t >= (int32_t)((int64_t)(blockIdx.x + 1) * wg.ntiles / gridDim.x)) return false;
+    const int32_t h = g.tiles_per_img / g.tiles_per_row;  // image rows
+    const int32_t col = t / h;
+    y0 = t - col * h;
+    img = col / g.tiles_per_row;
+    x0 = (col - img * g.tiles_per_row) * g.pitch;
+    return true;
+  }
+  const int32_t tile = blockIdx.x + i * gridDim.x;
+  if (tile >= wg.ntiles) return false;
+  img = tile / g.tiles_per_img;
+  const int32_t t = tile - img * g.tiles_per_img;
+  y0 = (t / g.tiles_per_row) * g.rows;
+  x0 = (t % g.tiles_per_row) * g.pitch;
+  return true;
+}
 
 struct StageInfo {
   int32_t in2;  // chunks of in2 (else of in)
@@ -234,15 +267,20 @@ __device__ __forceinline__ StageInfo stage_info(int32_t s, int32_t nci, int32_t 
   return st;
 }
 
-// Bounded wait that also gives up once another role raised the abort flag.
-__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int32_t* abort_flag) {
+// Bounded wait that also gives up once another role raised the abort flag. Waiters off the MMA
+// issue path sleep `backoff_ns` between polls, so that polling warps leave the SM's issue slots
+// and memory pipeline to the MMA and copy instructions.
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int32_t* abort_flag, uint32_t backoff_ns = 0) {
   for (uint32_t i = 0; i < umma::kWaitLimit; ++i) {
     if (umma::mbar_try_wait(bar, parity)) return true;
     if ((i & 255u) == 255u && *abort_flag) return false;
+    if (backoff_ns) __nanosleep(backoff_ns);
   }
   *abort_flag = 1;
   return false;
 }
+
+constexpr uint32_t kLoaderBackoffNs = 256, kEpilogueBackoffNs = 128;
 
 __device__ __forceinline__ void tile_origin(const ConvGeom& g, int32_t tile, int32_t& img, int32_t& y0, int32_t& x0) {
   img = tile / g.tiles_per_img;
@@ -291,8 +329,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
                                                                    const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_in2,
                                                                    const __grid_constant__ CUtensorMap tm_w) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t full[kMaxStages], ready[kMaxStages], empty[kMaxStages];
-  __shared__ uint64_t acc_full[2], acc_empty[2], wbar;
+  __shared__ uint64_t full[kMaxSlots], ready[kMaxSlots], empty[kMaxSlots];
+  __shared__ uint64_t acc_full[2], acc_empty[2], wbar, drain;
   __shared__ uint32_t tmem_slot;
   __shared__ int32_t abort_flag;
   const ConvGeom& g = wg.g;
@@ -307,7 +345,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
   const uint32_t ncols = 2u * (uint32_t)wg.acc_cols;
   if (warp == 0) umma::tmem_alloc(&tmem_slot, ncols);
   if (tid == 128) {
-    for (int i = 0; i < nst; ++i) {
+    for (int i = 0; i < (wg.ring ? wg.nslot : nst); ++i) {
       umma::mbar_init(&full[i], 1);
       umma::mbar_init(&ready[i], 1);
       umma::mbar_init(&empty[i], 1);
@@ -317,6 +355,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
       umma::mbar_init(&acc_empty[i], kTilePx);
     }
     umma::mbar_init(&wbar, 1);
+    umma::mbar_init(&drain, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_in)) : "memory");
@@ -339,13 +378,34 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
       umma::tma_load_4d(s0 + wg.b_off, &tm_w, &wbar, 0, 0, 0, 0);
     }
     int32_t k = 0, issued = 0, prev_in2 = 0, prev_nc = 0, prev_y0 = 0;
-    for (int32_t tile = blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x) {
+    if (wg.ring) {
+      // one load per input row: the rows of a run of tiles down one tile column plus the
+      // halo rows above and below (outside the image the TMA reads zeros)
+      const uint32_t row_bytes = (uint32_t)(16 * wg.spitch * 2 * nchunk);
+      int32_t i = 0, img, y0, x0;
+      while (lane == 0 && ok && cta_tile(wg, i, img, y0, x0)) {
+        int32_t n = 1, img2, y2, x2;
+        while (cta_tile(wg, i + n, img2, y2, x2) && img2 == img && x2 == x0) ++n;
+        for (int32_t r = y0 - 1; r <= y0 + n && ok; ++r, ++k) {
+          const int32_t slot = k % wg.nslot;
+          if (k >= wg.nslot) ok = ws_wait(&empty[slot], ((k / wg.nslot) + 1) & 1, abort_v, kLoaderBackoffNs);
+          if (!ok) break;
+          const uint32_t sa = s0 + slot * wg.slot_bytes;
+          umma::mbar_arrive_expect_tx(&full[slot], row_bytes);
+          umma::tma_load_5d(sa, &tm_in, &full[slot], 0, x0 - 1, r, 0, img);
+          if (p.c_in2 > 0) umma::tma_load_5d(sa + wg.in2_off, &tm_in2, &full[slot], 0, x0 - 1, r, 0, img);
+          issued = k + 1;
+        }
+        i += n;
+      }
+    }
+    for (int32_t tile = wg.ring ? wg.ntiles : blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x) {
       int32_t img, y0, x0;
       tile_origin(g, tile, img, y0, x0);
       for (int32_t sidx = 0; sidx < nsp && ok; ++sidx, ++k) {
         const StageInfo st = stage_info(sidx, nci, nchunk, G);
         const int32_t buf = k % nst;
-        if (k >= nst) ok = ws_wait(&empty[buf], ((k / nst) + 1) & 1, abort_v);
+        if (k >= nst) ok = ws_wait(&empty[buf], ((k / nst) + 1) & 1, abort_v, kLoaderBackoffNs);
         if (!ok) break;
         if (lane == 0) {
           const uint32_t abase = s0 + buf * wg.abuf;
@@ -366,38 +426,39 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
           if (!wg.resident) umma::tma_load_4d(s0 + wg.b_off + buf * wg.bstage, &tm_w, &full[buf], 0, 0, 2 * st.cs, 0);
         }
         issued = k + 1;
-        if (k >= 1) {
-          // stage k - 1: operands complete once its loads landed (and in2 is upsampled)
+        const bool half = st.in2 && !p.in2_full;
+        // stage k is ready once its loads land (the MMA warp waits on full[] too), unless its
+        // half-resolution in2 must be upsampled first
+        if (!half && lane == 0) umma::mbar_arrive(&ready[buf]);
+        if (k >= 1 && prev_in2) {
+          // stage k - 1: upsample its in2 once it landed
           const int32_t pb = (k - 1) % nst;
           ok = ws_wait(&full[pb], ((k - 1) / nst) & 1, abort_v);
           if (!ok) break;
-          if (prev_in2) {
-            ws_expand(wg, smem, pb, prev_nc, prev_y0, lane);
-            umma::fence_async_shared();
-          }
+          ws_expand(wg, smem, pb, prev_nc, prev_y0, lane);
+          umma::fence_async_shared();
           __syncwarp();
           if (lane == 0) umma::mbar_arrive(&ready[pb]);
         }
-        prev_in2 = st.in2 && !p.in2_full;
+        prev_in2 = half;
         prev_nc = st.nc;
         prev_y0 = y0;
       }
     }
-    if (ok && k >= 1) {
+    if (ok && k >= 1 && prev_in2) {
       const int32_t pb = (k - 1) % nst;
       ok = ws_wait(&full[pb], ((k - 1) / nst) & 1, abort_v);
       if (ok) {
-        if (prev_in2) {
-          ws_expand(wg, smem, pb, prev_nc, prev_y0, lane);
-          umma::fence_async_shared();
-        }
+        ws_expand(wg, smem, pb, prev_nc, prev_y0, lane);
+        umma::fence_async_shared();
         __syncwarp();
         if (lane == 0) umma::mbar_arrive(&ready[pb]);
       }
     }
     if (!ok && lane == 0) {
       // the copies in flight land before the CTA's shared memory is released
-      for (int32_t kk = max(0, issued - nst); kk < issued; ++kk) umma::mbar_wait(&full[kk % nst], (kk / nst) & 1);
+      const int32_t nb = wg.ring ? wg.nslot : nst;
+      for (int32_t kk = max(0, issued - nb); kk < issued; ++kk) umma::mbar_wait(&full[kk % nb], (kk / nb) & 1);
     }
   } else if (warp == 5) {
     // ---- MMA issuer ----
@@ -410,7 +471,52 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
       const uint32_t bchunk16 = (uint32_t)(2 * cout);
       if (wg.resident) ok = ws_wait(&wbar, 0, abort_v);
       int32_t k = 0, i = 0, last = -1;
-      for (int32_t tile = blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x, ++i) {
+      if (wg.ring) {
+        // tile row y of a run uses the ring rows y - 1, y, y + 1 (loads base + j, j = y - y_run
+        // + dy); a row is released after its last tile: row y - 1 after tile y, and the run's last
+        // two rows after its last tile
+        const uint64_t b_all = umma::make_desc(s0 + wg.b_off, cout * 16, 128);
+        const uint32_t plane16 = (uint32_t)wg.rowplane >> 4;
+        int32_t base = 0, waited = 0, img, y0, x0;
+        while (ok && cta_tile(wg, i, img, y0, x0)) {
+          int32_t n = 1, img2, y2, x2;
+          while (cta_tile(wg, i + n, img2, y2, x2) && img2 == img && x2 == x0) ++n;
+          for (int32_t j = 0; j < n && ok; ++j, ++i) {
+            const int32_t b = i & 1;
+            if (i >= 2) ok = ws_wait(&acc_empty[b], ((i >> 1) + 1) & 1, abort_v);
+            while (ok && waited <= base + j + 2) {
+              ok = ws_wait(&full[waited % wg.nslot], (waited / wg.nslot) & 1, abort_v);
+              ++waited;
+            }
+            if (!ok) break;
+            umma::fence_after_sync();
+            const uint32_t acc = tmem + (uint32_t)(b * wg.acc_cols);
+            for (int32_t dy = 0; dy < 3; ++dy) {
+              const uint32_t slot_addr = s0 + ((base + j + dy) % wg.nslot) * wg.slot_bytes;
+              const uint64_t a_row = umma::make_desc(slot_addr, wg.rowplane, 128);
+              const uint64_t a_in2 = umma::make_desc(slot_addr + wg.in2_off, wg.rowplane, 128);
+              for (int32_t cc = 0; cc < nchunk; ++cc) {
+                const uint64_t ad = cc < nci ? a_row + 2 * cc * plane16 : a_in2 + 2 * (cc - nci) * plane16;
+                const uint64_t bd = b_all + cc * bchunk16;
+#pragma unroll
+                for (int32_t dx = 0; dx < 3; ++dx) {
+                  umma::mma_bf16(acc, ad + dx, bd + (dy * 3 + dx) * btap16, idesc, dy > 0 || cc > 0 || dx > 0);
+                }
+              }
+            }
+            umma::commit(&empty[(base + j) % wg.nslot]);
+            last = (base + j) % wg.nslot;
+            if (j == n - 1) {
+              umma::commit(&empty[(base + j + 1) % wg.nslot]);
+              umma::commit(&empty[(base + j + 2) % wg.nslot]);
+            }
+            umma::commit(&acc_full[b]);
+          }
+          base += n + 2;
+        }
+        k = waited;
+      }
+      for (int32_t tile = wg.ring ? wg.ntiles : blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x, ++i) {
         const int32_t b = i & 1;
         if (i >= 2) ok = ws_wait(&acc_empty[b], ((i >> 1) + 1) & 1, abort_v);
         if (!ok) break;
@@ -419,7 +525,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
         for (int32_t sidx = 0; sidx < nsp; ++sidx, ++k) {
           const StageInfo st = stage_info(sidx, nci, nchunk, G);
           const int32_t buf = k % nst;
-          ok = ws_wait(&ready[buf], (k / nst) & 1, abort_v);
+          ok = ws_wait(&full[buf], (k / nst) & 1, abort_v) && ws_wait(&ready[buf], (k / nst) & 1, abort_v);
           if (!ok) break;
           umma::fence_after_sync();
           const uint64_t a_stage = umma::make_desc(s0 + buf * wg.abuf, wg.plane, 128);
@@ -441,17 +547,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
         umma::commit(&acc_full[b]);
       }
       if (!ok && last >= 0) {
-        // the MMAs in flight complete before their accumulators are released
-        umma::mbar_wait(&empty[last], ((k - 1) / nst) & 1);
+        // the MMAs in flight complete before their operands and accumulators are released
+        umma::commit(&drain);
+        umma::mbar_wait(&drain, 0);
       }
     }
   } else {
     // ---- epilogue: warp w reads accumulator rows (pixels) 32 w .. 32 w + 31 ----
     const int32_t m = tid;
-    int32_t i = 0;
-    for (int32_t tile = blockIdx.x; tile < wg.ntiles; tile += gridDim.x, ++i) {
+    int32_t img, y0, x0;
+    for (int32_t i = 0; cta_tile(wg, i, img, y0, x0); ++i) {
       const int32_t b = i & 1;
-      ok = ws_wait(&acc_full[b], (i >> 1) & 1, abort_v);
+      ok = ws_wait(&acc_full[b], (i >> 1) & 1, abort_v, kEpilogueBackoffNs);
       // tcgen05.ld is warp-collective
       if (!__all_sync(0xFFFFFFFFu, ok)) {
         ok = false;
@@ -459,8 +566,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv3x3_ws_kernel(const __grid_
         break;
       }
       umma::fence_after_sync();
-      int32_t img, y0, x0;
-      tile_origin(g, tile, img, y0, x0);
       const int64_t pix = ((int64_t)img * p.height + y0 + m / g.pitch) * p.width + x0 + m % g.pitch;
       const uint32_t acc = tmem + (uint32_t)(b * wg.acc_cols) + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
@@ -579,6 +684,16 @@ int make_weight_map(CUtensorMap* m, const void* base, int32_t cin, int32_t cout,
   return encode(m, base, 4, dims, strides, box);
 }
 
+// MJPBR_CONV_RING=0 keeps single-row tiles on the staged pipeline (kept for comparison).
+bool conv_ring_enabled() {
+  static int enabled = -1;
+  if (enabled < 0) {
+    const char* v = getenv("MJPBR_CONV_RING");
+    enabled = (v && v[0] == '0') ? 0 : 1;
+  }
+  return enabled == 1;
+}
+
 // MJPBR_CONV_PIPELINE=0 selects the one-tile-per-CTA kernel (kept for comparison).
 bool conv_pipeline_enabled() {
   static int enabled = -1;
@@ -653,12 +768,23 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     wg.group = G;
     wg.nstage = nst;
     wg.resident = resident;
+    // the row ring, when tiles are single rows, the skip input (if any) has full resolution and
+    // the weights plus at least four row slots fit
+    wg.rowplane = wg.spitch * 16;
+    wg.in2_off = (int32_t)round128((size_t)2 * nci * wg.rowplane);
+    wg.slot_bytes = (int32_t)round128((size_t)wg.in2_off + (size_t)2 * (nchunk - nci) * wg.rowplane);
+    wg.nslot = (int32_t)std::min<size_t>(kMaxSlots, kPipeSmemBudget > wbytes ? (kPipeSmemBudget - wbytes) / wg.slot_bytes : 0);
+    wg.ring = conv_ring_enabled() && wg.single && (c.c_in2 == 0 || c.in2_full) && wg.nslot >= 4;
     wg.abuf = (int32_t)round128((size_t)copies * 2 * G * wg.plane);
     wg.s2buf = half_in2 ? (int32_t)round128((size_t)2 * G * wg.s2plane) : 0;
     wg.bstage = resident ? 0 : 9 * 2 * G * c.c_out * 16;
     wg.s2_off = nst * wg.abuf;
     wg.b_off = wg.s2_off + nst * wg.s2buf;
-    const size_t smem = fixed + (size_t)nst * stage_bytes(G, resident);
+    if (wg.ring) {
+      wg.resident = 1;
+      wg.b_off = wg.nslot * wg.slot_bytes;
+    }
+    const size_t smem = wg.ring ? (size_t)wg.b_off + wbytes : fixed + (size_t)nst * stage_bytes(G, resident);
     if (smem > kPipeSmemMax) return set_error(MJPBR_ERR_ARG, "conv3x3: %zu bytes of shared memory needed", smem);
     static bool ws_smem_set = false;
     if (!ws_smem_set) {
@@ -668,10 +794,16 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     }
     CUtensorMap tm_in, tm_in2, tm_w;
     memset(&tm_in2, 0, sizeof(tm_in2));
-    if (make_act_map(&tm_in, c.in, c.c_in, c.width, c.height, c.nimg, wg.spitch, g.rows + 2, 2 * G) != 0) return MJPBR_ERR_CUDA;
-    if (half_in2 && make_act_map(&tm_in2, c.in2, c.c_in2, c.width / 2, c.height / 2, c.nimg, wg.s2w, wg.s2h, 2 * G) != 0) return MJPBR_ERR_CUDA;
-    if (c.c_in2 > 0 && c.in2_full && make_act_map(&tm_in2, c.in2, c.c_in2, c.width, c.height, c.nimg, wg.spitch, g.rows + 2, 2 * G) != 0) return MJPBR_ERR_CUDA;
-    if (make_weight_map(&tm_w, c.weight, g.cin, c.c_out, resident ? 2 * nchunk : 2 * G) != 0) return MJPBR_ERR_CUDA;
+    if (wg.ring) {
+      // boxes of one row of all channel groups of each input
+      if (make_act_map(&tm_in, c.in, c.c_in, c.width, c.height, c.nimg, wg.spitch, 1, 2 * nci) != 0) return MJPBR_ERR_CUDA;
+      if (c.c_in2 > 0 && make_act_map(&tm_in2, c.in2, c.c_in2, c.width, c.height, c.nimg, wg.spitch, 1, 2 * (nchunk - nci)) != 0) return MJPBR_ERR_CUDA;
+    } else {
+      if (make_act_map(&tm_in, c.in, c.c_in, c.width, c.height, c.nimg, wg.spitch, g.rows + 2, 2 * G) != 0) return MJPBR_ERR_CUDA;
+      if (half_in2 && make_act_map(&tm_in2, c.in2, c.c_in2, c.width / 2, c.height / 2, c.nimg, wg.s2w, wg.s2h, 2 * G) != 0) return MJPBR_ERR_CUDA;
+      if (c.c_in2 > 0 && c.in2_full && make_act_map(&tm_in2, c.in2, c.c_in2, c.width, c.height, c.nimg, wg.spitch, g.rows + 2, 2 * G) != 0) return MJPBR_ERR_CUDA;
+    }
+    if (make_weight_map(&tm_w, c.weight, g.cin, c.c_out, wg.resident ? 2 * nchunk : 2 * G) != 0) return MJPBR_ERR_CUDA;
     // resident CTAs per SM, limited by shared memory (1 KB of it reserved per CTA), registers
     // and the 512 tensor-memory columns (two accumulators per CTA)
     static cudaFuncAttributes attr = {};
