@@ -991,26 +991,35 @@ __global__ void __launch_bounds__(kConvThreads, 2) conv3x3_wgrad_kernel(const __
   if (warp == 0) umma::tmem_free(tmem, ncols);
 }
 
-// grad_bias[co] += sum over pixels of grad_out[p][co]: one CTA per 1024 pixels, shared partial
-// sums, one atomic per channel and CTA.
+// grad_bias[co] += sum over pixels of grad_out[p][co]: one CTA per kBiasPix pixels. Thread t sums
+// channel group t % (c_out / 8) of every (256 / groups)-th pixel in registers (consecutive threads
+// read consecutive 16-byte groups), then one shared atomic per channel and thread and one global
+// atomic per channel and CTA.
+constexpr int32_t kBiasPix = 4096;
+
 __global__ void __launch_bounds__(256) bias_grad_kernel(const uint16_t* __restrict__ grad_out, int64_t npix, int32_t cout,
                                                         float* __restrict__ grad_bias) {
   __shared__ float part[256];
   for (int32_t i = threadIdx.x; i < cout; i += blockDim.x) part[i] = 0.0f;
   __syncthreads();
-  const int64_t p0 = (int64_t)blockIdx.x * 1024;
-  const int64_t p1 = min(p0 + 1024, npix);
   const int32_t groups = cout / 8;
-  for (int64_t i = p0 * groups + threadIdx.x; i < p1 * groups; i += blockDim.x) {
-    const int64_t pix = i / groups;
-    const int32_t cg = (int32_t)(i - pix * groups);
-    const uint4 v = __ldg(reinterpret_cast<const uint4*>(grad_out + pix * cout + cg * 8));
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  const int32_t step = blockDim.x / groups;
+  const int32_t cg = threadIdx.x % groups, pofs = threadIdx.x / groups;
+  if (pofs < step) {
+    float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const int64_t p0 = (int64_t)blockIdx.x * kBiasPix;
+    const int64_t p1 = min(p0 + kBiasPix, npix);
+    for (int64_t pix = p0 + pofs; pix < p1; pix += step) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(grad_out + pix * cout + cg * 8));
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      atomicAdd(&part[cg * 8 + 2 * k], __uint_as_float(w[k] << 16));
-      atomicAdd(&part[cg * 8 + 2 * k + 1], __uint_as_float(w[k] & 0xFFFF0000u));
+      for (int k = 0; k < 4; ++k) {
+        acc[2 * k] += __uint_as_float(w[k] << 16);
+        acc[2 * k + 1] += __uint_as_float(w[k] & 0xFFFF0000u);
+      }
     }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) atomicAdd(&part[cg * 8 + k], acc[k]);
   }
   __syncthreads();
   for (int32_t i = threadIdx.x; i < cout; i += blockDim.x) atomicAdd(grad_bias + i, part[i]);
@@ -1055,7 +1064,7 @@ int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream) {
   if (int rc = check_launch("conv3x3_wgrad_kernel")) return rc;
   if (c.grad_bias) {
     const int64_t npix = (int64_t)c.nimg * c.height * c.width;
-    bias_grad_kernel<<<(unsigned)((npix + 1023) / 1024), 256, 0, stream>>>(c.grad_out, npix, c.c_out, c.grad_bias);
+    bias_grad_kernel<<<(unsigned)((npix + kBiasPix - 1) / kBiasPix), 256, 0, stream>>>(c.grad_out, npix, c.c_out, c.grad_bias);
     return check_launch("bias_grad_kernel");
   }
   return MJPBR_OK;
