@@ -123,7 +123,7 @@ typedef struct MjpbrConvGrad {
   int32_t* error_word;
   int32_t nimg, height, width, c_in, c_in2, c_out;
   int32_t tiles_per_cta; /* 128-pixel tiles each CTA accumulates before its atomic reduction (0: 64) */
-  int32_t pad_;
+  int32_t in2_full;      /* 1: in2 has the output resolution; 0: half of it, upsampled x2 */
 } MjpbrConvGrad;
 
 /* One mipmapped 2D texture inside MjpbrScene.tex_data (RGBA, row-major levels). */

@@ -287,7 +287,7 @@ class ConvGrad(ctypes.Structure):
     ("c_in2", c_i32),
     ("c_out", c_i32),
     ("tiles_per_cta", c_i32),
-    ("pad_", c_i32),
+    ("in2_full", c_i32),
   ]
 
 

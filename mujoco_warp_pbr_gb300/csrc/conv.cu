@@ -881,6 +881,7 @@ __device__ __forceinline__ uint4 load_in(const MjpbrConvGrad& p, int32_t img, in
   if (ch < p.c_in) {
     return __ldg(reinterpret_cast<const uint4*>(p.in + (((int64_t)img * p.height + iy) * p.width + ix) * p.c_in + ch));
   }
+  if (p.in2_full) return __ldg(reinterpret_cast<const uint4*>(p.in2 + (((int64_t)img * p.height + iy) * p.width + ix) * p.c_in2 + (ch - p.c_in)));
   const int32_t h2 = p.height >> 1, w2 = p.width >> 1;
   return __ldg(reinterpret_cast<const uint4*>(p.in2 + (((int64_t)img * h2 + (iy >> 1)) * w2 + (ix >> 1)) * p.c_in2 + (ch - p.c_in)));
 }
@@ -1025,6 +1026,221 @@ __global__ void __launch_bounds__(256) bias_grad_kernel(const uint16_t* __restri
   for (int32_t i = threadIdx.x; i < cout; i += blockDim.x) atomicAdd(grad_bias + i, part[i]);
 }
 
+
+// ---- weight gradients, warp-specialised: per tap, D_tap (c_out x cin, FP32 in tensor memory) +=
+// grad_out (c_out x pixels) * input shifted by the tap (cin x pixels)^T, K = the tile's 128
+// pixels, 16 per MMA. Both operands are MN-major (channels contiguous, as NHWC stores them), so
+// they are the TMA boxes as they land: grad_out as channel-group planes of 128 pixels x 16 bytes,
+// the input as the forward kernel stages it (halo rows, one copy with halo columns for one-row
+// tiles, three dx-shifted copies otherwise). MN-major descriptors: leading byte offset = stride
+// between 8-pixel groups (128 B), stride byte offset = stride between 8-channel groups (a plane).
+// M = c_out padded to 64 or 128 (zero planes); an M = 64 accumulator holds row r in tensor-memory
+// lane 32 (r / 16) + r % 16. Warp 4 loads, warps 5-7 issue the MMAs of taps j, j + 3, j + 6, and
+// after the CTA's tiles warps 0-3 add the accumulators to grad_weight with atomics. A launch
+// covers the taps whose accumulators fit the 512 tensor-memory columns (ntap x cin); the launcher
+// loops over tap ranges.
+constexpr int kWgThreads = 256;
+constexpr int kWgIssuers = 3;
+constexpr int kWgMaxStages = 6;
+
+struct WgGeom {
+  ConvGeom g;
+  int32_t ntiles;
+  int32_t single, spitch;
+  int32_t mpad;        // MMA M: 64 or 128
+  int32_t plane;       // bytes of one input channel-group plane: (rows + 2) x spitch x 16
+  int32_t in_copy;     // bytes of one input copy: (c_in / 8) planes
+  int32_t in2_copy;    // bytes of one in2 copy: (c_in2 / 8) planes
+  int32_t a_bytes;     // grad_out planes per stage: mpad / 8 x 2 KB
+  int32_t in_off, in2_off, stage_bytes;
+  int32_t nstage;
+  int32_t tap0, ntap;  // taps of this launch
+  int32_t tmem_cols;
+};
+
+__global__ void __launch_bounds__(kWgThreads, 1) conv3x3_wgrad_ws_kernel(const __grid_constant__ MjpbrConvGrad p, const __grid_constant__ WgGeom wg,
+                                                                         const __grid_constant__ CUtensorMap tm_go, const __grid_constant__ CUtensorMap tm_in,
+                                                                         const __grid_constant__ CUtensorMap tm_in2) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t full[kWgMaxStages], empty[kWgMaxStages], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int32_t abort_flag;
+  const ConvGeom& g = wg.g;
+  const int32_t cout = p.c_out, cin = g.cin;
+  const int32_t nst = wg.nstage;
+  const int32_t issuers = min(kWgIssuers, wg.ntap);
+  const uint32_t s0 = umma::smem_addr(smem);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // zero planes of the padded M rows (never written by the TMA)
+  for (int32_t st = 0; st < nst; ++st) {
+    for (int32_t i = (cout / 8) * 128 + tid; i < wg.a_bytes / 16; i += kWgThreads) {
+      *reinterpret_cast<uint4*>(smem + st * wg.stage_bytes + i * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+  umma::fence_async_shared();
+  if (warp == 0) umma::tmem_alloc(&tmem_slot, (uint32_t)wg.tmem_cols);
+  if (tid == 128) {
+    for (int i = 0; i < nst; ++i) {
+      umma::mbar_init(&full[i], 1);
+      umma::mbar_init(&empty[i], issuers);
+    }
+    umma::mbar_init(&done, issuers);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  volatile int32_t* abort_v = &abort_flag;
+  bool ok = true;
+  const int32_t copies = wg.single ? 1 : 3;
+  if (warp == 4) {
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)(16 * kTilePx * (cout / 8) + copies * (wg.in_copy + wg.in2_copy));
+      int32_t k = 0, issued = 0;
+      for (int32_t tile = blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x, ++k) {
+        int32_t img, y0, x0;
+        tile_origin(g, tile, img, y0, x0);
+        const int32_t buf = k % nst;
+        if (k >= nst) ok = ws_wait(&empty[buf], ((k / nst) + 1) & 1, abort_v, kLoaderBackoffNs);
+        if (!ok) break;
+        const uint32_t base = s0 + buf * wg.stage_bytes;
+        umma::mbar_arrive_expect_tx(&full[buf], bytes);
+        umma::tma_load_5d(base, &tm_go, &full[buf], 0, x0, y0, 0, img);
+        for (int32_t dx = 0; dx < copies; ++dx) {
+          const int32_t xs = wg.single ? x0 - 1 : dx - 1;
+          umma::tma_load_5d(base + wg.in_off + dx * wg.in_copy, &tm_in, &full[buf], 0, xs, y0 - 1, 0, img);
+          if (p.c_in2 > 0) umma::tma_load_5d(base + wg.in2_off + dx * wg.in2_copy, &tm_in2, &full[buf], 0, xs, y0 - 1, 0, img);
+        }
+        issued = k + 1;
+      }
+      if (!ok) {
+        // the copies in flight land before the CTA's shared memory is released
+        for (int32_t kk = max(0, issued - nst); kk < issued; ++kk) umma::mbar_wait(&full[kk % nst], (kk / nst) & 1);
+      }
+    }
+  } else if (warp >= 5 && warp < 5 + issuers) {
+    if (lane == 0) {
+      const int32_t j = warp - 5;
+      const uint32_t id_in = umma::make_idesc_bf16((uint32_t)wg.mpad, (uint32_t)p.c_in) | (1u << 15) | (1u << 16);
+      const uint32_t id_in2 = p.c_in2 > 0 ? umma::make_idesc_bf16((uint32_t)wg.mpad, (uint32_t)p.c_in2) | (1u << 15) | (1u << 16) : 0u;
+      int32_t k = 0;
+      bool issued = false;
+      for (int32_t tile = blockIdx.x; tile < wg.ntiles && ok; tile += gridDim.x, ++k) {
+        const int32_t buf = k % nst;
+        ok = ws_wait(&full[buf], (k / nst) & 1, abort_v);
+        if (!ok) break;
+        umma::fence_after_sync();
+        const uint32_t base = s0 + buf * wg.stage_bytes;
+        const uint64_t a0 = umma::make_desc(base, 128, 2048);
+        const uint64_t b_in = umma::make_desc(base + wg.in_off, 128, wg.plane);
+        const uint64_t b_in2 = umma::make_desc(base + wg.in2_off, 128, wg.plane);
+        for (int32_t t = j; t < wg.ntap; t += kWgIssuers) {
+          const int32_t tap = wg.tap0 + t, dy = tap / 3, dx = tap % 3;
+          // start of the tap's view of the staged input, in 16-byte units
+          const uint32_t sh = wg.single ? (uint32_t)(dy * wg.spitch + dx) : (uint32_t)(dx * wg.in_copy + dy * g.pitch * 16) >> 4;
+          const uint32_t sh2 = wg.single ? sh : (uint32_t)(dx * wg.in2_copy + dy * g.pitch * 16) >> 4;
+          const uint32_t d = tmem + (uint32_t)(t * cin);
+#pragma unroll 1
+          for (int32_t ks = 0; ks < kTilePx / 16; ++ks) {
+            const bool acc = k > 0 || ks > 0;
+            umma::mma_bf16(d, a0 + ks * 16, b_in + sh + ks * 16, id_in, acc);
+            if (p.c_in2 > 0) umma::mma_bf16(d + (uint32_t)p.c_in, a0 + ks * 16, b_in2 + sh2 + ks * 16, id_in2, acc);
+          }
+        }
+        umma::commit(&empty[buf]);
+        issued = true;
+      }
+      // done completes once every issuer's MMAs completed
+      umma::commit(&done);
+      if (!ok && issued) umma::mbar_wait(&done, 0);
+    }
+  } else if (warp < 4) {
+    // ---- epilogue: accumulator rows -> grad_weight ----
+    ok = ws_wait(&done, 0, abort_v, kEpilogueBackoffNs);
+    if (__all_sync(0xFFFFFFFFu, ok)) {
+      umma::fence_after_sync();
+      const int32_t row = wg.mpad == 128 ? tid : (lane < 16 ? warp * 16 + lane : -1);
+      for (int32_t t = 0; t < wg.ntap; ++t) {
+        const int32_t tap = wg.tap0 + t;
+        for (int32_t c0 = 0; c0 < cin; c0 += 16) {
+          float v[16];
+          umma::tmem_load16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * cin + c0), v);
+          if (row >= 0 && row < cout) {
+            float* gw = p.grad_weight + ((int64_t)row * 9 + tap) * cin + c0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) atomicAdd(gw + i, v[i]);
+          }
+        }
+      }
+    } else {
+      ok = false;
+    }
+  }
+  if (!ok && tid % 32 == 0 && p.error_word) atomicOr(p.error_word, kErrWaitTimeout);
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_free(tmem, (uint32_t)wg.tmem_cols);
+}
+
+
+constexpr int kWgradWsUnsuitable = -1000;
+
+// Plans and launches conv3x3_wgrad_ws_kernel over the tap ranges that fit tensor memory;
+// kWgradWsUnsuitable when two stages do not fit shared memory (the caller falls back).
+int wgrad_ws_launch(const MjpbrConvGrad& c, const WgradGeom& gg, cudaStream_t stream) {
+  WgGeom wg;
+  wg.g.pitch = gg.pitch;
+  wg.g.rows = gg.rows;
+  wg.g.tiles_per_row = gg.tiles_per_row;
+  wg.g.tiles_per_img = gg.tiles_per_img;
+  wg.g.cin = gg.cin;
+  wg.ntiles = gg.total;
+  wg.single = gg.rows == 1;
+  wg.spitch = wg.single ? gg.pitch + 2 : gg.pitch;
+  wg.mpad = c.c_out <= 64 ? 64 : 128;
+  if (c.c_out > 128) return kWgradWsUnsuitable;
+  const int32_t copies = wg.single ? 1 : 3;
+  auto round128 = [](int64_t v) { return (int32_t)((v + 127) / 128 * 128); };
+  wg.plane = (gg.rows + 2) * wg.spitch * 16;
+  wg.in_copy = (c.c_in / 8) * wg.plane;
+  wg.in2_copy = (c.c_in2 / 8) * wg.plane;
+  wg.a_bytes = wg.mpad / 8 * 2048;
+  wg.in_off = wg.a_bytes;
+  wg.in2_off = round128((int64_t)wg.in_off + (int64_t)copies * wg.in_copy);
+  wg.stage_bytes = round128((int64_t)wg.in2_off + (int64_t)copies * wg.in2_copy);
+  // TMA destinations are 128-byte aligned: the dx copies must be too
+  if (!wg.single && ((wg.in_copy % 128) || (wg.in2_copy % 128))) return kWgradWsUnsuitable;
+  wg.nstage = std::min<int64_t>(kWgMaxStages, (int64_t)kPipeSmemMax / wg.stage_bytes);
+  if (wg.nstage < 2) return kWgradWsUnsuitable;
+  const size_t smem = (size_t)wg.nstage * wg.stage_bytes;
+  static bool smem_set = false;
+  if (!smem_set) {
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmemMax);
+    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "conv3x3 wgrad: %zu bytes of shared memory: %s", kPipeSmemMax, cudaGetErrorString(e));
+    smem_set = true;
+  }
+  CUtensorMap tm_go, tm_in, tm_in2;
+  memset(&tm_in2, 0, sizeof(tm_in2));
+  if (make_act_map(&tm_go, c.grad_out, c.c_out, c.width, c.height, c.nimg, gg.pitch, gg.rows, c.c_out / 8) != 0) return MJPBR_ERR_CUDA;
+  if (make_act_map(&tm_in, c.in, c.c_in, c.width, c.height, c.nimg, wg.spitch, gg.rows + 2, c.c_in / 8) != 0) return MJPBR_ERR_CUDA;
+  if (c.c_in2 > 0 && make_act_map(&tm_in2, c.in2, c.c_in2, c.width, c.height, c.nimg, wg.spitch, gg.rows + 2, c.c_in2 / 8) != 0) return MJPBR_ERR_CUDA;
+  const int32_t per_pass = std::min(9, 512 / gg.cin);
+  if (per_pass < 1) return kWgradWsUnsuitable;
+  const int64_t grid = std::min<int64_t>(gg.total, conv_sm_count());
+  for (int32_t t0 = 0; t0 < 9; t0 += per_pass) {
+    wg.tap0 = t0;
+    wg.ntap = std::min(per_pass, 9 - t0);
+    int32_t cols = 32;
+    while (cols < wg.ntap * gg.cin) cols <<= 1;
+    wg.tmem_cols = cols;
+    conv3x3_wgrad_ws_kernel<<<(unsigned)grid, kWgThreads, smem, stream>>>(c, wg, tm_go, tm_in, tm_in2);
+    if (int rc = check_launch("conv3x3_wgrad_ws_kernel")) return rc;
+  }
+  return MJPBR_OK;
+}
+
 }  // namespace
 
 int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream) {
@@ -1034,7 +1250,8 @@ int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream) {
     return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: channels must be multiples of 16 (c_out <= 256), got %d + %d -> %d", c.c_in,
                      c.c_in2, c.c_out);
   }
-  if (c.c_in2 > 0 && (!c.in2 || c.height % 2 || c.width % 2)) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: in2 needs even sizes");
+  if (c.c_in2 > 0 && !c.in2) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: c_in2 > 0 needs in2");
+  if (c.c_in2 > 0 && !c.in2_full && (c.height % 2 || c.width % 2)) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: a half-resolution in2 needs even sizes");
   const int32_t w = c.width;
   const bool row_ok = (w >= 128) ? (w % 128 == 0) : (w >= 16 && 128 % w == 0);
   if (!row_ok) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: width %d is not a power of two in [16, 128] or a multiple of 128", w);
@@ -1050,6 +1267,18 @@ int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream) {
   if (total > INT32_MAX) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: too many tiles");
   g.total = (int32_t)total;
   g.per_cta = c.tiles_per_cta > 0 ? c.tiles_per_cta : 64;
+  if (conv_pipeline_enabled() && (c.c_in2 == 0 || c.in2_full) && (int64_t)c.nimg * c.height * c.width <= INT32_MAX) {
+    const int rc = wgrad_ws_launch(c, g, stream);
+    if (rc != kWgradWsUnsuitable) {
+      if (rc != MJPBR_OK) return rc;
+      if (c.grad_bias) {
+        const int64_t npix = (int64_t)c.nimg * c.height * c.width;
+        bias_grad_kernel<<<(unsigned)((npix + kBiasPix - 1) / kBiasPix), 256, 0, stream>>>(c.grad_out, npix, c.c_out, c.grad_bias);
+        return check_launch("bias_grad_kernel");
+      }
+      return MJPBR_OK;
+    }
+  }
   const int32_t mblocks = (9 * g.cin + 127) / 128;
   const int32_t splits = (g.total + g.per_cta - 1) / g.per_cta;
   if (splits > 65535) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: %d tile runs exceed the grid; raise tiles_per_cta", splits);

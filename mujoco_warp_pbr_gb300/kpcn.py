@@ -214,6 +214,7 @@ class KPCN:
     _lib.call("mjpbr_conv3x3_bf16", ctypes.byref(c), self._stream())
 
   def _wgrad(self, name: str, x: torch.Tensor, dy: torch.Tensor, x2: torch.Tensor | None = None) -> None:
+    """x2: the skip input at the resolution of x (the forward pass's upsampled copy)."""
     l = self.layers[name]
     s = l.spec
     n, h, w, _ = x.shape
@@ -221,7 +222,7 @@ class KPCN:
     per_cta = max(8, (tiles + 2047) // 2048)
     g = _lib.ConvGrad(
       in_=_ptr(x), in2=_ptr(x2), grad_out=_ptr(dy), grad_weight=_ptr(l.gw), grad_bias=_ptr(l.gb), error_word=_ptr(self.error),
-      nimg=n, height=h, width=w, c_in=s.c_in, c_in2=s.c_in2, c_out=s.c_out, tiles_per_cta=per_cta,
+      nimg=n, height=h, width=w, c_in=s.c_in, c_in2=s.c_in2, c_out=s.c_out, tiles_per_cta=per_cta, in2_full=1,
     )
     _lib.call("mjpbr_conv3x3_wgrad_bf16", ctypes.byref(g), self._stream())
 
@@ -277,17 +278,17 @@ class KPCN:
     dg("head", ws["dlogits"], ws["dv0"], mask=ws["v0"])
     wg("d0b", ws["u0"], ws["dv0"])
     dg("d0b", ws["dv0"], ws["du0"], mask=ws["u0"])
-    wg("d0a", ws["s0"], ws["du0"], x2=ws["v1"])
+    wg("d0a", ws["s0"], ws["du0"], x2=ws["up0"])
     dg("d0a", ws["du0"], None, out_f32=ws["dcat0"])
     _lib.call("mjpbr_split_concat_grad", _ptr(ws["dcat0"]), _ptr(ws["v1"]), _ptr(ws["dskip0"]), _ptr(ws["dv1"]), n, h, w, w0, w1, st)
     wg("d1b", ws["u1"], ws["dv1"])
     dg("d1b", ws["dv1"], ws["du1"], mask=ws["u1"])
-    wg("d1a", ws["s1"], ws["du1"], x2=ws["v2"])
+    wg("d1a", ws["s1"], ws["du1"], x2=ws["up1"])
     dg("d1a", ws["du1"], None, out_f32=ws["dcat1"])
     _lib.call("mjpbr_split_concat_grad", _ptr(ws["dcat1"]), _ptr(ws["v2"]), _ptr(ws["dskip1"]), _ptr(ws["dv2"]), n, h >> 1, w >> 1, w1, w2, st)
     wg("d2b", ws["u2"], ws["dv2"])
     dg("d2b", ws["dv2"], ws["du2"], mask=ws["u2"])
-    wg("d2a", ws["s2"], ws["du2"], x2=ws["b3"])
+    wg("d2a", ws["s2"], ws["du2"], x2=ws["up2"])
     dg("d2a", ws["du2"], None, out_f32=ws["dcat2"])
     _lib.call("mjpbr_split_concat_grad", _ptr(ws["dcat2"]), _ptr(ws["b3"]), _ptr(ws["dskip2"]), _ptr(ws["db3"]), n, h >> 2, w >> 2, w2, w3, st)
     wg("e3b", ws["a3"], ws["db3"])

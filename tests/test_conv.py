@@ -113,7 +113,7 @@ def test_conv3x3_matches_cpu(nimg, h, w, c1, c2, cout, use_bias, relu, use_mask,
 
 def wgrad_ref(x, dy, x2=None):
   if x2 is not None:
-    up = np.repeat(np.repeat(x2, 2, axis=1), 2, axis=2)
+    up = x2 if x2.shape[1] == x.shape[1] else np.repeat(np.repeat(x2, 2, axis=1), 2, axis=2)
     x = np.concatenate([x, up], axis=-1)
   n, h, w, c = x.shape
   xp = np.zeros((n, h + 2, w + 2, c))
@@ -132,18 +132,27 @@ WGRAD_CASES = [
   (2, 32, 32, 32, 16, 64, 5),
   (1, 4, 256, 16, 0, 16, 1),
   (3, 16, 64, 48, 96, 96, 0),
+  (40, 32, 128, 32, 0, 32, 0),
+]
+# the same with a full-resolution skip input
+WGRAD_FULL_CASES = [
+  (2, 32, 32, 32, 16, 64, 0),
+  (3, 16, 64, 48, 96, 96, 0),
+  (4, 16, 128, 32, 48, 32, 0),
+  (2, 8, 256, 16, 32, 48, 0),
 ]
 
 
 @pytest.mark.gpu
 @pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
-@pytest.mark.parametrize("nimg,h,w,c1,c2,cout,per_cta", WGRAD_CASES)
-def test_conv3x3_wgrad_matches_cpu(nimg, h, w, c1, c2, cout, per_cta):
+@pytest.mark.parametrize("nimg,h,w,c1,c2,cout,per_cta,full", [c + (False,) for c in WGRAD_CASES] + [c + (True,) for c in WGRAD_FULL_CASES])
+def test_conv3x3_wgrad_matches_cpu(nimg, h, w, c1, c2, cout, per_cta, full):
   from mujoco_warp_pbr_gb300 import _lib
 
   g = torch.Generator().manual_seed(nimg * 100 + h + w * 3 + c1 + c2 + cout)
   x = (torch.rand((nimg, h, w, c1), generator=g) * 2 - 1).to(torch.bfloat16)
-  x2 = (torch.rand((nimg, h // 2, w // 2, c2), generator=g) * 2 - 1).to(torch.bfloat16) if c2 else None
+  s2 = 1 if full else 2
+  x2 = (torch.rand((nimg, h // s2, w // s2, c2), generator=g) * 2 - 1).to(torch.bfloat16) if c2 else None
   dy = (torch.rand((nimg, h, w, cout), generator=g) * 2 - 1).to(torch.bfloat16)
   ref_w, ref_b = wgrad_ref(
     x.float().numpy().astype(np.float64), dy.float().numpy().astype(np.float64), None if x2 is None else x2.float().numpy().astype(np.float64)
@@ -155,7 +164,7 @@ def test_conv3x3_wgrad_matches_cpu(nimg, h, w, c1, c2, cout, per_cta):
   c = _lib.ConvGrad(
     in_=dx.data_ptr(), in2=dx2.data_ptr() if dx2 is not None else None, grad_out=ddy.data_ptr(), grad_weight=gw.data_ptr(),
     grad_bias=gb.data_ptr(), error_word=err.data_ptr(), nimg=nimg, height=h, width=w, c_in=c1, c_in2=c2, c_out=cout,
-    tiles_per_cta=per_cta,
+    tiles_per_cta=per_cta, in2_full=int(full),
   )
   _lib.call("mjpbr_conv3x3_wgrad_bf16", ctypes.byref(c), torch.cuda.current_stream().cuda_stream)
   torch.cuda.synchronize()
