@@ -475,7 +475,7 @@ def learned_denoiser(args) -> dict | None:
   from mujoco_warp_pbr_gb300 import train_kpcn
 
   net = kpcn.KPCN.load(WEIGHTS)
-  out = train_kpcn.evaluate(net, nworld=args.learned_worlds, res=128, ref_spp=args.learned_ref_spp)
+  out = train_kpcn.evaluate(net, nworld=args.learned_worlds, res=128, ref_spp=args.learned_ref_spp, time_worlds=args.learned_time_worlds)
   out["weights"] = str(WEIGHTS.relative_to(ROOT))
   return out
 
@@ -673,8 +673,10 @@ def main() -> None:
   p.add_argument("--spp", type=int, default=2)
   p.add_argument("--no-path-tier", action="store_true")
   p.add_argument("--no-learned", action="store_true")
-  p.add_argument("--learned-worlds", type=int, default=256)
-  p.add_argument("--learned-ref-spp", type=int, default=1024)
+  # quality against 4096-spp references on 64 worlds, throughput on the C4 batch of 1024 worlds
+  p.add_argument("--learned-worlds", type=int, default=64)
+  p.add_argument("--learned-ref-spp", type=int, default=4096)
+  p.add_argument("--learned-time-worlds", type=int, default=1024)
   p.add_argument("--nworld", type=int, default=None)
   p.add_argument("--res", type=int, default=None)
   p.add_argument("--seed", type=int, default=0)

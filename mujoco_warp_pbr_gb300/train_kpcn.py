@@ -142,10 +142,25 @@ def timed(fn, reps: int = 3) -> float:
   return e0.elapsed_time(e1) / reps
 
 
-def evaluate(net: kpcn_lib.KPCN, nworld: int, res: int, ref_spp: int, seed: int = 9000) -> dict:
-  """relMSE against ref_spp references and Mpix/s of the three pipelines on a held-out frame."""
+def evaluate(net: kpcn_lib.KPCN, nworld: int, res: int, ref_spp: int, seed: int = 9000, time_worlds: int | None = None) -> dict:
+  """relMSE against ref_spp references and Mpix/s of the pipelines on a held-out frame of nworld
+  worlds; with time_worlds, the Mpix/s are measured on a second frame of that many worlds (the
+  same scene seed), so that the quality reference and the throughput batch can differ in size."""
+  out = quality_and_speed(net, nworld, res, ref_spp, seed)
+  if time_worlds and time_worlds != nworld:
+    speed = quality_and_speed(net, time_worlds, res, 0, seed)
+    for k, v in speed.items():
+      if isinstance(v, dict) and "ms" in v:
+        out[k]["ms"], out[k]["mpix_s"] = v["ms"], v["mpix_s"]
+    out["time_worlds"] = time_worlds
+    out["speedup_learned2_vs_atrous16"] = out["atrous_16spp"]["ms"] / out["learned_2spp"]["ms"]
+  return out
+
+
+def quality_and_speed(net: kpcn_lib.KPCN, nworld: int, res: int, ref_spp: int, seed: int) -> dict:
+  """relMSE against ref_spp references (none when ref_spp is 0) and Mpix/s of the pipelines."""
   fr = make_frame(seed, nworld, res)
-  ref = converged_hdr(fr, ref_spp).float()
+  ref = converged_hdr(fr, ref_spp).float() if ref_spp > 0 else None
   npix = nworld * res * res
   out = {"ref_spp": ref_spp, "nworld": nworld, "res": res}
   # learned denoiser at 2 spp
@@ -157,22 +172,22 @@ def evaluate(net: kpcn_lib.KPCN, nworld: int, res: int, ref_spp: int, seed: int 
     net.denoise(fr.m, fr.d, rc2)
 
   ms = timed(learned)
-  out["learned_2spp"] = {"rel_mse": rel_mse(rc2.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  out["learned_2spp"] = {"rel_mse": rel_mse(rc2.hdr_data, ref) if ref is not None else None, "ms": ms, "mpix_s": npix / ms / 1e3}
   # a-trous at 16 spp, 5 iterations
   rc16 = fr.context(path_samples=16, denoise=True, denoise_iterations=5, render_hdr=True)
   mjpbr.refit_bvh(fr.m, fr.d, rc16)
   ms = timed(lambda: mjpbr.render(fr.m, fr.d, rc16, seed=5))
-  out["atrous_16spp"] = {"rel_mse": rel_mse(rc16.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  out["atrous_16spp"] = {"rel_mse": rel_mse(rc16.hdr_data, ref) if ref is not None else None, "ms": ms, "mpix_s": npix / ms / 1e3}
   # a-trous at 2 spp and plain 16 / 2 spp for context
   rca = fr.context(path_samples=2, denoise=True, denoise_iterations=5, render_hdr=True)
   mjpbr.refit_bvh(fr.m, fr.d, rca)
   ms = timed(lambda: mjpbr.render(fr.m, fr.d, rca, seed=5))
-  out["atrous_2spp"] = {"rel_mse": rel_mse(rca.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+  out["atrous_2spp"] = {"rel_mse": rel_mse(rca.hdr_data, ref) if ref is not None else None, "ms": ms, "mpix_s": npix / ms / 1e3}
   for spp in (2, 16):
     rcp = fr.context(path_samples=spp, render_hdr=True)
     mjpbr.refit_bvh(fr.m, fr.d, rcp)
     ms = timed(lambda rcp=rcp: mjpbr.render(fr.m, fr.d, rcp, seed=5))
-    out[f"plain_{spp}spp"] = {"rel_mse": rel_mse(rcp.hdr_data, ref), "ms": ms, "mpix_s": npix / ms / 1e3}
+    out[f"plain_{spp}spp"] = {"rel_mse": rel_mse(rcp.hdr_data, ref) if ref is not None else None, "ms": ms, "mpix_s": npix / ms / 1e3}
   out["speedup_learned2_vs_atrous16"] = out["atrous_16spp"]["ms"] / out["learned_2spp"]["ms"]
   return out
 
