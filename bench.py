@@ -544,7 +544,8 @@ def run_large(args) -> None:
                "l2": "frame working set far above L2"},
     "e2e": {"value": npix / e2e_ms / 1e3, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4), "d2h_bytes_per_step": int(out_host.numel() * 4)},
     "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
-    "gpu_launches": None,
+    # per replay: refit, path tracer, the denoiser's kernels (the pose copy is a memcpy node)
+    "gpu_launches": (2 + kpcn.denoise_launches(rc, args.chunk)) * args.steps,
     "clocks": clocks.summary(),
   }))
 

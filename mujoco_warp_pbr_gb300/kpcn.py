@@ -383,6 +383,16 @@ class KPCN:
     _lib.call("mjpbr_denoise_atrous", ctypes.byref(finish[1]), st)
 
 
+def denoise_launches(rc: Any, chunk: int = 512) -> int:
+  """Kernels one KPCN.denoise call launches: per RGB camera and chunk of worlds the features
+  kernel and the forward pass (15 convolutions, 3 poolings, 3 upsamplings, the kernel
+  application), then one finish pass."""
+  per_forward = len(layer_specs()) + 3 + 3 + 1
+  chunks = -(-rc.nworld // chunk)
+  cams = sum(1 for v in rc.base.render_rgb if v)
+  return cams * chunks * (1 + per_forward) + 1
+
+
 def forward_flops(nimg: int, h: int, w: int) -> int:
   """Multiply-add FLOPs (2 per MAC) of the network's convolutions for a batch."""
   total = 0
