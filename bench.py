@@ -13,7 +13,12 @@ environment rotation). A step is refit_bvh + render of one frame of every world.
   roofline   the render kernel's algorithmic HBM bytes (outputs written once, world blocks and
              tables read once) per launch over its event-timed duration, against the measured
              copy bandwidth; the kernel is bound by FP32 issue and traversal latency, not HBM,
-             so this fraction is small by construction (see "issue").
+             so this fraction is small by construction.
+  roofline_fp32, rays_per_s  the real-time kernel's algorithmic FP32 work: a 256-world frame of the
+             same scene rendered by the counting build (libmjpbr_count.so) counts ray queries,
+             box / triangle / primitive tests and shading work; FLOPS_PER_OP of
+             mujoco_warp_pbr_gb300/roofline.py turns them into FLOPs per pixel, scaled to the timed
+             frame over the product kernel's render time, against the nominal FP32 peak.
   cpu_baseline  the CPU oracle (scalar C restatement of the reference's real-time tier, OpenMP
              over all host cores) on a bounded sample of the same workload.
 
@@ -448,11 +453,15 @@ def run(args) -> None:
       },
       "render_ms": render_avg,
       "refit_ms": (total_ms / args.steps) - render_avg,
-      "rays_note": "primary rays = pixels x supersamples; shadow and mirror rays extra",
+      "rays_note": "rays_per_s: every ray query of the frame (primary, shadow, mirror), counted by the counting build",
       "gpu_launches": 2 * args.steps,
       "clocks": clocks.summary(),
       "cpu_baseline": baseline,
     }
+    if args.workload in ("mesh_ibl", "primitives"):
+      rt = rt_fp32_roofline(args, dev, npix, render_avg)
+      line["roofline_fp32"] = rt
+      line["rays_per_s"] = rt["rays_per_px"] * npix / (render_avg / 1000.0)
     if args.workload == "mesh_ibl" and not args.no_path_tier:
       line["path_tier"] = path_tier(dev, max(3, args.steps // 2))
       if not args.no_learned:
@@ -460,6 +469,31 @@ def run(args) -> None:
     print(json.dumps(line))
   if world_size > 1:
     dist.destroy_process_group()
+
+
+def rt_fp32_roofline(args, dev, npix: int, render_ms: float, count_worlds: int = 256) -> dict:
+  """FP32 roofline of the real-time kernel: one frame of the same scene with count_worlds worlds
+  rendered by the counting build (mujoco_warp_pbr_gb300/roofline.py), its operation counts per
+  pixel scaled to the timed frame, over the product kernel's render time."""
+  import copy
+
+  import torch
+
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import roofline
+  from mujoco_warp_pbr_gb300 import synthetic
+
+  small = copy.copy(args)
+  small.nworld = min(args.nworld, count_worlds)
+  sc = make_scene(small)
+  m = mjpbr.put_model(sc.mjm, device=dev)
+  d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld, device=dev)
+  rc = mjpbr.create_render_context(sc.mjm, sc.nworld, data=sc.mjd, device=dev, **sc.options)
+  synthetic.apply_per_world(sc, m, rc)
+  scene = mjpbr.scene_descriptor(m, d, rc)
+  counts = roofline.count_frame(scene, 1000, torch.cuda.current_stream(dev).cuda_stream)
+  counted = sc.nworld * sum(w * h for w, h in rc.base.cam_res)
+  return roofline.fp32_roofline(counts, counted, npix, render_ms)
 
 
 WEIGHTS = ROOT / "mujoco_warp_pbr_gb300" / "weights" / "kpcn_path.npz"

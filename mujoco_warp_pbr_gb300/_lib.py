@@ -361,6 +361,30 @@ def load() -> ctypes.CDLL:
   return _lib
 
 
+_count_lib: ctypes.CDLL | None = None
+
+
+def load_counting() -> ctypes.CDLL:
+  """The counting build (libmjpbr_count.so): the same entry points with the real-time render
+  kernels counting their ray queries, box / triangle / primitive tests and shading work into the
+  device array given to mjpbr_count_set. Benchmark instrumentation, not the render path."""
+  global _count_lib
+  with _lock:
+    if _count_lib is None:
+      path = LIBRARY.with_name("libmjpbr_count.so")
+      if not path.exists():
+        raise RuntimeError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+      lib = ctypes.CDLL(str(path))
+      for name, (restype, argtypes) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+      lib.mjpbr_count_set.restype = ctypes.c_int
+      lib.mjpbr_count_set.argtypes = [c_vp]
+      _count_lib = lib
+  return _count_lib
+
+
 def exported_symbols() -> list[str]:
   return list(_SIGNATURES)
 

@@ -22,6 +22,8 @@ CSRC = PACKAGE / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PACKAGE / "_build"
 LIBRARY = PACKAGE / "libmjpbr.so"
+# the render kernels with operation counters (benchmark instrumentation, not the product)
+COUNT_LIBRARY = PACKAGE / "libmjpbr_count.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -59,9 +61,9 @@ def _stale(obj: Path, src: Path, newest_header: float) -> bool:
   return src.stat().st_mtime > t or newest_header > t
 
 
-def _compile(nvcc: str, src: Path, obj: Path, verbose_ptxas: bool) -> tuple[Path, str]:
+def _compile(nvcc: str, src: Path, obj: Path, verbose_ptxas: bool, extra: tuple[str, ...] = ()) -> tuple[Path, str]:
   # MJPBR_NVCC_DEFINES: extra -D options (tuning builds, e.g. "MJPBR_RT_MIN_BLOCKS=3")
-  defines = [f"-D{d}" for d in os.environ.get("MJPBR_NVCC_DEFINES", "").split()]
+  defines = [f"-D{d}" for d in os.environ.get("MJPBR_NVCC_DEFINES", "").split()] + list(extra)
   cmd = [nvcc, *ARCH, *NVCC_FLAGS, *defines, "-c", str(src), "-o", str(obj)]
   if verbose_ptxas and src.suffix == ".cu":
     cmd += ["-Xptxas", "-v"]
@@ -78,20 +80,27 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
   newest_header = max((h.stat().st_mtime for h in _headers()), default=0.0)
   sources = _sources()
   objects = [BUILD / (src.name + ".o") for src in sources]
-  todo = [(s, o) for s, o in zip(sources, objects, strict=True) if force or _stale(o, s, newest_header)]
+  # the counting library: the same objects with the real-time render unit compiled with MJPBR_COUNT_OPS
+  count_src = CSRC / "render_rt.cu"
+  count_obj = BUILD / "render_rt.cu.count.o"
+  jobs_list = [(s, o, ()) for s, o in zip(sources, objects, strict=True) if force or _stale(o, s, newest_header)]
+  if force or _stale(count_obj, count_src, newest_header):
+    jobs_list.append((count_src, count_obj, ("-DMJPBR_COUNT_OPS",)))
   logs = []
-  if todo:
-    workers = jobs or min(len(todo), os.cpu_count() or 4)
+  if jobs_list:
+    workers = jobs or min(len(jobs_list), os.cpu_count() or 4)
     with concurrent.futures.ThreadPoolExecutor(workers) as pool:
-      for _obj, log in pool.map(lambda t: _compile(nvcc, t[0], t[1], verbose_ptxas), todo):
+      for _obj, log in pool.map(lambda t: _compile(nvcc, t[0], t[1], verbose_ptxas and not t[2], t[2]), jobs_list):
         logs.append(log)
-  if todo or not LIBRARY.exists():
-    tmp = LIBRARY.with_suffix(".so.tmp")
-    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objects)]
-    proc = subprocess.run(cmd, capture_output=True, text=True)
-    if proc.returncode != 0:
-      raise RuntimeError(f"linking libmjpbr.so failed:\n{proc.stdout}\n{proc.stderr}")
-    os.replace(tmp, LIBRARY)
+  count_objects = [count_obj if o.name == "render_rt.cu.o" else o for o in objects]
+  for lib, objs in ((LIBRARY, objects), (COUNT_LIBRARY, count_objects)):
+    if jobs_list or not lib.exists():
+      tmp = lib.with_suffix(".so.tmp")
+      cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+      proc = subprocess.run(cmd, capture_output=True, text=True)
+      if proc.returncode != 0:
+        raise RuntimeError(f"linking {lib.name} failed:\n{proc.stdout}\n{proc.stderr}")
+      os.replace(tmp, lib)
   if verbose_ptxas:
     sys.stdout.write("".join(logs))
   return LIBRARY

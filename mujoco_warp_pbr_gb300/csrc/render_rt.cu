@@ -68,6 +68,7 @@ struct Rt {
     const MjpbrSettings& st = c.s->settings;
     V3 l, ds, ss;
     float dist;
+    MJPBR_COUNT(kOpLight);
     eval_light(light, st.light_model, point, &l, &dist, &ds, &ss);
     float nol = dot(normal, l);
     if (nol <= 0.0f || (length_sq(ds) == 0.0f && length_sq(ss) == 0.0f)) return v3(0.0f);
@@ -87,9 +88,11 @@ struct Rt {
     const MjpbrScene& s = *c.s;
     const MjpbrSettings& st = s.settings;
     float nov = fmaxf(fdot(normal, view), 1.0e-4f);
+    MJPBR_COUNT(kOpShade);
     Lobes lb = shading_lobes(s.dfg_lut, s.dfg_size, sf, nov);
     V3 irradiance = c.ambient, prefiltered = c.ambient;
     if (kTex && st.has_env) {
+      MJPBR_COUNT(kOpEnv);
       irradiance = c.ambient + eval_sh9(s.env_sh + c.env * 27, rotate_yaw(normal, -c.env_yaw)) * c.env_scale;
       V3 r = view - normal * (2.0f * fdot(view, normal));
       float a2 = lb.alpha * lb.alpha;
@@ -132,6 +135,7 @@ struct Rt {
   static MJ_DEV V3 background(RtCtx& c, V3 d, float spread) {
     const MjpbrScene& s = *c.s;
     if (kTex && s.settings.env_background) {
+      MJPBR_COUNT(kOpBackground);
       float lod = log2f(fmaxf(spread * s.settings.inv_texel_angle, kMinTexels));
       return sample_radiance(s.env_radiance[c.env], s.env_data, d, c.env_yaw, lod) * c.env_scale;
     }
@@ -514,3 +518,10 @@ int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
 }
 
 }  // namespace mjpbr
+
+#ifdef MJPBR_COUNT_OPS
+// Counting build only: the device array (kOpCountN x kOpCopies uint64) the kernels add to, or NULL.
+extern "C" int mjpbr_count_set(void* counts) {
+  return cudaMemcpyToSymbol(mjpbr::g_op_counts, &counts, sizeof(counts)) == cudaSuccess ? 0 : 1;
+}
+#endif

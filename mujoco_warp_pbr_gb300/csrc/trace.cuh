@@ -12,6 +12,7 @@
 #pragma once
 
 #include "geometry.cuh"
+#include "opcount.cuh"
 
 namespace mjpbr {
 
@@ -56,6 +57,8 @@ MJ_DEV void push(const Stack& st, int& sp, int32_t code, float t, int32_t* err) 
 MJ_DEV void expand(const Stack& st, int& sp, const RayInv& ri, float4 alo, float4 ahi, float4 blo, float4 bhi, float cut,
                    int32_t* err) {
   const int32_t acnt = __float_as_int(ahi.w), bcnt = __float_as_int(bhi.w);
+  if (acnt >= 0) MJPBR_COUNT(kOpBox);
+  if (bcnt >= 0) MJPBR_COUNT(kOpBox);
   const float ta = acnt >= 0 ? box_entry(ri, alo.x, alo.y, alo.z, ahi.x, ahi.y, ahi.z, cut) : -1.0f;
   const float tb = bcnt >= 0 ? box_entry(ri, blo.x, blo.y, blo.z, bhi.x, bhi.y, bhi.z, cut) : -1.0f;
   const int32_t ca = (__float_as_int(alo.w) << 3) | acnt;
@@ -97,6 +100,7 @@ MJ_DEV float mesh_query(const MjpbrScene& sc, const Stack& st, int sp0, int32_t 
       const float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
       const V3 v0{a.x, a.y, a.z}, v1{b.x, b.y, b.z}, v2{c.x, c.y, c.z};
       float u, v;
+      MJPBR_COUNT(kOpTri);
       const float t = woop_hit(w, v0, v1, v2, best, &u, &v);
       if (t < 0.0f) continue;
       if (any) return t;
@@ -126,21 +130,27 @@ MJ_DEV float intersect_geom(const MjpbrScene& sc, const Stack& st, int sp, const
   float d = -1.0f;
   switch (type) {
     case MJPBR_GEOM_PLANE:
+      MJPBR_COUNT(kOpPlane);
       d = ray_plane(f, r, n);
       break;
     case MJPBR_GEOM_SPHERE:
+      MJPBR_COUNT(kOpSphere);
       d = ray_sphere(f, r, n);
       break;
     case MJPBR_GEOM_ELLIPSOID:
+      MJPBR_COUNT(kOpEllipsoid);
       d = ray_ellipsoid(f, r, n);
       break;
     case MJPBR_GEOM_CAPSULE:
+      MJPBR_COUNT(kOpCapsule);
       d = ray_capsule(f, r, n);
       break;
     case MJPBR_GEOM_CYLINDER:
+      MJPBR_COUNT(kOpCylinder);
       d = ray_cylinder(f, r, n);
       break;
     case MJPBR_GEOM_BOX:
+      MJPBR_COUNT(kOpBoxPrim);
       d = ray_box(f, r, n);
       break;
     default:
@@ -174,6 +184,11 @@ __device__ __noinline__ Hit trace_ray(const MjpbrScene& sc, const Stack& st, con
   h.v = 0.0f;
   h.face = -1;
   h.mesh = -1;
+  if (any) {
+    MJPBR_COUNT(kOpRayAny);
+  } else {
+    MJPBR_COUNT(kOpRayClosest);
+  }
   const RayInv ri = make_inv(r);
   int sp = 0;
   push(st, sp, 0, 0.0f, err);
