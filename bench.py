@@ -203,12 +203,24 @@ def path_tier(dev, steps: int, nworld: int = 1024, res: int = 128, spp: int = 2)
   assert mjpbr.check_errors(rc) == 0
   npix = sc.nworld * res * res
   avg = sum(ms) / len(ms)
+  # algorithmic work: a 256-world frame of the same scene through the counting build
+  from mujoco_warp_pbr_gb300 import roofline
+
+  small = synthetic.path_scene(seed=0, nworld=min(nworld, 256), res=res, spp=spp)
+  ms_ = mjpbr.put_model(small.mjm, device=dev)
+  ds_ = mjpbr.put_data(small.mjm, small.mjd, nworld=small.nworld, device=dev)
+  rcs = mjpbr.create_render_context(small.mjm, small.nworld, data=small.mjd, device=dev, **small.options)
+  synthetic.apply_per_world(small, ms_, rcs)
+  counts = roofline.count_frame(mjpbr.scene_descriptor(ms_, ds_, rcs), 100, stream.cuda_stream)
+  fp32 = roofline.fp32_roofline(counts, small.nworld * res * res, npix, avg, kernel="pt_kernel")
   return {
     "workload": sc.name,
     "value": npix / (avg / 1000.0) / 1e6,
     "unit": UNIT,
     "samples_per_s": npix * spp / (avg / 1000.0),
+    "rays_per_s": fp32["rays_per_px"] * npix / (avg / 1000.0),
     "ms_per_step": avg,
+    "roofline_fp32": fp32,
     "config": {"nworld": nworld, "cam_res": [res, res], "spp": spp, "max_depth": 4, "rr_depth": 2, "emissive_quads": 3},
   }
 

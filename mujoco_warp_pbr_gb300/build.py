@@ -80,19 +80,20 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
   newest_header = max((h.stat().st_mtime for h in _headers()), default=0.0)
   sources = _sources()
   objects = [BUILD / (src.name + ".o") for src in sources]
-  # the counting library: the same objects with the real-time render unit compiled with MJPBR_COUNT_OPS
-  count_src = CSRC / "render_rt.cu"
-  count_obj = BUILD / "render_rt.cu.count.o"
+  # the counting library: the same objects with the render units compiled with MJPBR_COUNT_OPS
+  counted = {"render_rt.cu", "pathtrace.cu"}
+  count_objs = {name: BUILD / (name + ".count.o") for name in counted}
   jobs_list = [(s, o, ()) for s, o in zip(sources, objects, strict=True) if force or _stale(o, s, newest_header)]
-  if force or _stale(count_obj, count_src, newest_header):
-    jobs_list.append((count_src, count_obj, ("-DMJPBR_COUNT_OPS",)))
+  for name, obj in count_objs.items():
+    if force or _stale(obj, CSRC / name, newest_header):
+      jobs_list.append((CSRC / name, obj, ("-DMJPBR_COUNT_OPS",)))
   logs = []
   if jobs_list:
     workers = jobs or min(len(jobs_list), os.cpu_count() or 4)
     with concurrent.futures.ThreadPoolExecutor(workers) as pool:
       for _obj, log in pool.map(lambda t: _compile(nvcc, t[0], t[1], verbose_ptxas and not t[2], t[2]), jobs_list):
         logs.append(log)
-  count_objects = [count_obj if o.name == "render_rt.cu.o" else o for o in objects]
+  count_objects = [count_objs.get(o.name[: -len(".o")], o) for o in objects]
   for lib, objs in ((LIBRARY, objects), (COUNT_LIBRARY, count_objects)):
     if jobs_list or not lib.exists():
       tmp = lib.with_suffix(".so.tmp")

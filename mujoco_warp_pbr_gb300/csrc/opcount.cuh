@@ -23,6 +23,9 @@ enum OpCount : int32_t {
   kOpLight,
   kOpEnv,
   kOpBackground,
+  kOpPtVertex,     // path tracer: surface vertex (surface, lobes, BSDF sample, pdf and value)
+  kOpPtLight,      // path tracer: next-event estimation of one light
+  kOpPtEnvSample,  // path tracer: environment importance sample (CDF searches, BSDF, MIS weight)
   kOpCountN
 };
 
@@ -30,7 +33,8 @@ enum OpCount : int32_t {
 constexpr int32_t kOpCopies = 32;
 
 #ifdef MJPBR_COUNT_OPS
-__device__ unsigned long long* g_op_counts;
+// one copy per translation unit (no relocatable device code): mjpbr_count_set sets every unit's
+static __device__ unsigned long long* g_op_counts;
 #define MJPBR_COUNT(k) \
   do { \
     if (g_op_counts) atomicAdd(g_op_counts + (k) * kOpCopies + (blockIdx.x & (kOpCopies - 1)), 1ull); \

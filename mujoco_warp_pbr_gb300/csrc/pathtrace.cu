@@ -57,6 +57,7 @@ struct Pt {
 
   static __device__ __noinline__ V3 environment(const RtCtx& c, V3 d) {
     const MjpbrScene& s = *c.s;
+    MJPBR_COUNT(kOpBackground);
     return sample_radiance(s.env_radiance[c.env], s.env_data, d, c.env_yaw, 0.0f) * c.env_scale;
   }
 
@@ -88,6 +89,7 @@ struct Pt {
     }
     V3 l, ds, ss;
     float dist;
+    MJPBR_COUNT(kOpPtLight);
     eval_light(light, st.light_model, point, &l, &dist, &ds, &ss);
     V3 ll{dot(l, t1), dot(l, t2), dot(l, normal)};
     if (ll.z <= 0.0f || (length_sq(ds) == 0.0f && length_sq(ss) == 0.0f)) return v3(0.0f);
@@ -129,6 +131,7 @@ struct Pt {
     }
     const V3 point = ps.o + ps.d * hit.dist;
     V3 normal;
+    MJPBR_COUNT(kOpPtVertex);
     Surface sf = eval_surface<kMesh, kTex>(s, c.blk, c.L, c.w, hit, hit.slot, point, ps.d, 0.0f, &normal);
     if (st.has_transparency) {
       if (pt_rand(seed, ps.sample, ps.depth + ps.passes, 0) >= sf.alpha && ps.passes < 4 * st.max_layers) {
@@ -189,6 +192,7 @@ struct Pt {
 
     if (kTex && st.has_env) {
       float pdf_env;
+      MJPBR_COUNT(kOpPtEnvSample);
       const int32_t h = s.cdf_height, w = s.cdf_width;
       V3 d_env = env_sample_direction(s.env_marginal + (int64_t)c.env * (h + 1), s.env_conditional + (int64_t)c.env * h * (w + 1),
                                       s.env_prob + (int64_t)c.env * h * w, h, w, c.env_yaw,
@@ -452,3 +456,10 @@ int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
 }
 
 }  // namespace mjpbr
+
+#ifdef MJPBR_COUNT_OPS
+namespace mjpbr {
+// Counting build only: this unit's copy of the counter array pointer (set by mjpbr_count_set).
+int pt_count_set(void* counts) { return cudaMemcpyToSymbol(g_op_counts, &counts, sizeof(counts)) == cudaSuccess ? 0 : 1; }
+}  // namespace mjpbr
+#endif

@@ -520,8 +520,14 @@ int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
 }  // namespace mjpbr
 
 #ifdef MJPBR_COUNT_OPS
-// Counting build only: the device array (kOpCountN x kOpCopies uint64) the kernels add to, or NULL.
+namespace mjpbr {
+int pt_count_set(void* counts);
+}
+
+// Counting build only: the device array (kOpCountN x kOpCopies uint64) the real-time and path
+// kernels add to, or NULL.
 extern "C" int mjpbr_count_set(void* counts) {
-  return cudaMemcpyToSymbol(mjpbr::g_op_counts, &counts, sizeof(counts)) == cudaSuccess ? 0 : 1;
+  if (cudaMemcpyToSymbol(mjpbr::g_op_counts, &counts, sizeof(counts)) != cudaSuccess) return 1;
+  return mjpbr::pt_count_set(counts);
 }
 #endif

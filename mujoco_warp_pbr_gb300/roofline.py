@@ -1,10 +1,11 @@
-"""FP32 roofline of the real-time tier: the algorithmic work of a frame from operation counts.
+"""FP32 roofline of the render kernels: the algorithmic work of a frame from operation counts.
 
 The real-time kernel is not HBM-bound (its compulsory traffic is ~16-28 B per pixel plus the
 scene), so its roofline is FP32 issue. The counting build of the render kernels
 (libmjpbr_count.so, `_lib.load_counting`) counts per frame: ray queries (closest / any hit),
 bounding-box tests, triangle tests, primitive tests by type, shaded surface hits, light
-evaluations, environment lookups (SH9 irradiance + prefiltered specular) and background lookups.
+evaluations, environment lookups (SH9 irradiance + prefiltered specular) and background lookups,
+and for the path tracer its surface vertices, light samples and environment samples.
 FLOPS_PER_OP turns the counts into algorithmic FP32 operations (an FMA counts 2, a min / max /
 compare 1, a reciprocal / square root / transcendental 4); the constants are a fixed model of the
 kernels' arithmetic, stated here and not measured. The achieved rate is that work over the
@@ -19,7 +20,7 @@ import ctypes
 # counter order of csrc/opcount.cuh (enum OpCount)
 OPS = (
   "ray_closest", "ray_any", "box", "triangle", "plane", "sphere", "ellipsoid", "capsule", "cylinder", "box_prim", "shade", "light",
-  "env", "background",
+  "env", "background", "pt_vertex", "pt_light", "pt_env_sample",
 )
 COPIES = 32
 
@@ -38,6 +39,9 @@ FLOPS_PER_OP = {
   "light": 90,  # light vector / attenuation / spot cone, GGX D, Smith V, Schlick F, sums
   "env": 220,  # SH9 irradiance (27 FMA), dominant direction, two equirect lookups (atan2, acos, trilinear)
   "background": 60,  # equirect lookup of the radiance mips
+  "pt_vertex": 350,  # path vertex: surface, lobes, tangent frame, BSDF sample, pdf and value, throughput
+  "pt_light": 200,  # next-event estimation of a light: sampling the bulb, light terms, two BSDF values
+  "pt_env_sample": 200,  # environment importance sample: two CDF searches, direction, BSDF, pdfs, MIS weight
 }
 
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -77,7 +81,7 @@ def count_frame(scene: ctypes.Structure, seed: int, stream: int) -> dict[str, in
   return counts_from_device(buf.cpu().tolist())
 
 
-def fp32_roofline(counts: dict[str, int], pixels_counted: int, pixels_frame: int, frame_ms: float) -> dict:
+def fp32_roofline(counts: dict[str, int], pixels_counted: int, pixels_frame: int, frame_ms: float, kernel: str = "rt_kernel") -> dict:
   """The roofline object of a frame of pixels_frame pixels rendered in frame_ms, from the counts
   of a frame of pixels_counted pixels of the same scene."""
   scale = pixels_frame / pixels_counted
@@ -85,7 +89,7 @@ def fp32_roofline(counts: dict[str, int], pixels_counted: int, pixels_frame: int
   achieved = frame_flops / (frame_ms * 1e-3) / 1e12
   return {
     "bound": "fp32",
-    "kernel": "rt_kernel",
+    "kernel": kernel,
     "achieved": achieved,
     "peak": FP32_PEAK_TFLOPS,
     "unit": "TFLOP/s",
