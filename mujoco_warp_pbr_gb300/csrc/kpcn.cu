@@ -72,7 +72,7 @@ __global__ void accumulate_f64_kernel(const float* __restrict__ src, double* __r
   if (i < n) acc[i] += (double)src[i];
 }
 
-__global__ void avgpool2_kernel(const uint16_t* __restrict__ in, uint16_t* __restrict__ out, int32_t nimg, int32_t h, int32_t w,
+__global__ void avgpool2_scalar_kernel(const uint16_t* __restrict__ in, uint16_t* __restrict__ out, int32_t nimg, int32_t h, int32_t w,
                                 int32_t ch) {
   const int32_t h2 = h / 2, w2 = w / 2;
   const int64_t total = (int64_t)nimg * h2 * w2 * ch;
@@ -86,6 +86,31 @@ __global__ void avgpool2_kernel(const uint16_t* __restrict__ in, uint16_t* __res
   const float v = bf16_value(in[base]) + bf16_value(in[base + ch]) + bf16_value(in[base + (int64_t)w * ch]) +
                   bf16_value(in[base + (int64_t)w * ch + ch]);
   out[i] = bf16_bits(0.25f * v);
+}
+
+// One thread per 8 channels (16 bytes) of an output pixel: the same sums as the scalar kernel
+// ((0,0) + (0,1) + (1,0) + (1,1) in FP32, times 1/4, rounded to BF16), 16-byte loads and stores.
+__global__ void avgpool2_kernel(const uint4* __restrict__ in, uint4* __restrict__ out, int32_t nimg, int32_t h, int32_t w, int32_t c8) {
+  const int32_t h2 = h / 2, w2 = w / 2;
+  const int64_t total = (int64_t)nimg * h2 * w2 * c8;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int32_t g = (int32_t)(i % c8);
+  const int64_t pix = i / c8;
+  const int32_t x = (int32_t)(pix % w2), y = (int32_t)((pix / w2) % h2);
+  const int64_t n = pix / ((int64_t)w2 * h2);
+  const int64_t base = ((n * h + 2 * y) * w + 2 * x) * c8 + g;
+  const uint4 a = __ldg(in + base), b = __ldg(in + base + c8), c = __ldg(in + base + (int64_t)w * c8), d = __ldg(in + base + (int64_t)w * c8 + c8);
+  const uint32_t av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w}, cv[4] = {c.x, c.y, c.z, c.w}, dv[4] = {d.x, d.y, d.z, d.w};
+  uint32_t o[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float lo = __uint_as_float(av[k] << 16) + __uint_as_float(bv[k] << 16) + __uint_as_float(cv[k] << 16) + __uint_as_float(dv[k] << 16);
+    const float hi = __uint_as_float(av[k] & 0xFFFF0000u) + __uint_as_float(bv[k] & 0xFFFF0000u) + __uint_as_float(cv[k] & 0xFFFF0000u) +
+                     __uint_as_float(dv[k] & 0xFFFF0000u);
+    o[k] = (uint32_t)bf16_bits(0.25f * lo) | ((uint32_t)bf16_bits(0.25f * hi) << 16);
+  }
+  out[i] = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
 // One thread per 16-byte group of 8 channels of an output pixel.
@@ -112,24 +137,41 @@ __global__ void apply_kernel(const float* __restrict__ logits, const float4* __r
   if (i >= total) return;
   const int32_t x = (int32_t)(i % w), y = (int32_t)((i / w) % h);
   const int64_t base = i - ((int64_t)y * w + x);
-  const float* lg = logits + i * kLogits;
-  float mx = lg[0];
-  for (int k = 1; k < kTaps; ++k) mx = fmaxf(mx, lg[k]);
-  float e[kTaps], sum = 0.0f;
+  // the pixel's 32 logits as 16-byte loads (25 used)
+  const float4* lg4 = reinterpret_cast<const float4*>(logits + i * kLogits);
+  float e[28];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    const float4 v = __ldg(lg4 + q);
+    e[4 * q] = v.x;
+    e[4 * q + 1] = v.y;
+    e[4 * q + 2] = v.z;
+    e[4 * q + 3] = v.w;
+  }
+  float mx = e[0];
+#pragma unroll
+  for (int k = 1; k < kTaps; ++k) mx = fmaxf(mx, e[k]);
+  float sum = 0.0f;
+#pragma unroll
   for (int k = 0; k < kTaps; ++k) {
-    e[k] = __expf(lg[k] - mx);
+    e[k] = __expf(e[k] - mx);
     sum += e[k];
   }
   const float inv = 1.0f / sum;
   float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-  for (int k = 0; k < kTaps; ++k) {
-    const float wk = e[k] * inv;
-    if (weights) weights[i * kTaps + k] = wk;
-    const int32_t yy = clampi(y + k / kKernel - 2, 0, h - 1), xx = clampi(x + k % kKernel - 2, 0, w - 1);
-    const float4 r = radiance[base + (int64_t)yy * w + xx];
-    acc.x += wk * r.x;
-    acc.y += wk * r.y;
-    acc.z += wk * r.z;
+#pragma unroll
+  for (int dy = 0; dy < kKernel; ++dy) {
+    const int64_t row = base + (int64_t)clampi(y + dy - 2, 0, h - 1) * w;
+#pragma unroll
+    for (int dx = 0; dx < kKernel; ++dx) {
+      const int k = dy * kKernel + dx;
+      const float wk = e[k] * inv;
+      if (weights) weights[i * kTaps + k] = wk;
+      const float4 r = __ldg(radiance + row + clampi(x + dx - 2, 0, w - 1));
+      acc.x += wk * r.x;
+      acc.y += wk * r.y;
+      acc.z += wk * r.z;
+    }
   }
   out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
@@ -341,9 +383,14 @@ int upsample2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h,
 
 int avgpool2_launch(const uint16_t* in, uint16_t* out, int32_t nimg, int32_t h, int32_t w, int32_t c, cudaStream_t st) {
   if (!in || !out || h % 2 || w % 2 || c < 1) return set_error(MJPBR_ERR_ARG, "avgpool2: bad arguments");
+  if (c % 8 == 0 && !((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u)) {
+    const int64_t n = (int64_t)nimg * (h / 2) * (w / 2) * (c / 8);
+    avgpool2_kernel<<<blocks(n, 256), 256, 0, st>>>(reinterpret_cast<const uint4*>(in), reinterpret_cast<uint4*>(out), nimg, h, w, c / 8);
+    return check_launch("avgpool2_kernel");
+  }
   const int64_t n = (int64_t)nimg * (h / 2) * (w / 2) * c;
-  avgpool2_kernel<<<blocks(n, 256), 256, 0, st>>>(in, out, nimg, h, w, c);
-  return check_launch("avgpool2_kernel");
+  avgpool2_scalar_kernel<<<blocks(n, 256), 256, 0, st>>>(in, out, nimg, h, w, c);
+  return check_launch("avgpool2_scalar_kernel");
 }
 
 int kpcn_apply_launch(const float* logits, const float* radiance, float* weights, float* out, int32_t nimg, int32_t h, int32_t w,

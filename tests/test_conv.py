@@ -187,3 +187,21 @@ def test_upsample2_is_nearest():
   torch.cuda.synchronize()
   ref = x.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2)
   assert torch.equal(out.cpu().view(torch.int16), ref.view(torch.int16))
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("c", [24, 12])
+def test_avgpool2_rounds_the_fp32_mean(c):
+  """16-byte path (channels a multiple of 8) and the scalar path: bit-exact against the same sums."""
+  from mujoco_warp_pbr_gb300 import _lib
+
+  g = torch.Generator().manual_seed(c)
+  x = torch.randn((3, 6, 10, c), generator=g).to(torch.bfloat16)
+  out = torch.zeros((3, 3, 5, c), dtype=torch.bfloat16, device="cuda")
+  xd = x.cuda()
+  _lib.call("mjpbr_avgpool2_bf16", xd.data_ptr(), out.data_ptr(), 3, 6, 10, c, torch.cuda.current_stream().cuda_stream)
+  torch.cuda.synchronize()
+  f = x.float()
+  ref = ((f[:, 0::2, 0::2] + f[:, 0::2, 1::2] + f[:, 1::2, 0::2] + f[:, 1::2, 1::2]) * 0.25).to(torch.bfloat16)
+  assert torch.equal(out.cpu().view(torch.int16), ref.view(torch.int16))
