@@ -295,6 +295,52 @@ def geom_aabbs(mjm: Any, xpos: np.ndarray, xmat: np.ndarray, mesh_bounds: np.nda
   return lo, hi
 
 
+def geom_aabbs_all(mjm: Any, xpos: np.ndarray, xmat: np.ndarray, mesh_bounds: np.ndarray | None) -> tuple[np.ndarray, np.ndarray]:
+  """geom_aabbs for every world at once: xpos (nworld, ngeom, 3), xmat (nworld, ngeom, 9) ->
+  lo, hi (nworld, ngeom, 3), the same formulas vectorised over worlds and the geoms of a type."""
+  xpos = np.asarray(xpos, np.float64)
+  R_all = np.asarray(xmat, np.float64).reshape(xpos.shape[0], xpos.shape[1], 3, 3)
+  types = np.asarray(mjm.geom_type).reshape(-1)
+  size = np.asarray(mjm.geom_size, np.float64).reshape(-1, 3)
+  c = xpos.copy()
+  e = np.zeros_like(xpos)
+
+  def pick(sel):
+    R = R_all[:, sel]  # (nworld, n, 3, 3)
+    return R, np.abs(R), size[sel][None]  # s: (1, n, 3)
+
+  sel = types == GEOM_SPHERE
+  e[:, sel] = size[sel, 0][None, :, None]
+  sel = types == GEOM_CAPSULE
+  R, A, sz = pick(sel)
+  e[:, sel] = A[..., 2] * sz[..., 1:2] + sz[..., 0:1]
+  sel = types == GEOM_ELLIPSOID
+  R, A, sz = pick(sel)
+  e[:, sel] = np.sqrt(((R * sz[:, :, None, :]) ** 2).sum(-1))
+  sel = types == GEOM_CYLINDER
+  R, A, sz = pick(sel)
+  e[:, sel] = A[..., 2] * sz[..., 1:2] + sz[..., 0:1] * np.sqrt(np.maximum(0.0, 1.0 - R[..., 2] ** 2))
+  sel = types == GEOM_BOX
+  R, A, sz = pick(sel)
+  e[:, sel] = (A * sz[:, :, None, :]).sum(-1)
+  sel = types == GEOM_PLANE
+  R, A, sz = pick(sel)
+  sx = np.where(sz[..., 0:1] > 0, sz[..., 0:1], 1e6)
+  sy = np.where(sz[..., 1:2] > 0, sz[..., 1:2], 1e6)
+  e[:, sel] = A[..., 0] * sx + A[..., 1] * sy
+  if mesh_bounds is not None:
+    dataid = np.asarray(mjm.geom_dataid).reshape(-1)
+    sel = np.isin(types, [GEOM_MESH, GEOM_SDF]) & (dataid >= 0)
+    if np.any(sel):
+      R, A, _ = pick(sel)
+      mb = np.asarray(mesh_bounds, np.float64)[dataid[sel]]
+      lc = 0.5 * (mb[:, :3] + mb[:, 3:])
+      half = 0.5 * (mb[:, 3:] - mb[:, :3])
+      e[:, sel] = (A * half[None, :, None, :]).sum(-1)
+      c[:, sel] = c[:, sel] + (R * lc[None, :, None, :]).sum(-1)
+  return c - e, c + e
+
+
 def build_scene_topology(lo: np.ndarray, hi: np.ndarray) -> np.ndarray:
   """(nnode, 2) child refs of an SAH tree over the boxes (libmjpbr's host builder)."""
   lib = _lib.load()
@@ -649,9 +695,10 @@ def prepare_context(
     lo, hi = geom_aabbs(mjm, xpos, xmat, meshes.get("mesh_bounds"))
     topo = build_scene_topology(lo[enabled], hi[enabled])[None]
   else:
-    topo = np.stack(
-      [build_scene_topology(*(b[enabled] for b in geom_aabbs(mjm, *world_arrays(w), meshes.get("mesh_bounds")))) for w in range(nworld)]
-    )
+    xpos_all = np.asarray(host_data.geom_xpos, np.float64)
+    xmat_all = np.asarray(host_data.geom_xmat, np.float64).reshape(xpos_all.shape[0], ngeom, 9)
+    lo_all, hi_all = geom_aabbs_all(mjm, xpos_all[:nworld], xmat_all[:nworld], meshes.get("mesh_bounds"))
+    topo = np.stack([build_scene_topology(lo_all[w][enabled], hi_all[w][enabled]) for w in range(nworld)])
   nbvh = len(enabled)
   nnode = topo.shape[1]
   lib = _lib.load()
