@@ -293,6 +293,58 @@ __global__ void split_concat_grad_kernel(const float* __restrict__ dcat, const u
   }
 }
 
+__device__ __forceinline__ uint32_t relu_masked_bf16x2(float a, float b, uint32_t act2) {
+  // a BF16 activation is > 0 when its sign bit is clear and it is not zero
+  const uint32_t lo = (act2 & 0x8000u) || !(act2 & 0x7FFFu) ? 0u : (uint32_t)bf16_bits(a);
+  const uint32_t hi = (act2 & 0x80000000u) || !(act2 & 0x7FFF0000u) ? 0u : (uint32_t)bf16_bits(b);
+  return lo | (hi << 16);
+}
+
+// 4 channels per thread (the 16-byte form of split_concat_grad_kernel; same sums and masks).
+__global__ void split_concat_grad4_kernel(const float4* __restrict__ dcat, const uint2* __restrict__ low, float4* __restrict__ dskip,
+                                          uint2* __restrict__ dlow, int32_t nimg, int32_t h, int32_t w, int32_t c1q, int32_t c2q) {
+  const int32_t ctq = c1q + c2q;
+  const int32_t h2 = h / 2, w2 = w / 2;
+  const int64_t nskip = (int64_t)nimg * h * w * c1q;
+  const int64_t nlow = (int64_t)nimg * h2 * w2 * c2q;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nskip) {
+    const int64_t pix = i / c1q;
+    dskip[i] = __ldg(dcat + pix * ctq + (i - pix * c1q));
+  }
+  if (i < nlow) {
+    const int32_t q = (int32_t)(i % c2q);
+    const int64_t pix = i / c2q;
+    const int32_t x = (int32_t)(pix % w2), y = (int32_t)((pix / w2) % h2);
+    const int64_t n = pix / ((int64_t)w2 * h2);
+    const int64_t b = ((n * h + 2 * y) * w + 2 * x) * ctq + c1q + q;
+    const float4 a = __ldg(dcat + b), bb = __ldg(dcat + b + ctq), c = __ldg(dcat + b + (int64_t)w * ctq), d = __ldg(dcat + b + (int64_t)w * ctq + ctq);
+    const uint2 lw = __ldg(low + i);
+    dlow[i] = make_uint2(relu_masked_bf16x2(a.x + bb.x + c.x + d.x, a.y + bb.y + c.y + d.y, lw.x),
+                         relu_masked_bf16x2(a.z + bb.z + c.z + d.z, a.w + bb.w + c.w + d.w, lw.y));
+  }
+}
+
+// 4 channels per thread (the 16-byte form of unpool_add_grad_kernel; same sums and masks).
+__global__ void unpool_add_grad4_kernel(const float4* __restrict__ dskip, const float4* __restrict__ dpool, const uint2* __restrict__ act,
+                                        uint2* __restrict__ dact, int32_t nimg, int32_t h, int32_t w, int32_t cq) {
+  const int64_t total = (int64_t)nimg * h * w * cq;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int32_t q = (int32_t)(i % cq);
+  const int64_t pix = i / cq;
+  const int32_t x = (int32_t)(pix % w), y = (int32_t)((pix / w) % h);
+  const int64_t n = pix / ((int64_t)w * h);
+  const float4 dp = __ldg(dpool + ((n * (h / 2) + y / 2) * (w / 2) + x / 2) * cq + q);
+  float4 v = make_float4(0.25f * dp.x, 0.25f * dp.y, 0.25f * dp.z, 0.25f * dp.w);
+  if (dskip) {
+    const float4 ds = __ldg(dskip + i);
+    v = make_float4(v.x + ds.x, v.y + ds.y, v.z + ds.z, v.w + ds.w);
+  }
+  const uint2 ac = __ldg(act + i);
+  dact[i] = make_uint2(relu_masked_bf16x2(v.x, v.y, ac.x), relu_masked_bf16x2(v.z, v.w, ac.y));
+}
+
 // Gradient of a skip activation s = (dskip + the 2 x 2 average-pool gradient of dpool) masked by
 // the ReLU of s, as BF16 (dskip may be NULL at the bottom level).
 __global__ void unpool_add_grad_kernel(const float* __restrict__ dskip, const float* __restrict__ dpool, const uint16_t* __restrict__ act,
@@ -432,6 +484,14 @@ int kpcn_apply_grad_launch(const float* grad, const float* weights, const float*
 int split_concat_grad_launch(const float* dcat, const uint16_t* low, float* dskip, uint16_t* dlow, int32_t nimg, int32_t h, int32_t w,
                              int32_t c1, int32_t c2, cudaStream_t st) {
   if (!dcat || !low || !dskip || !dlow || h % 2 || w % 2) return set_error(MJPBR_ERR_ARG, "split concat grad: bad arguments");
+  if (c1 % 4 == 0 && c2 % 4 == 0 && !((reinterpret_cast<uintptr_t>(dcat) | reinterpret_cast<uintptr_t>(dskip)) & 15u) &&
+      !((reinterpret_cast<uintptr_t>(low) | reinterpret_cast<uintptr_t>(dlow)) & 7u)) {
+    const int64_t n = std::max<int64_t>((int64_t)nimg * h * w * (c1 / 4), (int64_t)nimg * (h / 2) * (w / 2) * (c2 / 4));
+    split_concat_grad4_kernel<<<blocks(n, 256), 256, 0, st>>>(reinterpret_cast<const float4*>(dcat), reinterpret_cast<const uint2*>(low),
+                                                             reinterpret_cast<float4*>(dskip), reinterpret_cast<uint2*>(dlow), nimg, h, w, c1 / 4,
+                                                             c2 / 4);
+    return check_launch("split_concat_grad4_kernel");
+  }
   const int64_t n = std::max<int64_t>((int64_t)nimg * h * w * c1, (int64_t)nimg * (h / 2) * (w / 2) * c2);
   split_concat_grad_kernel<<<blocks(n, 256), 256, 0, st>>>(dcat, low, dskip, dlow, nimg, h, w, c1, c2);
   return check_launch("split_concat_grad_kernel");
@@ -440,6 +500,13 @@ int split_concat_grad_launch(const float* dcat, const uint16_t* low, float* dski
 int unpool_add_grad_launch(const float* dskip, const float* dpool, const uint16_t* act, uint16_t* dact, int32_t nimg, int32_t h,
                            int32_t w, int32_t c, cudaStream_t st) {
   if (!dpool || !act || !dact || h % 2 || w % 2) return set_error(MJPBR_ERR_ARG, "unpool add grad: bad arguments");
+  if (c % 4 == 0 && !((reinterpret_cast<uintptr_t>(dskip) | reinterpret_cast<uintptr_t>(dpool)) & 15u) &&
+      !((reinterpret_cast<uintptr_t>(act) | reinterpret_cast<uintptr_t>(dact)) & 7u)) {
+    const int64_t n = (int64_t)nimg * h * w * (c / 4);
+    unpool_add_grad4_kernel<<<blocks(n, 256), 256, 0, st>>>(reinterpret_cast<const float4*>(dskip), reinterpret_cast<const float4*>(dpool),
+                                                           reinterpret_cast<const uint2*>(act), reinterpret_cast<uint2*>(dact), nimg, h, w, c / 4);
+    return check_launch("unpool_add_grad4_kernel");
+  }
   const int64_t n = (int64_t)nimg * h * w * c;
   unpool_add_grad_kernel<<<blocks(n, 256), 256, 0, st>>>(dskip, dpool, act, dact, nimg, h, w, c);
   return check_launch("unpool_add_grad_kernel");
