@@ -57,6 +57,25 @@ PATH_METRIC = "Mpix/s (path-traced tier, 1 GB300)"
 UNIT = "Mpix/s"
 
 
+def max_over_ranks(value: float, device=None) -> float:
+  """The maximum of a per-rank value over the process group (the value itself without one):
+  every timed region is reported as its slowest rank."""
+  import torch
+  import torch.distributed as dist
+
+  if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+    return value
+  t = torch.tensor([value], dtype=torch.float64, device=device)
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t.item())
+
+
+def aggregate_rate(units_per_rank: float, ms: float, world_size: int) -> float:
+  """Whole-job throughput in millions of units per second: every rank processed units_per_rank
+  (replicas of the workload, weak scaling) in ms, the slowest rank's time."""
+  return units_per_rank * world_size / (ms / 1000.0) / 1e6
+
+
 def _peaks() -> dict:
   p = ROOT / "MEASURED_PEAKS.json"
   if p.exists():
@@ -391,12 +410,8 @@ def run(args) -> None:
     dist.barrier()
   step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends, strict=True)]
   render_ms = [s.elapsed_time(e) for s, e in zip(mids, ends, strict=True)]
-  total_ms = sum(step_ms)
-  if world_size > 1:
-    t = torch.tensor([total_ms], device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-  value = npix * args.steps * world_size / (total_ms / 1000.0) / 1e6
+  total_ms = max_over_ranks(sum(step_ms), dev)
+  value = aggregate_rate(npix * args.steps, total_ms, world_size)
   assert mjpbr.check_errors(rc) == 0
 
   # ---- end to end through the public API with host buffers
@@ -423,12 +438,8 @@ def run(args) -> None:
     out_host.copy_(rc.base.rgb_data, non_blocking=True)
   e1.record(stream)
   torch.cuda.synchronize()
-  e2e_ms = e0.elapsed_time(e1)
-  if world_size > 1:
-    t = torch.tensor([e2e_ms], device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_ms = float(t.item())
-  e2e_value = npix * e2e_steps * world_size / (e2e_ms / 1000.0) / 1e6
+  e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
+  e2e_value = aggregate_rate(npix * e2e_steps, e2e_ms, world_size)
 
   if rank == 0:
     peaks = _peaks()
@@ -644,12 +655,8 @@ def run_batched(args) -> None:
       graph.replay()
       ends[i].record(stream)
     torch.cuda.synchronize()
-  total_ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends, strict=True))
-  if world_size > 1:
-    t = torch.tensor([total_ms], device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-  value = npix * args.steps * world_size / (total_ms / 1000.0) / 1e6
+  total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(starts, ends, strict=True)), dev)
+  value = aggregate_rate(npix * args.steps, total_ms, world_size)
   # end to end: next poses from pinned host memory, the graph, the RGB back to pinned memory
   host_poses = poses.cpu().pin_memory()
   out_host = torch.empty(rc.base.rgb_data.shape, dtype=rc.base.rgb_data.dtype).pin_memory()
@@ -662,8 +669,8 @@ def run_batched(args) -> None:
     out_host.copy_(rc.base.rgb_data, non_blocking=True)
   e1.record(stream)
   torch.cuda.synchronize()
-  e2e_ms = e0.elapsed_time(e1)
-  e2e_value = npix * e2e_steps * world_size / (e2e_ms / 1000.0) / 1e6
+  e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
+  e2e_value = aggregate_rate(npix * e2e_steps, e2e_ms, world_size)
   assert mjpbr.check_errors(rc) == 0
   if rank == 0:
     peaks = _peaks()
