@@ -76,7 +76,8 @@ struct Pt {
   }
 
   // Next-event estimate of one punctual light (its bulb disc for soft shadows).
-  static MJ_DEV V3 light_sample(RtCtx& c, Light light, const Lobes& lb, V3 point, V3 normal, V3 t1, V3 t2, V3 v, float u0,
+  // out of line: one copy of the light-sampling code in the bounce loop (1 % faster measured)
+  static __device__ __noinline__ V3 light_sample(RtCtx& c, Light light, const Lobes& lb, V3 point, V3 normal, V3 t1, V3 t2, V3 v, float u0,
                                 float u1) {
     const MjpbrSettings& st = c.s->settings;
     if (light.type != MJPBR_LIGHT_DIRECTIONAL && light.bulbradius > 0.0f) {
