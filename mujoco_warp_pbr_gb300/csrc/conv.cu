@@ -14,6 +14,11 @@
 //
 // The U-Net's skip concatenation is read in place: channels past c_in come from in2, either at
 // the output resolution (in2_full) or at half of it, upsampled x2 (nearest) while staging.
+//
+// Weight gradients: conv3x3_wgrad_ws_kernel (persistent, warp-specialised, MN-major TMA operands,
+// three MMA-issuing warps) for full-resolution skips, else conv3x3_wgrad_kernel (one CTA per 128
+// rows of (tap, channel), register transposes into K-major operands); bias gradients by
+// bias_grad_kernel.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
