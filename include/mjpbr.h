@@ -198,7 +198,7 @@ typedef struct MjpbrScene {
 
   /* ---- Model (mujoco_warp.Model fields) ---- */
   const int32_t* geom_type;        /* (ngeom,) MjpbrGeomType */
-  mjpbr_i32b geom_dataid;          /* (*, ngeom) mesh id of mesh geoms */
+  mjpbr_i32b geom_dataid;          /* (*, ngeom) mesh id of mesh geoms, height-field id of height fields */
   mjpbr_i32b geom_matid;           /* (*, ngeom) */
   mjpbr_f32b geom_size;            /* (*, ngeom, 3) */
   mjpbr_f32b geom_rgba;            /* (*, ngeom, 4) */
@@ -280,16 +280,17 @@ typedef struct MjpbrScene {
   int32_t nnode;                   /* inner nodes per world (nbvh_geom - 1, at least 1) */
   const int32_t* enabled_geom_ids; /* (nbvh_geom,) slot -> geom id */
   mjpbr_i32b tlas_child;           /* (*, nnode, 2) child refs: >= 0 inner node, < 0 leaf slot ~ref */
-  const float* mesh_bounds;        /* (nmesh, 6) local AABB of each mesh (lower, upper) */
+  const float* mesh_bounds;        /* (nmesh + nhfield, 6) local AABB of each triangle BVH (lower, upper) */
   float* world_blocks;             /* (nworld, world_block_floats) written by mjpbr_refit_bvh */
   int32_t world_block_floats;      /* per-world block size in floats (a multiple of 4) */
-  int32_t pad1_;
+  int32_t nhfield;                 /* height fields; their triangle BVHs follow the meshes' */
 
-  /* ---- Mesh BVHs (one per mesh, shared by every world) ---- */
+  /* ---- Triangle BVHs, shared by every world: one per mesh (index = mesh id), then one per
+   *      height field (index = nmesh + height-field id, its grid triangulated as a closed prism) */
   const float* blas_nodes;         /* (nblasnode, 16) child-bounds nodes, see mjpbr_build_mesh_bvh */
   const float* blas_tris;          /* (nblastri, 12) v0, v1, v2 (xyz + face id bits in w of v0) */
-  const int32_t* blas_root;        /* (nmesh,) first node of each mesh */
-  const int32_t* blas_tri_base;    /* (nmesh,) first triangle of each mesh */
+  const int32_t* blas_root;        /* (nmesh + nhfield,) first node of each BVH */
+  const int32_t* blas_tri_base;    /* (nmesh + nhfield,) first triangle of each BVH */
 
   /* ---- Textures ---- */
   const MjpbrTexture* textures;    /* (ntex,) device copy */

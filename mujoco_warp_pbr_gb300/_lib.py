@@ -206,7 +206,7 @@ class Scene(ctypes.Structure):
     ("mesh_bounds", c_vp),
     ("world_blocks", c_vp),
     ("world_block_floats", c_i32),
-    ("pad1_", c_i32),
+    ("nhfield", c_i32),
     # mesh BVHs
     ("blas_nodes", c_vp),
     ("blas_tris", c_vp),

@@ -283,8 +283,8 @@ def geom_aabbs(mjm: Any, xpos: np.ndarray, xmat: np.ndarray, mesh_bounds: np.nda
       sx = s[0] if s[0] > 0 else 1e6
       sy = s[1] if s[1] > 0 else 1e6
       e = A[:, 0] * sx + A[:, 1] * sy
-    elif t in (GEOM_MESH, GEOM_SDF) and mesh_bounds is not None and int(mjm.geom_dataid[g]) >= 0:
-      mb = mesh_bounds[int(mjm.geom_dataid[g])]
+    elif (b := blas_index(t, int(mjm.geom_dataid[g]), mjm)) >= 0 and mesh_bounds is not None:
+      mb = mesh_bounds[b]
       lc = 0.5 * (mb[:3] + mb[3:])
       e = A @ (0.5 * (mb[3:] - mb[:3]))
       c = c + R @ lc
@@ -329,11 +329,11 @@ def geom_aabbs_all(mjm: Any, xpos: np.ndarray, xmat: np.ndarray, mesh_bounds: np
   sy = np.where(sz[..., 1:2] > 0, sz[..., 1:2], 1e6)
   e[:, sel] = A[..., 0] * sx + A[..., 1] * sy
   if mesh_bounds is not None:
-    dataid = np.asarray(mjm.geom_dataid).reshape(-1)
-    sel = np.isin(types, [GEOM_MESH, GEOM_SDF]) & (dataid >= 0)
+    blas = np.array([blas_index(int(t), int(d), mjm) for t, d in zip(types, np.asarray(mjm.geom_dataid).reshape(-1))], np.int64)
+    sel = blas >= 0
     if np.any(sel):
       R, A, _ = pick(sel)
-      mb = np.asarray(mesh_bounds, np.float64)[dataid[sel]]
+      mb = np.asarray(mesh_bounds, np.float64)[blas[sel]]
       lc = 0.5 * (mb[:, :3] + mb[:, 3:])
       half = 0.5 * (mb[:, 3:] - mb[:, :3])
       e[:, sel] = (A * half[None, :, None, :]).sum(-1)
@@ -354,19 +354,91 @@ def build_scene_topology(lo: np.ndarray, hi: np.ndarray) -> np.ndarray:
   return out
 
 
+def nhfield_of(mjm: Any) -> int:
+  """Height fields of a model (0 for models without the hfield_* fields)."""
+  nrow = getattr(mjm, "hfield_nrow", None)
+  return 0 if nrow is None else int(len(np.asarray(nrow).reshape(-1)))
+
+
+def blas_index(gtype: int, dataid: int, mjm: Any) -> int:
+  """Triangle BVH of a geom: its mesh's (index = mesh id), a height field's (index = nmesh +
+  height-field id, after every mesh), or -1 (the refit kernel's mapping)."""
+  if dataid < 0:
+    return -1
+  if gtype in (GEOM_MESH, GEOM_SDF) and dataid < mjm.nmesh:
+    return dataid
+  if gtype == GEOM_HFIELD and dataid < nhfield_of(mjm):
+    return mjm.nmesh + dataid
+  return -1
+
+
+def hfield_mesh(mjm: Any, h: int) -> tuple[np.ndarray, np.ndarray]:
+  """Height field h as a closed triangle mesh in the geom frame: (vertices (nv, 3) float32, faces
+  (nf, 3) int32), every face wound outwards.
+
+  MuJoCo's height-field solid: elevation samples on an nrow x ncol grid spanning
+  [-size0, size0] x [-size1, size1] (columns along x, rows along y), z = size2 * elevation, standing
+  on a base at z = -size3. Faces, in this order: the top (two triangles per grid cell: (r, c),
+  (r, c+1), (r+1, c+1) and (r, c), (r+1, c+1), (r+1, c), cells row by row); the four side walls (two
+  triangles per border segment: top p, base q, top q and top p, base p, base q, for consecutive
+  border samples p -> q walked counter-clockwise seen from +z, starting at sample (0, 0)); the base
+  (a fan from the centre (0, 0, -size3) over the same segments: centre, base q, base p). Coordinates are computed in float64 and rounded
+  once to float32: x = size0 (2 c / (ncol - 1) - 1), y = size1 (2 r / (nrow - 1) - 1). Replaces the
+  third-party height-field mesh of MuJoCo Warp that the reference traces (traverse.py:161-164)."""
+  nr, nc = int(mjm.hfield_nrow[h]), int(mjm.hfield_ncol[h])
+  if nr < 2 or nc < 2:
+    raise ValueError(f"height field {h}: nrow and ncol must be at least 2, got {nr} x {nc}")
+  size = np.asarray(mjm.hfield_size, np.float32).reshape(-1, 4)[h].astype(np.float64)
+  adr = int(mjm.hfield_adr[h])
+  elev = np.asarray(mjm.hfield_data, np.float32).reshape(-1)[adr : adr + nr * nc].reshape(nr, nc).astype(np.float64)
+  xs = size[0] * (2.0 * np.arange(nc) / (nc - 1) - 1.0)
+  ys = size[1] * (2.0 * np.arange(nr) / (nr - 1) - 1.0)
+  top = np.stack(np.broadcast_arrays(xs[None, :], ys[:, None], size[2] * elev), -1).reshape(-1, 3)
+  base = top.copy()
+  base[:, 2] = -size[3]
+  centre = np.array([[0.0, 0.0, -size[3]]])
+  vert = np.concatenate([top, base, centre]).astype(np.float32)
+  nb = nr * nc  # first base vertex
+  ic = 2 * nb  # the base centre
+
+  def tid(r: np.ndarray, c: np.ndarray) -> np.ndarray:
+    return r * nc + c
+
+  r, c = np.meshgrid(np.arange(nr - 1), np.arange(nc - 1), indexing="ij")
+  r, c = r.reshape(-1), c.reshape(-1)
+  a, b, d, e = tid(r, c), tid(r, c + 1), tid(r + 1, c + 1), tid(r + 1, c)
+  top_faces = np.stack([np.stack([a, b, d], -1), np.stack([a, d, e], -1)], 1).reshape(-1, 3)
+  # border samples counter-clockwise seen from +z: along row 0, up column nc-1, back along row
+  # nr-1, down column 0
+  ring_r = np.concatenate([np.zeros(nc - 1, int), np.arange(nr - 1), np.full(nc - 1, nr - 1), np.arange(nr - 1, 0, -1)])
+  ring_c = np.concatenate([np.arange(nc - 1), np.full(nr - 1, nc - 1), np.arange(nc - 1, 0, -1), np.zeros(nr - 1, int)])
+  p = tid(ring_r, ring_c)
+  q = np.roll(p, -1)
+  side = np.stack([np.stack([p, q + nb, q], -1), np.stack([p, p + nb, q + nb], -1)], 1).reshape(-1, 3)
+  bottom = np.stack([np.full_like(p, ic), q + nb, p + nb], -1)
+  face = np.concatenate([top_faces, side, bottom]).astype(np.int32)
+  return vert, face
+
+
 def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
-  """Per-mesh BVHs concatenated: nodes (nnode, 16), tris (ntri, 12), root / tri_base per mesh,
-  mesh AABBs (nmesh, 6)."""
+  """Triangle BVHs concatenated, one per mesh, then one per height field (hfield_mesh): nodes
+  (nnode, 16), tris (ntri, 12), root / tri_base per BVH, local AABBs (nmesh + nhfield, 6)."""
   lib = _lib.load()
   nodes, tris, roots, bases, bounds, nfaces = [], [], [], [], [], []
   node_total = tri_total = 0
   vert_all = np.asarray(mjm.mesh_vert, np.float32).reshape(-1, 3)
   face_all = np.asarray(mjm.mesh_face, np.int32).reshape(-1, 3)
+  sources = []
   for m in range(mjm.nmesh):
     v0, nv = int(mjm.mesh_vertadr[m]), int(mjm.mesh_vertnum[m])
     f0, nf = int(mjm.mesh_faceadr[m]), int(mjm.mesh_facenum[m])
-    vert = np.ascontiguousarray(vert_all[v0 : v0 + nv])
-    face = np.ascontiguousarray(face_all[f0 : f0 + nf])
+    sources.append((f"mesh {m}", vert_all[v0 : v0 + nv], face_all[f0 : f0 + nf]))
+  for h in range(nhfield_of(mjm)):
+    sources.append((f"height field {h}", *hfield_mesh(mjm, h)))
+  for name, vert, face in sources:
+    vert = np.ascontiguousarray(vert, np.float32)
+    face = np.ascontiguousarray(face, np.int32)
+    nv, nf = len(vert), len(face)
     cap = lib.mjpbr_bvh_node_count(nf)
     node_buf = np.zeros((cap, 16), np.float32)
     tri_buf = np.zeros((nf, 12), np.float32)
@@ -376,7 +448,7 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
       vert.ctypes.data, nv, face.ctypes.data, nf, 4, node_buf.ctypes.data, tri_buf.ctypes.data, bnd.ctypes.data, ctypes.byref(nnode)
     )
     if status != 0:
-      raise ValueError(f"mesh {m}: BVH build failed (status {status})")
+      raise ValueError(f"{name}: BVH build failed (status {status})")
     nodes.append(node_buf[: nnode.value])
     tris.append(tri_buf)
     roots.append(node_total)
@@ -391,7 +463,8 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
     "blas_root": np.array(roots, np.int32) if roots else None,
     "blas_tri_base": np.array(bases, np.int32) if bases else None,
     "mesh_bounds": np.stack(bounds).astype(np.float32) if bounds else None,
-    "mesh_nface": nfaces,
+    "mesh_nface": nfaces[: mjm.nmesh],
+    "nhfield": nhfield_of(mjm),
   }
 
 
@@ -676,13 +749,13 @@ def prepare_context(
     return xpos, xmat.reshape(ngeom, 9)
 
   # ---- meshes, scene BVH topology
-  meshes = build_mesh_bvhs(mjm) if mjm.nmesh else {"mesh_nface": [], "mesh_bounds": None}
+  meshes = build_mesh_bvhs(mjm) if mjm.nmesh or nhfield_of(mjm) else {"mesh_nface": [], "mesh_bounds": None, "nhfield": 0}
   enabled = np.nonzero(rendered)[0].astype(np.int32)
   geom_types = np.asarray(mjm.geom_type).reshape(-1)
-  supported = np.isin(geom_types[enabled], [GEOM_PLANE, GEOM_SPHERE, GEOM_CAPSULE, GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH, GEOM_SDF])
+  supported = np.isin(geom_types[enabled], [GEOM_PLANE, GEOM_SPHERE, GEOM_CAPSULE, GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH, GEOM_SDF, GEOM_HFIELD])
   if not np.all(supported):
     bad = sorted(set(geom_types[enabled][~supported].tolist()))
-    warnings.warn(f"geom types {bad} are not rendered by the GB300 build (height fields)", stacklevel=3)
+    warnings.warn(f"geom types {bad} are not rendered by the GB300 build", stacklevel=3)
   per_world = host_data is not None and np.asarray(host_data.geom_xpos).ndim == 3
   if host_data is None:
     lo = np.zeros((ngeom, 3))
@@ -1005,6 +1078,7 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     blas_root=_dev(m.get("blas_root"), device),
     blas_tri_base=_dev(m.get("blas_tri_base"), device),
     mesh_nface=list(m.get("mesh_nface", [])),
+    nhfield=int(m.get("nhfield", 0)),
     textures=textures,
     tex_data=tex_data,
     tex_desc=tex_desc,

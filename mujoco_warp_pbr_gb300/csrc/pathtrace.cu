@@ -448,7 +448,7 @@ int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
   tm.tiles_per_world = tm.tile_base[s.nrender];
   tm.total = tm.tiles_per_world * s.nworld;
   if (tm.total == 0) return MJPBR_OK;
-  bool mesh = s.nmesh > 0 && s.blas_root != nullptr;
+  bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
   if (mesh && tex) return launch_variant<true, true>(s, seed, tm, stream);
   if (mesh) return launch_variant<true, false>(s, seed, tm, stream);

@@ -57,9 +57,14 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
     V3 pos{xp[0], xp[1], xp[2]};
     V3 size{sz[0], sz[1], sz[2]};
     int32_t flags = 0;
+    // Triangle BVH of a mesh-like geom: the mesh's, or for a height field the one after the meshes.
+    int32_t blas = -1;
+    if (s.blas_root != nullptr && dataid >= 0) {
+      if ((type == MJPBR_GEOM_MESH || type == MJPBR_GEOM_SDF) && dataid < s.nmesh) blas = dataid;
+      if (type == MJPBR_GEOM_HFIELD && dataid < s.nhfield) blas = s.nmesh + dataid;
+    }
     bool supported = type == MJPBR_GEOM_PLANE || type == MJPBR_GEOM_SPHERE || type == MJPBR_GEOM_CAPSULE ||
-                     type == MJPBR_GEOM_ELLIPSOID || type == MJPBR_GEOM_CYLINDER || type == MJPBR_GEOM_BOX ||
-                     ((type == MJPBR_GEOM_MESH || type == MJPBR_GEOM_SDF) && dataid >= 0 && s.blas_root != nullptr);
+                     type == MJPBR_GEOM_ELLIPSOID || type == MJPBR_GEOM_CYLINDER || type == MJPBR_GEOM_BOX || blas >= 0;
     if (rgba.w == 0.0f || !supported) flags |= kGeomFlagSkip;
     float* gr = blk + L.geom_off + slot * kGeomFloats;
     gr[0] = pos.x;
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
     gr[14] = m[8];
     gr[15] = size.z;
     gr[16] = __int_as_float(g);
-    gr[17] = __int_as_float(dataid);
+    gr[17] = __int_as_float(blas);
     gr[18] = __int_as_float(matid);
     gr[19] = __int_as_float(flags);
 
@@ -112,9 +117,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
           ax[i] = r0 * sx + r1 * sy;
           break;
         }
-        default: {  // mesh: transformed local AABB
-          if (dataid >= 0 && s.mesh_bounds) {
-            const float* mb = s.mesh_bounds + dataid * 6;
+        default: {  // mesh or height field: transformed local AABB
+          if (blas >= 0 && s.mesh_bounds) {
+            const float* mb = s.mesh_bounds + blas * 6;
             float hx = 0.5f * (mb[3] - mb[0]), hy = 0.5f * (mb[4] - mb[1]), hz = 0.5f * (mb[5] - mb[2]);
             ax[i] = r0 * hx + r1 * hy + r2 * hz;
           } else {
@@ -124,8 +129,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
         }
       }
     }
-    if ((type == MJPBR_GEOM_MESH || type == MJPBR_GEOM_SDF) && dataid >= 0 && s.mesh_bounds) {
-      const float* mb = s.mesh_bounds + dataid * 6;
+    if (blas >= 0 && s.mesh_bounds) {
+      const float* mb = s.mesh_bounds + blas * 6;
       V3 lc{0.5f * (mb[0] + mb[3]), 0.5f * (mb[1] + mb[4]), 0.5f * (mb[2] + mb[5])};
       c = pos + V3{m[0] * lc.x + m[1] * lc.y + m[2] * lc.z, m[3] * lc.x + m[4] * lc.y + m[5] * lc.z,
                    m[6] * lc.x + m[7] * lc.y + m[8] * lc.z};

@@ -467,7 +467,7 @@ int render_rt_queue(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
   if (total == 0) return MJPBR_OK;
   if (total > INT32_MAX) return set_error(MJPBR_ERR_ARG, "render queue: %lld work items exceed the counter", (long long)total);
   qm.total = (int32_t)total;
-  const bool mesh = s.nmesh > 0 && s.blas_root != nullptr;
+  const bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   const bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
   if (mesh && tex) return launch_queue_variant<true, true>(s, seed, qm, stream);
   if (mesh) return launch_queue_variant<true, false>(s, seed, qm, stream);
@@ -509,7 +509,7 @@ int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
     tm.tile_base[c + 1] = tm.tile_base[c] + (any ? tm.tiles_x[c] * ty : 0);
   }
   if (tm.tile_base[s.nrender] == 0 || s.nworld == 0) return MJPBR_OK;
-  bool mesh = s.nmesh > 0 && s.blas_root != nullptr;
+  bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
   if (mesh && tex) return launch_variant<true, true>(s, seed, tm, stream);
   if (mesh) return launch_variant<true, false>(s, seed, tm, stream);

@@ -41,7 +41,8 @@ MJ_DEV void primitive_uv(int32_t type, V3 p, V3 ln, V3 size, float rx, float ry,
   *repy = ry;
   const float inv2pi = 0.5f / kPi;
   switch (type) {
-    case MJPBR_GEOM_PLANE: {
+    case MJPBR_GEOM_PLANE:
+    case MJPBR_GEOM_HFIELD: {  // a height field maps its texture over its x-y extent like a plane
       float sx = size.x > 0.0f ? size.x : 1.0f, sy = size.y > 0.0f ? size.y : 1.0f;
       if (uniform) {
         *u = p.x;

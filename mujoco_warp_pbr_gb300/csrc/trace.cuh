@@ -121,7 +121,8 @@ MJ_DEV float mesh_query(const MjpbrScene& sc, const Stack& st, int sp0, int32_t 
   return best;
 }
 
-// One geom against the ray: distance (or -1), world normal, mesh hit details.
+// One geom against the ray: distance (or -1), world normal, mesh hit details. Height fields are
+// traced as meshes (the reference's traverse.py:161-164 queries MuJoCo Warp's height-field mesh BVH).
 template <bool kMesh>
 MJ_DEV float intersect_geom(const MjpbrScene& sc, const Stack& st, int sp, const float* g, const Ray& r, float max_t,
                             bool cull, bool any, V3* n, float* u, float* v, int32_t* face, int32_t* mesh, int32_t* err) {
@@ -154,8 +155,8 @@ MJ_DEV float intersect_geom(const MjpbrScene& sc, const Stack& st, int sp, const
       d = ray_box(f, r, n);
       break;
     default:
-      if (kMesh && (type == MJPBR_GEOM_MESH || type == MJPBR_GEOM_SDF)) {
-        const int32_t mid = __float_as_int(g[17]);
+      if (kMesh && (type == MJPBR_GEOM_MESH || type == MJPBR_GEOM_SDF || type == MJPBR_GEOM_HFIELD)) {
+        const int32_t mid = __float_as_int(g[17]);  // triangle BVH (a height field's follows the meshes')
         if (mid >= 0) {
           V3 lo, ld, nl = v3(0.0f);
           map_local(f, r, &lo, &ld);

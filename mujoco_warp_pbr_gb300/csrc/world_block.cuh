@@ -28,7 +28,7 @@ constexpr int32_t kCamFloats = 24;
 constexpr int32_t kTriFloats = 12;
 
 // Geom record: [0..2] pos, [3] type; [4..6] xmat row 0, [7] size.x; [8..10] row 1, [11] size.y;
-// [12..14] row 2, [15] size.z; [16] geom id, [17] mesh id (dataid), [18] material id, [19] flags.
+// [12..14] row 2, [15] size.z; [16] geom id, [17] triangle BVH (mesh id; nmesh + height-field id; -1), [18] material id, [19] flags.
 constexpr int32_t kGeomFlagSkip = 1;  // rgba alpha == 0: invisible to every ray
 
 // Light record: [0..2] pos, [3] type; [4..6] dir, [7] flags; [8..10] diffuse, [11] intensity;

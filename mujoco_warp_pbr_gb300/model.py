@@ -33,7 +33,7 @@ class HostModel:
   geom_rgba: np.ndarray  # (ngeom, 4)
   geom_matid: np.ndarray  # (ngeom,)
   geom_group: np.ndarray  # (ngeom,)
-  geom_dataid: np.ndarray  # (ngeom,) mesh id of mesh geoms, else -1
+  geom_dataid: np.ndarray  # (ngeom,) mesh id of mesh geoms, height-field id of height fields, else -1
   # materials
   mat_rgba: np.ndarray  # (nmat, 4)
   mat_emission: np.ndarray  # (nmat,)
@@ -77,6 +77,13 @@ class HostModel:
   mesh_facenormal: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 3), np.int32))
   mesh_texcoord: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 2), np.float32))
   mesh_facetexcoord: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 3), np.int32))
+  # height fields (MuJoCo layout: nrow x ncol elevations in [0, 1], row-major, rows along y;
+  # size = x half-extent, y half-extent, elevation scale, base depth)
+  hfield_size: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 4), np.float32))
+  hfield_nrow: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
+  hfield_ncol: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
+  hfield_adr: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
+  hfield_data: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.float32))
   # textures (2D only; RGB or RGBA bytes concatenated in tex_data)
   tex_type: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))  # 0: 2D
   tex_width: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
@@ -114,6 +121,10 @@ class HostModel:
   @property
   def nmesh(self) -> int:
     return int(len(self.mesh_vertadr))
+
+  @property
+  def nhfield(self) -> int:
+    return int(len(self.hfield_nrow))
 
   @property
   def ntex(self) -> int:

@@ -190,4 +190,5 @@ class PbrRenderContext:
   max_registers: int | None = None
   ordered_traversal: bool | None = None
   traversal: str = "software"
+  nhfield: int = 0  # height-field BVHs after the meshes' in blas_root / blas_tri_base / mesh_bounds
   _host_cache: dict[str, Any] = dataclasses.field(default_factory=dict)

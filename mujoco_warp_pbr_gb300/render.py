@@ -173,6 +173,7 @@ def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
       "nlight": int(f["light_xpos"].shape[1]) if f["light_xpos"] is not None else 0,
       "ncam": int(f["cam_projection"].shape[0]),
       "nmesh": len(rc.mesh_nface),
+      "nhfield": int(rc.nhfield),
       "ntex": len(rc.tex_desc),
       "nenv": env.nenv if env is not None else 0,
       "nrender": b.nrender,

@@ -28,7 +28,7 @@ import numpy as np
 from mujoco_warp_pbr_gb300.model import HostData
 from mujoco_warp_pbr_gb300.model import HostModel
 
-GEOM_PLANE, GEOM_SPHERE, GEOM_CAPSULE, GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH = 0, 2, 3, 4, 5, 6, 7
+GEOM_PLANE, GEOM_HFIELD, GEOM_SPHERE, GEOM_CAPSULE, GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH = 0, 1, 2, 3, 4, 5, 6, 7
 LIGHT_SPOT, LIGHT_DIRECTIONAL, LIGHT_POINT = 0, 1, 2
 
 
@@ -79,6 +79,7 @@ class Builder:
   cams: list[dict[str, Any]] = dataclasses.field(default_factory=list)
   meshes: list[dict[str, Any]] = dataclasses.field(default_factory=list)
   textures: list[dict[str, Any]] = dataclasses.field(default_factory=list)
+  hfields: list[dict[str, Any]] = dataclasses.field(default_factory=list)
   headlight_active: bool = False
   headlight_ambient: tuple[float, float, float] = (0.0, 0.0, 0.0)
   headlight_diffuse: tuple[float, float, float] = (0.4, 0.4, 0.4)
@@ -157,6 +158,12 @@ class Builder:
     self.meshes.append({"vert": np.asarray(vert, np.float32), "face": np.asarray(face, np.int32), "normal": normal, "texcoord": texcoord})
     return len(self.meshes) - 1
 
+  def hfield(self, elevation: np.ndarray, size: Any) -> int:
+    """A height field: (nrow, ncol) elevations in [0, 1] (rows along y), size = x half-extent,
+    y half-extent, elevation scale, base depth (MuJoCo's hfield size)."""
+    self.hfields.append({"data": np.asarray(elevation, np.float32), "size": np.asarray(size, np.float32)})
+    return len(self.hfields) - 1
+
   def texture(self, rgba: np.ndarray, colorspace: int = 0) -> int:
     """A 2D RGBA8 texture (h, w, 4); colorspace 0 auto (colour roles sRGB), 1 linear, 2 sRGB."""
     self.textures.append({"data": np.ascontiguousarray(rgba, np.uint8), "colorspace": colorspace})
@@ -202,6 +209,8 @@ class Builder:
       tex_w.append(d.shape[1])
       tex_data.append(d.reshape(-1))
       off += d.size
+    hf = self.hfields
+    hf_adr = np.cumsum([0] + [h["data"].size for h in hf])[: len(hf)]
     center = np.mean([x["pos"] for x in g], axis=0) if g else np.zeros(3)
     mjm = HostModel(
       geom_type=np.array([x["type"] for x in g], np.int32),
@@ -256,6 +265,11 @@ class Builder:
       tex_adr=np.array(tex_adr, np.int64),
       tex_data=np.concatenate(tex_data) if tex_data else np.zeros(0, np.uint8),
       tex_colorspace=np.array([t["colorspace"] for t in self.textures], np.int32),
+      hfield_size=np.array([h["size"] for h in hf], np.float32).reshape(-1, 4),
+      hfield_nrow=np.array([h["data"].shape[0] for h in hf], np.int32),
+      hfield_ncol=np.array([h["data"].shape[1] for h in hf], np.int32),
+      hfield_adr=np.asarray(hf_adr, np.int32),
+      hfield_data=np.concatenate([h["data"].reshape(-1) for h in hf]) if hf else np.zeros(0, np.float32),
       headlight_active=self.headlight_active,
       headlight_ambient=self.headlight_ambient,
       headlight_diffuse=self.headlight_diffuse,
@@ -592,6 +606,60 @@ def procedural_env(rng: np.random.Generator, width: int = 1024) -> np.ndarray:
   ang = np.arccos(np.clip(d @ sun, -1, 1))
   img = img + 1.0e3 * np.exp(-0.5 * (ang / 0.03) ** 2)[..., None]
   return img.astype(np.float32)
+
+
+def hfield_scene(seed: int = 0, nworld: int = 8, res: int = 64, grid: int = 33, textured: bool = True) -> SyntheticScene:
+  """Terrain: a seeded value-noise height field (grid x grid samples over 3 x 3 m, 0.5 m of relief
+  on a 0.1 m base, a texture mapped over it) with five primitives resting above it, a sun and a
+  soft-shadowed point light. Per world: the terrain's yaw, the primitives' poses and colours."""
+  rng = np.random.default_rng(seed)
+  b = Builder()
+  elevation = noise_image(rng, grid - 1, 4, 1)[..., 0]
+  elevation = np.concatenate([elevation, elevation[:1]], 0)
+  elevation = np.concatenate([elevation, elevation[:, :1]], 1)  # (grid, grid), tileable noise closed
+  hid = b.hfield(elevation, (1.5, 1.5, 0.5, 0.1))
+  texid = {}
+  if textured:
+    albedo = noise_image(rng, 64, 8, 3) * 0.7 + 0.2
+    rgba = np.concatenate([albedo, np.ones((64, 64, 1))], -1)
+    texid = {1: b.texture((rgba * 255.0 + 0.5).astype(np.uint8))}
+  ground = b.material(rgba=(0.5, 0.5, 0.5, 1), metallic=0.0, roughness=0.8, texid=texid, texrepeat=(2.0, 2.0))
+  b.geom(GEOM_HFIELD, (1.5, 1.5, 0.3), matid=ground, dataid=hid)
+  for t, size in _random_primitives(rng, 5):
+    b.geom(t, size)
+  b.light(LIGHT_DIRECTIONAL, pos=(0, 0, 4), dir=(0.4, 0.3, -1.0), diffuse=(0.8, 0.8, 0.8), castshadow=True)
+  b.light(LIGHT_POINT, pos=(-0.6, 0.4, 1.6), diffuse=(0.4, 0.4, 0.4), range=10.0, bulbradius=0.05, castshadow=True)
+  b.camera((0.0, -3.0, 2.0), (0.0, 0.0, 0.2), fovy=50.0, resolution=(res, res))
+  mjm, mjd0 = b.build()
+  ngeom = mjm.ngeom
+  xpos = np.broadcast_to(mjd0.geom_xpos, (nworld, ngeom, 3)).copy()
+  xmat = np.broadcast_to(mjd0.geom_xmat, (nworld, ngeom, 9)).copy()
+  yaw = rng.uniform(0.0, 2.0 * np.pi, nworld)
+  c, s_ = np.cos(yaw), np.sin(yaw)
+  z, o = np.zeros(nworld), np.ones(nworld)
+  xmat[:, 0] = np.stack([c, -s_, z, s_, c, z, z, z, o], -1)
+  xpos[:, 1:, :2] = rng.uniform(-1.0, 1.0, (nworld, ngeom - 1, 2))
+  xpos[:, 1:, 2] = rng.uniform(0.4, 0.9, (nworld, ngeom - 1))
+  xmat[:, 1:] = quat_to_mat(random_quats(rng, (nworld, ngeom - 1)))
+  mjd = HostData(
+    geom_xpos=xpos.astype(np.float32),
+    geom_xmat=xmat.astype(np.float32),
+    cam_xpos=np.broadcast_to(mjd0.cam_xpos, (nworld, mjm.ncam, 3)).astype(np.float32),
+    cam_xmat=np.broadcast_to(mjd0.cam_xmat, (nworld, mjm.ncam, 9)).astype(np.float32),
+    light_xpos=np.broadcast_to(mjd0.light_xpos, (nworld, mjm.nlight, 3)).astype(np.float32),
+    light_xdir=np.broadcast_to(mjd0.light_xdir, (nworld, mjm.nlight, 3)).astype(np.float32),
+  )
+  rgba = np.concatenate([rng.uniform(0.05, 0.95, (nworld, ngeom, 3)), np.ones((nworld, ngeom, 1))], axis=-1)
+  rgba[:, 0] = (0.5, 0.5, 0.5, 1.0)  # the terrain keeps its material colour
+  return SyntheticScene(
+    name=f"hfield_{nworld}x{res}",
+    mjm=mjm,
+    mjd=mjd,
+    nworld=nworld,
+    options={"cam_res": (res, res), "render_rgb": True, "render_depth": True, "render_seg": True, "shadow_samples": 4},
+    per_world={"geom_rgba": rgba.astype(np.float32)},
+    seed=seed,
+  )
 
 
 def mesh_ibl_scene(seed: int = 0, nworld: int = 4096, res: int = 128, tex_size: int = 512, env_width: int = 1024) -> SyntheticScene:

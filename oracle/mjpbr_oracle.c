@@ -657,6 +657,146 @@ static float mesh_query(const MjpbrScene* s, int mesh, int nface, v3 lo, v3 ld, 
   return best;
 }
 
+/* Height fields: MuJoCo's height-field solid (an nrow x ncol elevation grid over
+ * [-size0, size0] x [-size1, size1], z = size2 * elevation, on a base at z = -size3), triangulated
+ * by the oracle itself into a closed mesh and queried by brute force. The reference traces MuJoCo
+ * Warp's height-field mesh (mujoco_warp_pbr/_src/traverse.py:161-164, third party). Faces, in
+ * order: the top, two per cell (r, c), (r, c+1), (r+1, c+1) and (r, c), (r+1, c+1), (r+1, c),
+ * cells row by row; the side walls, two per border segment p -> q of the border walked
+ * counter-clockwise seen from +z from sample (0, 0) (top p, base q, top q and top p, base p,
+ * base q); the base, a fan centre, base q, base p over the same segments. Outward winding.
+ * Coordinates in double, rounded once to float. Set by oracle_set_hfields. */
+typedef struct {
+  int nvert, nface;
+  float* vert;  /* (nvert, 3) */
+  int32_t* face; /* (nface, 3) */
+} ohf_t;
+
+static ohf_t* g_hf = NULL;
+static int g_nhf = 0;
+
+static void hf_free(void) {
+  for (int h = 0; h < g_nhf; ++h) {
+    free(g_hf[h].vert);
+    free(g_hf[h].face);
+  }
+  free(g_hf);
+  g_hf = NULL;
+  g_nhf = 0;
+}
+
+static void hf_build(ohf_t* o, int nr, int nc, const float* size, const float* elev) {
+  int ntop = nr * nc, nring = 2 * (nr - 1) + 2 * (nc - 1);
+  o->nvert = 2 * ntop + 1;
+  o->nface = 2 * (nr - 1) * (nc - 1) + 3 * nring;
+  o->vert = (float*)malloc(sizeof(float) * 3 * (size_t)o->nvert);
+  o->face = (int32_t*)malloc(sizeof(int32_t) * 3 * (size_t)o->nface);
+  for (int r = 0; r < nr; ++r) {
+    for (int c = 0; c < nc; ++c) {
+      double x = (double)size[0] * (2.0 * c / (nc - 1) - 1.0);
+      double y = (double)size[1] * (2.0 * r / (nr - 1) - 1.0);
+      float* top = o->vert + 3 * (r * nc + c);
+      float* bot = o->vert + 3 * (ntop + r * nc + c);
+      top[0] = bot[0] = (float)x;
+      top[1] = bot[1] = (float)y;
+      top[2] = (float)((double)size[2] * (double)elev[r * nc + c]);
+      bot[2] = (float)(-(double)size[3]);
+    }
+  }
+  float* centre = o->vert + 3 * (2 * ntop);
+  centre[0] = 0.0f;
+  centre[1] = 0.0f;
+  centre[2] = (float)(-(double)size[3]);
+  int32_t* f = o->face;
+  for (int r = 0; r + 1 < nr; ++r) {
+    for (int c = 0; c + 1 < nc; ++c) {
+      int a = r * nc + c, b = r * nc + c + 1, d = (r + 1) * nc + c + 1, e = (r + 1) * nc + c;
+      f[0] = a, f[1] = b, f[2] = d;
+      f[3] = a, f[4] = d, f[5] = e;
+      f += 6;
+    }
+  }
+  /* border ring, counter-clockwise from +z */
+  int* ring = (int*)malloc(sizeof(int) * (size_t)nring);
+  int k = 0;
+  for (int c = 0; c + 1 < nc; ++c) ring[k++] = c;
+  for (int r = 0; r + 1 < nr; ++r) ring[k++] = r * nc + nc - 1;
+  for (int c = nc - 1; c > 0; --c) ring[k++] = (nr - 1) * nc + c;
+  for (int r = nr - 1; r > 0; --r) ring[k++] = r * nc;
+  for (int i = 0; i < nring; ++i) {
+    int p = ring[i], q = ring[(i + 1) % nring];
+    f[0] = p, f[1] = q + ntop, f[2] = q;
+    f[3] = p, f[4] = p + ntop, f[5] = q + ntop;
+    f += 6;
+  }
+  for (int i = 0; i < nring; ++i) {
+    int p = ring[i], q = ring[(i + 1) % nring];
+    f[0] = 2 * ntop, f[1] = q + ntop, f[2] = p + ntop;
+    f += 3;
+  }
+  free(ring);
+}
+
+/* Replaces the oracle's height fields (MuJoCo's hfield_* arrays; n = 0 clears them). Returns 0,
+ * or 1 for a grid smaller than 2 x 2. */
+int oracle_set_hfields(int n, const int32_t* nrow, const int32_t* ncol, const float* size, const int32_t* adr,
+                       const float* data) {
+  hf_free();
+  if (n <= 0) return 0;
+  for (int h = 0; h < n; ++h)
+    if (nrow[h] < 2 || ncol[h] < 2) return 1;
+  g_hf = (ohf_t*)calloc((size_t)n, sizeof(ohf_t));
+  g_nhf = n;
+  for (int h = 0; h < n; ++h) hf_build(&g_hf[h], nrow[h], ncol[h], size + 4 * h, data + adr[h]);
+  return 0;
+}
+
+/* Copies height field h's triangulation out (for tests): counts always, arrays when not NULL. */
+int oracle_hfield_mesh(int h, int* nvert, int* nface, float* vert, int32_t* face) {
+  if (h < 0 || h >= g_nhf) return 1;
+  *nvert = g_hf[h].nvert;
+  *nface = g_hf[h].nface;
+  if (vert) memcpy(vert, g_hf[h].vert, sizeof(float) * 3 * (size_t)g_hf[h].nvert);
+  if (face) memcpy(face, g_hf[h].face, sizeof(int32_t) * 3 * (size_t)g_hf[h].nface);
+  return 0;
+}
+
+/* Closest (any_hit: first) face of height field h in [0, tmax), brute force in face order. */
+static float hfield_query(int h, v3 lo, v3 ld, float tmax, int cull, int any_hit, v3* nl, float* bu, float* bv,
+                          int* face) {
+  const ohf_t* o = &g_hf[h];
+  woop_t w = woop_setup(lo, ld);
+  float best = tmax;
+  int found = -1;
+  v3 e1b = V(0, 0, 0), e2b = V(0, 0, 0);
+  float ub = 0.0f, vb = 0.0f;
+  for (int f = 0; f < o->nface; ++f) {
+    const int32_t* fv = o->face + 3 * f;
+    const float* p0 = o->vert + 3 * fv[0];
+    const float* p1 = o->vert + 3 * fv[1];
+    const float* p2 = o->vert + 3 * fv[2];
+    v3 v0 = V(p0[0], p0[1], p0[2]), v1 = V(p1[0], p1[1], p1[2]), v2 = V(p2[0], p2[1], p2[2]);
+    float u, v;
+    float t = woop_hit(&w, v0, v1, v2, best, &u, &v);
+    if (t < 0.0f) continue;
+    v3 e1 = vsub(v1, v0), e2 = vsub(v2, v0);
+    if (!any_hit && cull && vdot(ld, vcross(e1, e2)) > 0.0f) continue;
+    if (any_hit) return t;
+    best = t;
+    found = f;
+    e1b = e1;
+    e2b = e2;
+    ub = u;
+    vb = v;
+  }
+  if (found < 0) return -1.0f;
+  *nl = vnorm(vcross(e1b, e2b));
+  *bu = ub;
+  *bv = vb;
+  *face = found;
+  return best;
+}
+
 /* ------------------------------------------------------------------ scene queries */
 
 typedef struct {
@@ -721,6 +861,15 @@ static float intersect(const world_t* W, int g, v3 o, v3 d, float max_t, int cul
       float t = mesh_query(s, mid, W->mesh_nface[mid], lo, ld, max_t, cull, any_hit, &nl, u, v, face);
       *n = any_hit ? V(0, 0, 0) : mat_mul(f.mat, nl);
       *mesh = mid;
+      return t;
+    }
+    case MJPBR_GEOM_HFIELD: {
+      int hid = s->geom_dataid.ptr ? bi(s->geom_dataid, W->w, s->ngeom, g) : -1;
+      if (hid < 0 || hid >= g_nhf) return -1.0f;
+      v3 lo, ld, nl = V(0, 0, 0);
+      map_local(&f, o, d, &lo, &ld);
+      float t = hfield_query(hid, lo, ld, max_t, cull, any_hit, &nl, u, v, face);
+      *n = any_hit ? V(0, 0, 0) : mat_mul(f.mat, nl);
       return t;
     }
     default:
@@ -1107,7 +1256,7 @@ static void primitive_uv(int type, v3 p, v3 ln, v3 size, float rx, float ry, int
   const float inv2pi = 0.5f / PI_F;
   *repx = rx;
   *repy = ry;
-  if (type == MJPBR_GEOM_PLANE) {
+  if (type == MJPBR_GEOM_PLANE || type == MJPBR_GEOM_HFIELD) { /* height fields map like planes */
     float sx = size.x > 0.0f ? size.x : 1.0f, sy = size.y > 0.0f ? size.y : 1.0f;
     if (uniform) {
       *u = p.x;

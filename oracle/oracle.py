@@ -60,6 +60,10 @@ def load() -> ctypes.CDLL:
     lib.oracle_prefilter.argtypes = [ctypes.POINTER(_lib.Texture), vp, i32, i32, i32, i32, vp]
     lib.oracle_struct_layout.argtypes = [ctypes.POINTER(ctypes.c_int64)]
     lib.oracle_set_mesh_bvh.argtypes = [i32]
+    lib.oracle_set_hfields.argtypes = [i32, vp, vp, vp, vp, vp]
+    lib.oracle_set_hfields.restype = i32
+    lib.oracle_hfield_mesh.argtypes = [i32, ctypes.POINTER(i32), ctypes.POINTER(i32), vp, vp]
+    lib.oracle_hfield_mesh.restype = i32
     lib.oracle_nthreads.restype = i32
     lib.oracle_sincos_turns.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     lib.oracle_rand01.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
@@ -204,6 +208,7 @@ class OracleScene:
         "nlight": nlight,
         "ncam": ncam,
         "nmesh": mjm.nmesh,
+        "nhfield": io_lib.nhfield_of(mjm),
         "ntex": mjm.ntex,
         "nrender": o["nrender"],
         "total_rays": o["total_rays"],
@@ -271,6 +276,7 @@ class OracleScene:
       self.ray_origin, self.ray_direction = rays_lib.pack_camera_rays(options["camera_rays"], o["cam_res"])
       a.update({"ray_origin": self.ray_origin, "ray_direction": self.ray_direction, "bundle_res": o["cam_res"]})
     self.mesh_nface = np.ascontiguousarray(self.hc.meshes.get("mesh_nface", []), i32)
+    self.hfields = hfield_arrays(mjm)
     self.arrays = a  # keeps every array alive
     self.scene = _scene.fill_scene({k: v for k, v in a.items() if v is not None})
 
@@ -279,6 +285,7 @@ class OracleScene:
     with settings.denoise the a-trous filter then runs over every world (unless denoise=False)."""
     w0, w1 = worlds if worlds is not None else (0, self.nworld)
     lib = load()
+    set_hfields(self.hfields)
     fn = lib.oracle_render_pt if self.hc.settings["tier"] == 1 else lib.oracle_render_rt
     status = fn(self.scene, self.mesh_nface.ctypes.data if len(self.mesh_nface) else None, seed & 0xFFFFFFFF, w0, w1, nthreads)
     if status != 0:
@@ -294,6 +301,42 @@ class OracleScene:
     """Runs the oracle's a-trous filter on the current demodulated buffer and guide arrays."""
     if load().oracle_denoise(self.scene, nthreads) != 0:
       raise RuntimeError("oracle_denoise failed")
+
+
+def hfield_arrays(mjm: Any) -> tuple[np.ndarray, ...]:
+  """(nrow, ncol, size, adr, data) of a model's height fields as contiguous arrays (empty without)."""
+  n = io_lib.nhfield_of(mjm)
+  if n == 0:
+    return ()
+  return (
+    np.ascontiguousarray(np.asarray(mjm.hfield_nrow).reshape(-1), np.int32),
+    np.ascontiguousarray(np.asarray(mjm.hfield_ncol).reshape(-1), np.int32),
+    np.ascontiguousarray(np.asarray(mjm.hfield_size).reshape(-1, 4), np.float32),
+    np.ascontiguousarray(np.asarray(mjm.hfield_adr).reshape(-1), np.int32),
+    np.ascontiguousarray(np.asarray(mjm.hfield_data).reshape(-1), np.float32),
+  )
+
+
+def set_hfields(arrays: tuple[np.ndarray, ...]) -> None:
+  """Gives the oracle a model's height fields (hfield_arrays), which it triangulates itself."""
+  if not arrays:
+    status = load().oracle_set_hfields(0, None, None, None, None, None)
+  else:
+    status = load().oracle_set_hfields(len(arrays[0]), *(a.ctypes.data for a in arrays))
+  if status != 0:
+    raise ValueError("height fields need at least 2 x 2 samples")
+
+
+def hfield_mesh(h: int) -> tuple[np.ndarray, np.ndarray]:
+  """The oracle's triangulation of height field h (after set_hfields): vertices, faces."""
+  lib = load()
+  nv, nf = ctypes.c_int32(0), ctypes.c_int32(0)
+  if lib.oracle_hfield_mesh(h, ctypes.byref(nv), ctypes.byref(nf), None, None) != 0:
+    raise IndexError(f"no height field {h}")
+  vert = np.zeros((nv.value, 3), np.float32)
+  face = np.zeros((nf.value, 3), np.int32)
+  lib.oracle_hfield_mesh(h, ctypes.byref(nv), ctypes.byref(nf), vert.ctypes.data, face.ctypes.data)
+  return vert, face
 
 
 def unpack_rgb(rgb: np.ndarray) -> np.ndarray:

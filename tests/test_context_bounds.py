@@ -27,9 +27,10 @@ def test_batched_bounds_match_per_world_bounds():
   ])
   size = rng.uniform(0.05, 0.5, size=(len(types), 3))
   size[0, :2] = 0.0  # an infinite plane
-  dataid = np.array([-1, -1, -1, -1, -1, -1, -1, 0, 1, 0, -1])
-  mjm = SimpleNamespace(geom_type=types, geom_size=size, geom_dataid=dataid)
-  mesh_bounds = rng.normal(size=(2, 6))
+  dataid = np.array([-1, -1, -1, -1, -1, -1, -1, 0, 1, 0, 0])
+  # two meshes and one height field: BVH bounds of the meshes, then of the height field
+  mjm = SimpleNamespace(geom_type=types, geom_size=size, geom_dataid=dataid, nmesh=2, hfield_nrow=np.array([3]))
+  mesh_bounds = rng.normal(size=(3, 6))
   mesh_bounds[:, 3:] = mesh_bounds[:, :3] + np.abs(mesh_bounds[:, 3:])
   nworld = 5
   xpos = rng.normal(size=(nworld, len(types), 3))
@@ -39,3 +40,10 @@ def test_batched_bounds_match_per_world_bounds():
     lo, hi = context.geom_aabbs(mjm, xpos[w], xmat[w], mesh_bounds)
     np.testing.assert_allclose(lo_all[w], lo, rtol=0, atol=1e-12)
     np.testing.assert_allclose(hi_all[w], hi, rtol=0, atol=1e-12)
+  # the height field is bounded by its own BVH box (index nmesh + 0), not by its geom size
+  R = xmat[0, -1].reshape(3, 3)
+  mb = mesh_bounds[2]
+  centre = xpos[0, -1] + R @ (0.5 * (mb[:3] + mb[3:]))
+  half = np.abs(R) @ (0.5 * (mb[3:] - mb[:3]))
+  np.testing.assert_allclose(lo_all[0, -1], centre - half, atol=1e-12)
+  np.testing.assert_allclose(hi_all[0, -1], centre + half, atol=1e-12)
