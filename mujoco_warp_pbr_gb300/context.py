@@ -22,6 +22,7 @@ import torch
 
 from mujoco_warp_pbr_gb300 import _lib
 from mujoco_warp_pbr_gb300 import envmap as envmap_lib
+from mujoco_warp_pbr_gb300 import model as model_lib
 from mujoco_warp_pbr_gb300.pbr_types import LightModel
 from mujoco_warp_pbr_gb300.pbr_types import Outputs
 from mujoco_warp_pbr_gb300.pbr_types import PbrRenderContext
@@ -648,6 +649,7 @@ def prepare_context(
   data: Any = None,
 ) -> HostContext:
   """Host half of create_render_context (see there); needs no GPU."""
+  mjm = model_lib.as_host_model(mjm)
   light_model = _enum(LightModel, light_model, "light_model")
   tone_mapper = _enum(ToneMapper, tone_mapper, "tone_mapper")
   unset_material = _enum(UnsetMaterial, unset_material, "unset_material")

@@ -4,8 +4,9 @@ The reference takes a mujoco.MjModel (host) plus mujoco_warp Model / Data (devic
 MuJoCo Warp are not dependencies of this package, so:
 
   * `HostModel` / `HostData` hold the MjModel / MjData fields the render path reads, under
-    MuJoCo's names (numpy arrays). Any object with those attributes works, including a real
-    mujoco.MjModel for the fields it has.
+    MuJoCo's names (numpy arrays). A real mujoco.MjModel / MjData works too: `as_host_model`
+    flattens the MjModel's nested headlight / statistic / clip-plane structs, and
+    create_render_context, put_model and put_data call it.
   * `put_model` / `put_data` make the device `Model` / `Data` (torch CUDA tensors with MuJoCo
     Warp's field names and batching: per-world tables have a leading dimension of 1 or nworld),
     like mujoco_warp.put_model / put_data. Objects exposing __cuda_array_interface__ (e.g. Warp
@@ -131,6 +132,43 @@ class HostModel:
     return int(len(self.tex_type))
 
 
+def as_host_model(mjm: Any) -> Any:
+  """The model as the renderer reads it: a HostModel (or any object already carrying HostModel's
+  flat names) as it is; a mujoco.MjModel converted.
+
+  An MjModel keeps the headlight, the model statistics and the clip planes in nested structs
+  (mjm.vis.headlight.active / ambient / diffuse / specular, mjm.stat.center / extent,
+  mjm.vis.map.znear / zfar as fractions of the extent), which the reference reads there
+  (mujoco_warp_pbr/_src/io.py:242-243, lights.py:146-147); every other field has the same name in
+  both. Fields a MuJoCo release lacks fall back to HostModel's defaults, or raise ValueError when
+  HostModel has none.
+  """
+  if isinstance(mjm, HostModel) or not hasattr(mjm, "vis") or not hasattr(mjm, "stat"):
+    return mjm
+  values: dict[str, Any] = {}
+  missing = []
+  for f in dataclasses.fields(HostModel):
+    if hasattr(mjm, f.name):
+      values[f.name] = np.array(getattr(mjm, f.name), copy=True)
+    elif f.default is dataclasses.MISSING and f.default_factory is dataclasses.MISSING:
+      missing.append(f.name)
+  if missing:
+    raise ValueError(f"the model lacks {', '.join(missing)} (the renderer needs MuJoCo 3.3 or later)")
+  hl = mjm.vis.headlight
+  extent = float(mjm.stat.extent)
+  values.update(
+    headlight_active=bool(int(hl.active)),
+    headlight_ambient=tuple(float(c) for c in hl.ambient),
+    headlight_diffuse=tuple(float(c) for c in hl.diffuse),
+    headlight_specular=tuple(float(c) for c in hl.specular),
+    stat_center=tuple(float(c) for c in mjm.stat.center),
+    stat_extent=extent,
+    znear=float(mjm.vis.map.znear) * extent,
+    zfar=float(mjm.vis.map.zfar) * extent,
+  )
+  return HostModel(**values)
+
+
 @dataclasses.dataclass
 class HostData:
   """MjData fields used by the renderer, for one world (or (nworld, ...) per world)."""
@@ -170,7 +208,9 @@ def _t(a: Any, dtype: torch.dtype, device: torch.device) -> torch.Tensor:
 
 
 def put_model(mjm: HostModel, device: Any = None) -> Model:
-  """Device copy of the model (mujoco_warp.put_model's role); per-world tables get batch 1."""
+  """Device copy of the model (mujoco_warp.put_model's role); per-world tables get batch 1. Takes a
+  HostModel or a mujoco.MjModel (as_host_model)."""
+  mjm = as_host_model(mjm)
   dev = _device(device)
   f32, i32 = torch.float32, torch.int32
 
@@ -221,6 +261,7 @@ def put_model(mjm: HostModel, device: Any = None) -> Model:
 def put_data(mjm: HostModel, mjd: HostData, nworld: int = 1, device: Any = None) -> Data:
   """Device data for nworld worlds (mujoco_warp.put_data's role): a single world's arrays are
   replicated; arrays with a leading nworld dimension are copied as they are."""
+  mjm = as_host_model(mjm)
   dev = _device(device)
 
   def per_world(a: np.ndarray, n: int, k: int) -> torch.Tensor:

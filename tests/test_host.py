@@ -200,3 +200,62 @@ def test_output_layout():
   assert o["rgb_adr"] == [0, -1] and o["rgb_stride"] == 12
   assert o["depth_adr"] == [0, 12] and o["depth_stride"] == 22
   assert o["seg_adr"] == [-1, 0] and o["seg_stride"] == 10
+
+
+_NESTED = ("headlight_active", "headlight_ambient", "headlight_diffuse", "headlight_specular", "stat_center", "stat_extent", "znear", "zfar")
+
+
+def _as_mujoco(hm):
+  """A stand-in for mujoco.MjModel: HostModel's arrays under their (shared) MuJoCo names, the
+  headlight, statistics and clip planes in MuJoCo's nested vis / stat structs."""
+  import dataclasses
+  from types import SimpleNamespace
+
+  from mujoco_warp_pbr_gb300.model import HostModel
+
+  ns = SimpleNamespace(**{f.name: getattr(hm, f.name) for f in dataclasses.fields(HostModel) if f.name not in _NESTED})
+  ns.vis = SimpleNamespace(
+    headlight=SimpleNamespace(active=int(hm.headlight_active), ambient=np.array(hm.headlight_ambient, np.float32),
+                              diffuse=np.array(hm.headlight_diffuse, np.float32), specular=np.array(hm.headlight_specular, np.float32)),
+    map=SimpleNamespace(znear=hm.znear / hm.stat_extent, zfar=hm.zfar / hm.stat_extent),
+  )
+  ns.stat = SimpleNamespace(center=np.array(hm.stat_center), extent=hm.stat_extent)
+  return ns
+
+
+def test_mujoco_model_is_accepted():
+  """A mujoco.MjModel keeps the headlight, statistics and clip planes in nested structs (the
+  reference reads mjm.vis.headlight, mjm.stat: io.py:242-243, lights.py:146-147); the context built
+  from one equals the context built from the flat HostModel."""
+  import dataclasses
+
+  from mujoco_warp_pbr_gb300 import model as model_lib
+
+  sc = synthetic.primitive_scene(seed=4, nworld=2, res=16)
+  hm = dataclasses.replace(sc.mjm, headlight_active=True, headlight_ambient=(0.2, 0.1, 0.05), stat_extent=2.5, znear=0.025, zfar=125.0)
+  fake = _as_mujoco(hm)
+  conv = model_lib.as_host_model(fake)
+  for f in dataclasses.fields(type(hm)):
+    a, b = getattr(conv, f.name), getattr(hm, f.name)
+    if isinstance(b, np.ndarray):
+      np.testing.assert_array_equal(a, b, err_msg=f.name)
+    else:
+      np.testing.assert_allclose(np.asarray(a, np.float64), np.asarray(b, np.float64), rtol=1e-6, err_msg=f.name)
+  assert model_lib.as_host_model(hm) is hm
+  a = context.prepare_context(fake, 2, data=sc.mjd, **sc.options)
+  b = context.prepare_context(hm, 2, data=sc.mjd, **sc.options)
+  assert a.settings.keys() == b.settings.keys()
+  for k in b.settings:
+    np.testing.assert_allclose(np.asarray(a.settings[k], np.float64), np.asarray(b.settings[k], np.float64), rtol=1e-6, err_msg=k)
+  for k in b.tables:
+    np.testing.assert_array_equal(a.tables[k], b.tables[k], err_msg=k)
+  np.testing.assert_array_equal(a.tlas_child, b.tlas_child)
+
+
+def test_mujoco_model_without_required_fields():
+  from mujoco_warp_pbr_gb300 import model as model_lib
+
+  fake = _as_mujoco(synthetic.primitive_scene(seed=0, nworld=1, res=8).mjm)
+  del fake.light_intensity
+  with pytest.raises(ValueError, match="light_intensity .*MuJoCo 3.3"):
+    model_lib.as_host_model(fake)
