@@ -165,15 +165,19 @@ def algorithmic_bytes(rc) -> int:
 
 
 def _traffic(workload: str) -> float | None:
-  p = ROOT / "profiles" / "ncu_traffic.json"
+  """DRAM bytes per launch of the workload's render kernel from an ncu capture
+  (profiles/ncu_traffic.txt: workload, bytes per launch, kernel), or None."""
+  p = ROOT / "profiles" / "ncu_traffic.txt"
   if not p.exists():
     return None
-  try:
-    data = json.loads(p.read_text())
-    entry = data.get(workload)
-    return float(entry["bytes_per_launch"]) if entry else None
-  except (ValueError, KeyError, TypeError):
-    return None
+  for line in p.read_text().splitlines():
+    parts = line.split("#", 1)[0].split()
+    if len(parts) >= 2 and parts[0] == workload:
+      try:
+        return float(parts[1])
+      except ValueError:
+        return None
+  return None
 
 
 def make_scene(args):

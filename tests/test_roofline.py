@@ -41,3 +41,12 @@ def test_copies_are_summed_and_scaled():
   assert r["achieved"] == pytest.approx(flops * 10 / 1e-3 / 1e12)
   assert r["frac"] == pytest.approx(r["achieved"] / roofline.FP32_PEAK_TFLOPS)
   assert roofline.FP32_PEAK_TFLOPS == pytest.approx(80.55, abs=0.01)
+
+
+def test_bench_reads_committed_traffic():
+  """The bench's roofline.traffic comes from the committed ncu figures, per workload."""
+  import bench
+
+  assert bench._traffic("mesh_ibl_4096x128") == 533256704 + 12613810176
+  assert bench._traffic("path_1024x128_spp2") == 21236992 + 1029066240
+  assert bench._traffic("mesh_ibl_1024x128") is None
