@@ -204,7 +204,10 @@ def _device(device: Any) -> torch.device:
 
 
 def _t(a: Any, dtype: torch.dtype, device: torch.device) -> torch.Tensor:
-  return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(device)
+  arr = np.ascontiguousarray(a)
+  if not arr.flags.writeable:  # e.g. a broadcast view: torch wants memory it may write
+    arr = arr.copy()
+  return torch.as_tensor(arr, dtype=dtype).to(device)
 
 
 def put_model(mjm: HostModel, device: Any = None) -> Model:

@@ -10,6 +10,7 @@ like the reference's launch-input cache, mujoco_warp_pbr/_src/launch.py:89-115).
 
 from __future__ import annotations
 
+import warnings
 from typing import Any
 
 import numpy as np
@@ -257,11 +258,41 @@ def scene(m: Any, d: Any, rc: PbrRenderContext) -> _lib.Scene:
   if cached is not None and cached[1] == ids:
     return cached[2]
   _check_env_id(rc)
+  _warn_ignored_overrides(m, rc)
   fields = scene_fields(m, d, rc)
   struct = _scene.fill_scene(fields)
   # the cache holds the sources and the converted tensors so their addresses stay valid
   rc._host_cache["scene"] = (sources, ids, struct, fields)
   return struct
+
+
+def _warn_ignored_overrides(m: Any, rc: PbrRenderContext) -> None:
+  """UserWarning when a replaced array needs a flag that is off: translucent m.geom_rgba without
+  rc.has_transparency, positive rc.mat_reflectance without rc.has_reflection (both flags are
+  derived from the model at creation; mujoco_warp_pbr/_src/launch.py:59-86). Each array is
+  checked once, when it first appears; the arrays of the first render are not checked; nothing
+  is checked while a graph is being captured."""
+  if torch.cuda.is_available() and torch.cuda.is_current_stream_capturing():
+    return
+  checks = (
+    ("geom_rgba", getattr(m, "geom_rgba", None), rc.has_transparency, "has_transparency",
+     lambda a: bool(np.any((a[..., 3] > 0.0) & (a[..., 3] < 1.0)))),
+    ("mat_reflectance", rc.mat_reflectance, rc.has_reflection, "has_reflection", lambda a: bool(np.any(a > 0.0))),
+  )
+  for name, array, enabled, flag, needs in checks:
+    key = "seen_" + name
+    seen = rc._host_cache.get(key)
+    rc._host_cache[key] = array
+    if array is None or seen is None or seen is array or enabled:
+      continue
+    if isinstance(array, torch.Tensor):
+      values = array.detach().cpu().numpy()
+    elif hasattr(array, "__cuda_array_interface__"):
+      values = torch.as_tensor(array, device=rc.device).cpu().numpy()
+    else:
+      values = np.asarray(array)
+    if values.size and needs(values):
+      warnings.warn(f"the replaced {name} is ignored by the renderer: set rc.{flag} = True to render it", stacklevel=4)
 
 
 def _check_env_id(rc: PbrRenderContext) -> None:
