@@ -723,7 +723,7 @@ def run_batched(args) -> None:
 def main() -> None:
   p = argparse.ArgumentParser()
   p.add_argument("--gpus", type=int, default=1)
-  p.add_argument("--steps", type=int, default=20)
+  p.add_argument("--steps", type=int, default=None, help="timed steps (default 20; 2000 for the 0.1 ms primitives frame, so the clock sampler sees the GPU under load)")
   p.add_argument("--warmup", type=int, default=3)
   p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
   p.add_argument("--workload", choices=["mesh_ibl", "primitives", "path", "batched", "large_path"], default="mesh_ibl")
@@ -745,6 +745,8 @@ def main() -> None:
     args.nworld = {"mesh_ibl": 4096, "path": 1024, "batched": 2048, "large_path": 8192}.get(args.workload, 16)
   if args.res is None:
     args.res = {"mesh_ibl": 128, "path": 128, "large_path": 256}.get(args.workload, 64)
+  if args.steps is None:
+    args.steps = 2000 if (args.workload == "primitives" and args.impl == "gb300") else 20
   args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
   if args.impl == "reference":
     run_reference(args)
