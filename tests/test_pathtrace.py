@@ -166,3 +166,32 @@ def test_tiles_cover_ragged_cameras():
   gpu = helpers.render_gpu(m, d, rc, seed=4)
   ref = helpers.oracle_render(sc, seed=4, tables=helpers.gpu_tables(rc), **opts)
   _assert_path_parity(gpu, ref)
+
+
+def _rel_mse(x: np.ndarray, ref: np.ndarray) -> float:
+  """The reference's relative MSE on linear HDR (benchmarks/validate.py:140)."""
+  return float(np.mean((x - ref) ** 2 / (ref**2 + 1.0e-2)))
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+def test_converged_means_at_4096_spp_match_oracle():
+  """Path-traced means at 4096 spp on the path workload (emissive quads, NEE, depth 4, Russian
+  roulette after bounce 2): the GPU's image against the oracle's with the same seed, and, for
+  scale, against an independent 4096-spp oracle estimate (another seed)."""
+  from mujoco_warp_pbr_gb300 import synthetic
+  from tests import helpers
+
+  sc = synthetic.path_scene(seed=3, nworld=2, res=32, spp=4096)
+  opts = dict(path_samples=4096, denoise=False, render_hdr=True)
+  m, d, rc = helpers.gpu_scene(sc, **opts)
+  gpu = helpers.render_gpu(m, d, rc, seed=21)["hdr"].astype(np.float64)
+  tables = helpers.gpu_tables(rc)
+  ref = helpers.oracle_render(sc, seed=21, tables=tables, **opts)["hdr"].astype(np.float64)
+  other = helpers.oracle_render(sc, seed=22, tables=tables, **opts)["hdr"].astype(np.float64)
+  same_seed, noise = _rel_mse(gpu, ref), _rel_mse(other, ref)
+  means = gpu.reshape(2, -1, 3).mean(1), ref.reshape(2, -1, 3).mean(1)
+  print(f"4096 spp: relMSE GPU vs oracle (same seed) {same_seed:.3e}, oracle seed 22 vs 21 {noise:.3e}; "
+        f"per-world means GPU {means[0].round(5).tolist()} oracle {means[1].round(5).tolist()}")
+  np.testing.assert_allclose(means[0], means[1], rtol=1e-3)
+  assert same_seed < 0.1 * noise
