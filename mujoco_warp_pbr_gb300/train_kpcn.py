@@ -10,7 +10,9 @@ path-traced passes with other seeds, their HDR summed in FP64 on the device
     python -m mujoco_warp_pbr_gb300.train_kpcn --out weights.npz [--crops 6144 --target-spp 1024 --steps 8000]
 
 The committed weights (weights/kpcn_path.npz) came from --crops 6144 --frame-worlds 256
---target-spp 1024 --steps 8000 --batch 16 --lr 1e-3 --spp 2 --loss-space demod.
+--target-spp 1024 --steps 8000 --batch 16 --lr 1e-3 --spp 2 --loss-space demod, then fine-tuned on
+4096-spp targets: --init <those weights> --crops 2048 --frame-worlds 256 --target-spp 4096
+--steps 4000 --batch 16 --lr 3e-4 --spp 2 --loss-space demod (held-out relMSE 0.0143 -> 0.0141).
 
 prints one JSON line: training time and loss curve, and on held-out scenes the relative MSE
 (mean((x - ref)^2 / (ref^2 + 0.01)) on linear HDR) against 4096-spp references of the learned
