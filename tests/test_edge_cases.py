@@ -1,0 +1,108 @@
+"""Edge cases of the render path, GPU against the oracle (segmentation bit-exact, depth 1e-5, RGB
+within 1/255): a 1 x 1 camera, odd image sizes over many worlds, a world whose geoms are all
+hidden, a scene without lights, a camera inside a sphere, a scene of one plane, and the same
+small cases on the path-traced tier. The oracle side of each case also runs on the CPU."""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from mujoco_warp_pbr_gb300 import synthetic  # noqa: E402
+from mujoco_warp_pbr_gb300.synthetic import GEOM_BOX, GEOM_PLANE, GEOM_SPHERE, LIGHT_DIRECTIONAL, LIGHT_POINT  # noqa: E402
+from tests import helpers  # noqa: E402
+
+GPU = [pytest.mark.gpu, pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")]
+
+
+def _scene(name, build, nworld=1, per_world=None, **options):
+  b = synthetic.Builder()
+  build(b)
+  mjm, mjd = b.build()
+  opts = {"render_rgb": True, "render_depth": True, "render_seg": True, **options}
+  return synthetic.SyntheticScene(name=name, mjm=mjm, mjd=mjd, nworld=nworld, options=opts, per_world=per_world or {}, seed=0)
+
+
+def _basic(b, res=(1, 1), lights=True, target=(0, 0, 0.3)):
+  b.geom(GEOM_PLANE, (2, 2, 0.1), rgba=(0.6, 0.6, 0.6, 1))
+  b.geom(GEOM_SPHERE, (0.3, 0, 0), pos=(0, 0, 0.3), rgba=(0.8, 0.2, 0.2, 1))
+  b.geom(GEOM_BOX, (0.15, 0.15, 0.15), pos=(0.5, 0.2, 0.15), rgba=(0.2, 0.3, 0.9, 1))
+  if lights:
+    b.light(LIGHT_DIRECTIONAL, dir=(0.3, 0.2, -1.0), castshadow=True)
+    b.light(LIGHT_POINT, pos=(-0.5, -0.5, 1.5), bulbradius=0.05, castshadow=True)
+  b.camera((0.2, -2.0, 1.2), target, resolution=res)
+
+
+def _hidden_world(nworld):
+  rgba = np.broadcast_to(np.array([[0.6, 0.6, 0.6, 1], [0.8, 0.2, 0.2, 1], [0.2, 0.3, 0.9, 1]], np.float32), (nworld, 3, 4)).copy()
+  rgba[1, :, 3] = 0.0  # world 1 hides every geom
+  return {"geom_rgba": rgba}
+
+
+def _inside(b):
+  b.geom(GEOM_SPHERE, (1.0, 0, 0), rgba=(0.7, 0.7, 0.2, 1))
+  b.geom(GEOM_BOX, (0.1, 0.1, 0.1), pos=(0.3, 0.0, 0.0), rgba=(0.2, 0.7, 0.2, 1))
+  b.light(LIGHT_POINT, pos=(0, 0, 0.5), castshadow=True)
+  b.camera((0, 0, 0), (1, 0, 0), resolution=(24, 16))
+
+
+def _plane_only(b):
+  b.geom(GEOM_PLANE, (0, 0, 0.1), rgba=(0.5, 0.7, 0.5, 1))
+  b.light(LIGHT_DIRECTIONAL, dir=(0.0, 0.3, -1.0), castshadow=True)
+  b.camera((0, -2.0, 1.0), (0, 0, 0), resolution=(20, 20))
+
+
+CASES = {
+  "pixel_1x1": lambda: _scene("1x1", lambda b: _basic(b, (1, 1)), nworld=3),
+  "odd_sizes_many_worlds": lambda: _scene("odd", lambda b: _basic(b, (37, 5)), nworld=67),
+  "hidden_world": lambda: _scene("hidden", lambda b: _basic(b, (16, 12)), nworld=3, per_world=_hidden_world(3)),
+  "no_lights": lambda: _scene("dark", lambda b: _basic(b, (16, 16), lights=False), nworld=2),
+  "camera_inside_sphere": lambda: _scene("inside", _inside, nworld=2),
+  "plane_only": lambda: _scene("plane", _plane_only, nworld=2),
+}
+
+
+def _compare(gpu, ref):
+  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
+  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
+  diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
+  assert diff.max() <= 1, f"max RGB difference {diff.max()}/255"
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_oracle_renders_edge_case(case):
+  sc = CASES[case]()
+  out = helpers.oracle_render(sc, seed=1)
+  seg = out["seg"][..., 0]
+  if case == "hidden_world":
+    assert np.all(seg[1] == -1) and np.all(out["depth"][1] == 0)
+    assert np.any(seg[0] >= 0)
+  if case == "camera_inside_sphere":
+    # back-face culling (the default) hides the sphere's inner wall: only the box is seen
+    assert not np.any(seg == 0) and np.any(seg == 1)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_realtime_edge_case_matches_oracle(case):
+  sc = CASES[case]()
+  m, d, rc = helpers.gpu_scene(sc)
+  gpu = helpers.render_gpu(m, d, rc, seed=1)
+  ref = helpers.oracle_render(sc, seed=1, tables=helpers.gpu_tables(rc))
+  _compare(gpu, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("case", ["pixel_1x1", "odd_sizes_many_worlds", "hidden_world", "camera_inside_sphere"])
+def test_path_traced_edge_case_matches_oracle(case):
+  sc = CASES[case]()
+  opts = {"tier": 1, "path_samples": 3, "max_depth": 3}
+  m, d, rc = helpers.gpu_scene(sc, **opts)
+  gpu = helpers.render_gpu(m, d, rc, seed=4)
+  ref = helpers.oracle_render(sc, seed=4, tables=helpers.gpu_tables(rc), **opts)
+  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
+  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
+  diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
+  assert float(np.mean(diff <= 1)) >= 0.995
