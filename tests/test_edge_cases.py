@@ -12,9 +12,6 @@ from mujoco_warp_pbr_gb300 import synthetic  # noqa: E402
 from mujoco_warp_pbr_gb300.synthetic import GEOM_BOX, GEOM_PLANE, GEOM_SPHERE, LIGHT_DIRECTIONAL, LIGHT_POINT  # noqa: E402
 from tests import helpers  # noqa: E402
 
-GPU = [pytest.mark.gpu, pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")]
-
-
 def _scene(name, build, nworld=1, per_world=None, **options):
   b = synthetic.Builder()
   build(b)
