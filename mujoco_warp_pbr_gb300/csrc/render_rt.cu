@@ -301,6 +301,78 @@ MJ_DEV void render_pixel(const MjpbrScene& s, uint32_t seed, const float* blk, c
   if (c.err && s.error_word) atomicOr(s.error_word, c.err);
 }
 
+// Four consecutive lanes render the 2 x 2 supersamples of one pixel (sample = lane & 3): the
+// samples of a pixel are nearly the same ray, so a warp's lanes stay on one code path far more
+// often than with 32 pixels per warp (5 % faster on the mesh / IBL workload). The pixel's first lane
+// sums the four results in sample order (warp shuffles), which are the sums of render_pixel's
+// sequential loop, so the images are identical. Every lane of the warp must make the call;
+// `valid` false marks lanes past the image edge.
+template <bool kMesh, bool kTex>
+MJ_DEV void render_pixel_lanes(const MjpbrScene& s, uint32_t seed, const float* blk, const BlockLayout& L, int32_t w,
+                               Pixel& p, bool valid, int32_t smp, const Stack& stack) {
+  const int32_t cam = p.cam;
+  const MjpbrSettings& st = s.settings;
+  RtCtx c;
+  c.st = stack;
+  init_ctx(c, s, blk, L, w, kTex);
+  V3 display = v3(0.0f), hdr = v3(0.0f);
+  if (valid) {
+    p.pixelid = p.py * p.width + p.px;
+    p.rec = blk + L.cam_off + cam * kCamFloats;
+    const M3 R = cam_mat(p.rec);
+    const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
+    const int32_t n = 2;
+    const float inv_n = 1.0f / (float)n;
+    float pixel_spread, pixel_width;
+    pixel_cone(s, p, &pixel_spread, &pixel_width);
+    const float spread = pixel_spread * inv_n, width = pixel_width * inv_n;
+    const V3 head_dir = -V3{R.m[2], R.m[5], R.m[8]};
+    const uint32_t pixel_seed = seed + (uint32_t)w * (uint32_t)s.total_rays + (uint32_t)(s.ray_adr[cam] + p.pixelid);
+    V3 dcam, ocam;
+    float max_dist, depth_z;
+    primary_ray(s, p, n, smp % n, smp / n, &dcam, &ocam, &max_dist, &depth_z);
+    V3 origin = cpos + mul(R, ocam);
+    V3 dir = mul(R, dcam);
+    Hit first;
+    V3 albedo = v3(0.0f), gnormal = v3(0.0f);
+    V3 radiance = Rt<kMesh, kTex>::trace_pixel(c, origin, dir, max_dist, width, spread, head_dir, pixel_seed, 2 * smp,
+                                               &first, &albedo, &gnormal);
+    if (smp == 0) {
+      write_geometry(s, w, p, first, depth_z);
+      if (st.render_guides && s.guide_albedo) {
+        int64_t a = ((int64_t)w * s.rgb_stride + s.rgb_adr[cam] + p.pixelid) * 3;
+        V3 al = first.geom != -1 ? albedo : v3(0.0f), nm = first.geom != -1 ? gnormal : v3(0.0f);
+        s.guide_albedo[a] = al.x;
+        s.guide_albedo[a + 1] = al.y;
+        s.guide_albedo[a + 2] = al.z;
+        s.guide_normal[a] = nm.x;
+        s.guide_normal[a + 1] = nm.y;
+        s.guide_normal[a + 2] = nm.z;
+      }
+    }
+    display = v3(0.0f) + display_transform(radiance * c.exposure, st.tone_mapper);
+    hdr = v3(0.0f) + radiance;
+  }
+  const unsigned full = 0xffffffffu;
+  V3 sd = display, sh = hdr;
+#pragma unroll
+  for (int k = 1; k < 4; ++k) {
+    sd += V3{__shfl_down_sync(full, display.x, k), __shfl_down_sync(full, display.y, k), __shfl_down_sync(full, display.z, k)};
+    sh += V3{__shfl_down_sync(full, hdr.x, k), __shfl_down_sync(full, hdr.y, k), __shfl_down_sync(full, hdr.z, k)};
+  }
+  if (valid && smp == 0) {
+    const int64_t adr = (int64_t)w * s.rgb_stride + s.rgb_adr[cam] + p.pixelid;
+    const float inv_nn = 0.25f;
+    if (st.render_hdr && s.hdr_data) {
+      s.hdr_data[adr * 3] = sh.x * inv_nn;
+      s.hdr_data[adr * 3 + 1] = sh.y * inv_nn;
+      s.hdr_data[adr * 3 + 2] = sh.z * inv_nn;
+    }
+    s.rgb_data[adr] = encode_display(sd * inv_nn);
+  }
+  if (c.err && s.error_word) atomicOr(s.error_word, c.err);
+}
+
 MJ_DEV Stack thread_stack(float* stacks) {
   Stack st;
   int32_t* base = reinterpret_cast<int32_t*>(stacks);
@@ -330,6 +402,27 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   p.width = s.cam_res[cam][0];
   p.height = s.cam_res[cam][1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (s.settings.samples_per_axis == 2 && s.render_rgb[cam] != 0) {
+    // sample lanes: 4 passes of 64 pixels, each warp a 4 x 2 pixel block (ROW tiles of 32 x 8 in
+    // passes of 2 rows, TILED tiles of 16 x 16 in 8 x 8 quadrants)
+    const Stack st = thread_stack(smem + s.world_block_floats);
+    const bool row = s.settings.render_order == MJPBR_ORDER_ROW;
+    const int32_t smp = lane & 3, pix = lane >> 2;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+      Pixel pp = p;
+      if (row) {
+        pp.px = tx * 32 + warp * 4 + (pix & 3);
+        pp.py = ty * 8 + q * 2 + (pix >> 2);
+      } else {
+        pp.px = tx * 16 + (q & 1) * 8 + (warp & 1) * 4 + (pix & 3);
+        pp.py = ty * 16 + (q >> 1) * 8 + (warp >> 1) * 2 + (pix >> 2);
+      }
+      const bool valid = pp.px < pp.width && pp.py < pp.height;
+      render_pixel_lanes<kMesh, kTex>(s, seed, blk, L, w, pp, valid, smp, st);
+    }
+    return;
+  }
   if (s.settings.render_order == MJPBR_ORDER_ROW) {
     p.px = tx * 32 + lane;
     p.py = ty * 8 + warp;
