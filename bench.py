@@ -22,11 +22,12 @@ environment rotation). A step is refit_bvh + render of one frame of every world.
   cpu_baseline  the CPU oracle (scalar C restatement of the reference's real-time tier, OpenMP
              over all host cores) on a bounded sample of the same workload.
 
-Other workloads (--workload): primitives (BASELINE config 1), batched (config 3: 3 cameras of uneven
-size, fisheye bundle, enable masks, autotuned launch shape, one CUDA graph per step), path (the
-path-traced tier as the headline), large_path (config 5: 8192 worlds x 2 cameras x 256², 2 spp,
-learned denoiser, one CUDA graph per frame). The default line also carries path_tier (config 4's
-path tracer) and learned_denoiser (learned 2 spp vs a-trous 16 spp: relative MSE and Mpix/s).
+Other workloads (--workload): primitives (16 worlds x 64², plane + 8 primitives, soft shadows),
+batched (2048 worlds x 3 cameras of 64², 128² and 256², one a fisheye bundle, enable masks,
+autotuned launch shape, one CUDA graph per step), path (the path-traced tier as the headline),
+large_path (8192 worlds x 2 cameras x 256², 2 spp, four environments, learned denoiser, one CUDA
+graph per frame). The default line also carries path_tier (1024 worlds x 128² with emissive quads
+at 2 spp) and learned_denoiser (learned 2 spp vs a-trous 16 spp: relative MSE and Mpix/s).
 
 --impl reference times the reference's own CPU implementation of the path: the reference is
 Python on Warp / MuJoCo Warp (not installable here), so its CPU path is timed through the C
