@@ -732,7 +732,7 @@ def main() -> None:
   p.add_argument("--spp", type=int, default=2)
   p.add_argument("--no-path-tier", action="store_true")
   p.add_argument("--no-learned", action="store_true")
-  # quality against 4096-spp references on 64 worlds, throughput on the C4 batch of 1024 worlds
+  # quality against 4096-spp references on 64 worlds, throughput on the 1024-world path batch
   p.add_argument("--learned-worlds", type=int, default=64)
   p.add_argument("--learned-ref-spp", type=int, default=4096)
   p.add_argument("--learned-time-worlds", type=int, default=1024)
