@@ -2,8 +2,9 @@
  * CPU oracle of the GB300 render path — TEST INFRASTRUCTURE ONLY.
  *
  * A plain scalar C restatement of julien-blanchon/mujoco_warp_pbr's real-time and path-traced
- * tiers and of its context-creation tables. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
- * may load it, as the checker (and, timed, as the CPU baseline); the product never calls it.
+ * tiers and of its context-creation tables. Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline legs may load it, to check the GPU results (and, timed, as the CPU baseline); the
+ * product never calls it.
  *
  * It reads the same MjpbrScene descriptor as libmjpbr (include/mjpbr.h), but with HOST pointers,
  * and it is independent of the CUDA code: no world blocks, no scene BVH (every enabled geom is
