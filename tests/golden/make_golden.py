@@ -2,7 +2,7 @@
 
 The reference ships no golden images (its tests are analytic or relative), so these fixtures pin
 the oracle itself: geometry (segmentation, depth) must reproduce bit for bit on every machine the
-oracle is compiled on (x86-64 here, aarch64 on the GPU machine), colours within 1/255.
+oracle is compiled on (x86-64 or aarch64), colours within 1/255.
 
   python tests/golden/make_golden.py
 """

@@ -1,6 +1,6 @@
 """The reference's analytic known-answer tests (tests/test_render.py, test_ibl.py and
 test_effects.py of mujoco_warp_pbr), restated on array scenes. Each runs on the CPU oracle (pinning
-the oracle itself) and, on a GPU machine, through the public API of the GPU library."""
+the oracle itself) and, on a machine with a GPU, through the public API of the GPU library."""
 
 import numpy as np
 import pytest
