@@ -140,3 +140,30 @@ def test_captured_frame_replays_the_eager_frame(tier):
   assert mjpbr.check_errors(rc) == 0
   for a, b in zip(_outputs(rc), eager):
     np.testing.assert_array_equal(a, b)
+
+
+def test_sample_lane_tiles_cover_each_pixel_once():
+  """The real-time grid kernel's 2 x 2 sample-lane mapping (csrc/render_rt.cu, rt_kernel): over a
+  CTA's 4 passes, 8 warps x 32 lanes visit every pixel of a ROW (32 x 8) or TILED (16 x 16) tile
+  exactly four times, once per sample, and a pixel's four samples sit on four consecutive lanes
+  of one warp (the shuffle reduction's assumption)."""
+  from collections import defaultdict
+
+  for row in (True, False):
+    seen = defaultdict(list)
+    for q in range(4):
+      for warp in range(8):
+        for lane in range(32):
+          pix, smp = lane >> 2, lane & 3
+          if row:
+            px, py = warp * 4 + (pix & 3), q * 2 + (pix >> 2)
+          else:
+            px, py = (q & 1) * 8 + (warp & 1) * 4 + (pix & 3), (q >> 1) * 8 + (warp >> 1) * 2 + (pix >> 2)
+          seen[(px, py)].append((q, warp, lane, smp))
+    w, h = (32, 8) if row else (16, 16)
+    assert set(seen) == {(x, y) for x in range(w) for y in range(h)}
+    for visits in seen.values():
+      assert sorted(v[3] for v in visits) == [0, 1, 2, 3]
+      q, warp, lane0 = visits[0][0], visits[0][1], min(v[2] for v in visits)
+      assert all(v[0] == q and v[1] == warp for v in visits) and lane0 % 4 == 0
+      assert sorted(v[2] for v in visits) == [lane0, lane0 + 1, lane0 + 2, lane0 + 3]
