@@ -424,9 +424,10 @@ int mjpbr_adam(float* param, float* grad, float* m, float* v, uint16_t* copy, ui
  * the library (scene->world_blocks and scene->work_counter are ignored). For hosts that cannot
  * give the library device memory after start-up (a fixed device-memory arena, a plugin host that
  * owns every allocation). Limit: nworld * world_block_floats <= 4,194,304 (16 MiB), else
- * MJPBR_ERR_ARG. Calls overlapping in time share the static memory and race. The first call on a
- * device looks the memory up; make it before any stream capture. No counterpart in the
- * reference. */
+ * MJPBR_ERR_ARG. Calls overlapping in time share the static memory and race. The memory belongs
+ * to the current device: a stream of another device is rejected with MJPBR_ERR_ARG. The first
+ * call on a device (and the first after its context was re-created) looks the memory up; make it
+ * before any stream capture. No counterpart in the reference. */
 int mjpbr_refit_render_static(const MjpbrScene* scene, uint32_t seed, void* stream);
 
 /* Display RGB in [0, 1] of rendering camera `cam` into out (nworld_out, H, W, 3) float32.

@@ -23,6 +23,7 @@ from mujoco_warp_pbr_gb300.output import get_hdr as get_hdr
 from mujoco_warp_pbr_gb300.output import get_normal as get_normal
 from mujoco_warp_pbr_gb300.output import get_rgb as get_rgb
 from mujoco_warp_pbr_gb300.output import get_segmentation as get_segmentation
+from mujoco_warp_pbr_gb300.rays import CameraRays as CameraRays
 from mujoco_warp_pbr_gb300.rays import set_camera_rays as set_camera_rays
 from mujoco_warp_pbr_gb300.render import check_errors as check_errors
 from mujoco_warp_pbr_gb300.render import denoise as denoise
@@ -37,6 +38,7 @@ from mujoco_warp_pbr_gb300.pbr_types import ToneMapper as ToneMapper
 from mujoco_warp_pbr_gb300.pbr_types import UnsetMaterial as UnsetMaterial
 
 __all__ = [
+  "CameraRays",
   "Data",
   "HostData",
   "HostModel",
@@ -47,8 +49,11 @@ __all__ = [
   "Tier",
   "ToneMapper",
   "UnsetMaterial",
+  "autotune",
+  "capture_frame",
   "check_errors",
   "create_render_context",
+  "denoise",
   "get_albedo",
   "get_depth",
   "get_hdr",
@@ -62,4 +67,5 @@ __all__ = [
   "render",
   "resolve_geom_materials",
   "scene_descriptor",
+  "set_camera_rays",
 ]

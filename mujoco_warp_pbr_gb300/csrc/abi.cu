@@ -1,5 +1,6 @@
 // C entry points of libmjpbr (declared in include/mjpbr.h): argument checks, error reporting and
 // dispatch to the kernel launchers. Nothing here synchronises or allocates.
+#include <atomic>
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
@@ -28,6 +29,26 @@ int check_launch(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
   return MJPBR_OK;
+}
+
+namespace {
+
+constexpr int kMaxSmDevices = 64;
+std::atomic<int> g_device_sms[kMaxSmDevices];
+
+}  // namespace
+
+int device_sm_count() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (dev >= 0 && dev < kMaxSmDevices) {
+    const int cached = g_device_sms[dev].load(std::memory_order_relaxed);
+    if (cached > 0) return cached;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+  if (dev >= 0 && dev < kMaxSmDevices) g_device_sms[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 namespace {

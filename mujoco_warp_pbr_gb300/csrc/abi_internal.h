@@ -12,6 +12,9 @@ int set_error(int code, const char* fmt, ...);
 // MJPBR_OK, or MJPBR_ERR_CUDA with the launch error of the last kernel.
 int check_launch(const char* what);
 
+// Streaming multiprocessors of the current device (looked up once per device, thread-safe).
+int device_sm_count();
+
 // MJPBR_OK, or MJPBR_ERR_ARG with a message naming the first inconsistent field of the scene.
 int validate_scene(const MjpbrScene* s, bool need_outputs);
 

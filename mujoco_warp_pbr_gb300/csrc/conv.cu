@@ -631,17 +631,7 @@ namespace {
 #endif
 constexpr size_t kPipeSmemBudget = MJPBR_CONV_SMEM_BUDGET;
 constexpr size_t kPipeSmemMax = 220 * 1024;
-int g_conv_sms = 0;
-
-int conv_sm_count() {
-  if (g_conv_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_conv_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_conv_sms <= 0) g_conv_sms = 1;
-  }
-  return g_conv_sms;
-}
+int conv_sm_count() { return device_sm_count(); }
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);

@@ -406,21 +406,13 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
-int g_sm_count = 0;
-
 template <bool kMesh, bool kTex>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const PtTiles& tm, cudaStream_t stream) {
   size_t smem = (size_t)s.world_block_floats * sizeof(float) + (size_t)kThreads * kStackDepth * 8;
   auto kern = pt_kernel<kMesh, kTex>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path tracer: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
-  if (g_sm_count == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sm_count <= 0) g_sm_count = 1;
-  }
-  int grid = std::min(tm.total, g_sm_count * 2);
+  int grid = std::min(tm.total, device_sm_count() * 2);
   e = cudaMemsetAsync(s.work_counter, 0, 4 * sizeof(int32_t), stream);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path tracer: work counter: %s", cudaGetErrorString(e));
   kern<<<grid, kThreads, smem, stream>>>(s, seed, tm);

@@ -493,18 +493,6 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_queue_kernel
   }
 }
 
-int g_sm_count = 0;
-
-int sm_count() {
-  if (g_sm_count == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sm_count <= 0) g_sm_count = 1;
-  }
-  return g_sm_count;
-}
-
 // Largest dynamic shared memory a CTA may use while MJPBR_RT_MIN_BLOCKS CTAs stay resident.
 constexpr size_t kSmemPerSm = 228 * 1024;
 constexpr size_t kQueueSmemLimit = kSmemPerSm / MJPBR_RT_MIN_BLOCKS - 2048;
@@ -538,7 +526,7 @@ int launch_queue_variant(const MjpbrScene& s, uint32_t seed, const QueueMap& qm,
   }
   cudaError_t e = cudaMemsetAsync(s.work_counter + 1, 0, sizeof(int32_t), stream);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render queue: work counter: %s", cudaGetErrorString(e));
-  const int grid = std::min(qm.total, sm_count() * MJPBR_RT_MIN_BLOCKS);
+  const int grid = std::min(qm.total, device_sm_count() * MJPBR_RT_MIN_BLOCKS);
   kern<<<grid, kThreads, smem, stream>>>(s, seed, qm);
   return check_launch("rt_queue_kernel");
 }

@@ -11,8 +11,10 @@
 // Limits: the blocks of all worlds must fit kStaticBlockFloats floats (16 MiB), i.e.
 // nworld * world_block_floats <= 4,194,304, else the call fails with MJPBR_ERR_ARG before any
 // work. The static buffers are shared by every call in the process on a device: calls that
-// overlap in time (two streams, or two host threads without ordering) race on them. The first
-// call on each device looks the buffers up (cudaGetSymbolAddress), so make that first call before
+// overlap in time (two streams, or two host threads without ordering) race on them. The buffers
+// belong to the current device, so the stream must be one of that device (else MJPBR_ERR_ARG).
+// The first call on each device (and the first after that device's context was re-created, e.g.
+// by cudaDeviceReset) looks the buffers up with cudaGetSymbolAddress, so make that call before
 // any stream capture.
 #include <mutex>
 
@@ -27,29 +29,66 @@ constexpr int kMaxDevices = 64;
 __device__ __align__(256) float g_static_blocks[kStaticBlockFloats];
 __device__ __align__(256) int32_t g_static_counter[4];
 
-std::mutex g_lookup_mutex;
-float* g_blocks[kMaxDevices];
-int32_t* g_counter[kMaxDevices];
+using CtxGetCurrentFn = int (*)(void**);
 
-// Device addresses of the static buffers on the current device (looked up once per device).
-int static_scratch(float** blocks, int32_t** counter) {
+// cuCtxGetCurrent through the runtime's driver entry point (no link against libcuda).
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      f = nullptr;
+    }
+    return reinterpret_cast<CtxGetCurrentFn>(f);
+  }();
+  return fn;
+}
+
+struct DeviceScratch {
+  void* ctx;  // the context the addresses below were looked up in
+  float* blocks;
+  int32_t* counter;
+};
+
+std::mutex g_lookup_mutex;
+DeviceScratch g_scratch[kMaxDevices];
+
+// Device addresses of the static buffers on the current device, looked up again whenever the
+// device's current context differs from the one of the cached addresses (a module reloaded after
+// a context was destroyed and re-created may place the buffers elsewhere).
+int static_scratch(cudaStream_t stream, float** blocks, int32_t** counter) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return set_error(MJPBR_ERR_ARG, "device %d beyond the %d supported", dev, kMaxDevices);
+  if (stream) {
+    int sdev = -1;
+    e = cudaStreamGetDevice(stream, &sdev);
+    if (e != cudaSuccess) return set_error(MJPBR_ERR_ARG, "stream: %s", cudaGetErrorString(e));
+    if (sdev != dev) {
+      return set_error(MJPBR_ERR_ARG, "the stream belongs to device %d but device %d is current: the static scratch is per device", sdev,
+                       dev);
+    }
+  }
+  void* ctx = nullptr;
+  CtxGetCurrentFn get = ctx_get_current();
+  if (!get || get(&ctx) != 0 || !ctx) return set_error(MJPBR_ERR_CUDA, "no current CUDA context on device %d", dev);
   std::lock_guard<std::mutex> lock(g_lookup_mutex);
-  if (!g_blocks[dev]) {
+  DeviceScratch& d = g_scratch[dev];
+  if (d.ctx != ctx || !d.blocks) {
     void* b = nullptr;
     void* c = nullptr;
     e = cudaGetSymbolAddress(&b, g_static_blocks);
     if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "static world blocks: %s", cudaGetErrorString(e));
     e = cudaGetSymbolAddress(&c, g_static_counter);
     if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "static work counter: %s", cudaGetErrorString(e));
-    g_counter[dev] = static_cast<int32_t*>(c);
-    g_blocks[dev] = static_cast<float*>(b);
+    d.blocks = static_cast<float*>(b);
+    d.counter = static_cast<int32_t*>(c);
+    d.ctx = ctx;
   }
-  *blocks = g_blocks[dev];
-  *counter = g_counter[dev];
+  *blocks = d.blocks;
+  *counter = d.counter;
   return MJPBR_OK;
 }
 
@@ -65,11 +104,11 @@ extern "C" int mjpbr_refit_render_static(const MjpbrScene* scene, uint32_t seed,
                      (long long)kStaticBlockFloats, (long long)need, scene->nworld, scene->world_block_floats);
   }
   MjpbrScene s = *scene;
-  int rc = static_scratch(&s.world_blocks, &s.work_counter);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = static_scratch(st, &s.world_blocks, &s.work_counter);
   if (rc) return rc;
   rc = validate_scene(&s, true);
   if (rc) return rc;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   rc = refit_launch(s, st);
   if (rc) return rc;
   // render_pt_launch zeroes the work counter on the stream before its kernel starts

@@ -15,6 +15,12 @@ from typing import Any
 import numpy as np
 import torch
 
+# Rays of every rendering camera: an array (nrender, height, width, 2, 3) when the cameras share a
+# resolution, or one (height, width, 2, 3) array per rendering camera (NumPy or float32 torch);
+# [..., 0, :] is the camera-frame origin, [..., 1, :] the direction (the reference's CameraRays
+# alias, _src/rays.py:33-37).
+CameraRays = np.ndarray | torch.Tensor | Sequence[np.ndarray | torch.Tensor]
+
 
 def _images(camera_rays: Any) -> list[Any]:
   """The rays as one (height, width, 2, 3) array per camera (NumPy or torch)."""

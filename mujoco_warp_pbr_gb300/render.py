@@ -324,7 +324,8 @@ def render(m: Any, d: Any, rc: PbrRenderContext, seed: int = 0, denoise: bool = 
   tier, one persistent kernel for the path-traced tier). The image is a deterministic function of
   the seed. The per-world blocks come from the last refit_bvh; the first render of a context
   refits once itself. A path-traced context created with denoise=True then runs the a-trous
-  filter (render.py:431-470); denoise=False leaves the noisy image and the filter's inputs for a
+  filter (the reference's _src/render.py:431-460 dispatch and _src/pathtrace.py:426-438);
+  denoise=False leaves the noisy image and the filter's inputs for a
   later denoise() call."""
   s = scene(m, d, rc)
   stream = _stream(rc)

@@ -21,10 +21,7 @@ def test_primitive_scene_matches_oracle(seed, shadow_samples):
   m, d, rc = helpers.gpu_scene(sc, render_hdr=True)
   gpu = helpers.render_gpu(m, d, rc, seed=7)
   ref = helpers.oracle_render(sc, seed=7, tables=helpers.gpu_tables(rc), render_hdr=True)
-  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
-  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
-  diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
-  assert diff.max() <= 1, f"max RGB difference {diff.max()}/255 at {np.argwhere(diff > 1)[:5]}"
+  _assert_realtime_parity(gpu, ref, f"primitives 4 x 48^2 seed {seed} shadow samples {shadow_samples}")
   np.testing.assert_allclose(gpu["hdr"], ref["hdr"], rtol=2e-3, atol=1e-3 * float(np.abs(ref["hdr"]).max()))
 
 
@@ -76,19 +73,50 @@ def test_dfg_table_matches_oracle():
   assert mjpbr.check_errors(rc) == 0
 
 
+def _assert_realtime_parity(gpu, ref, what):
+  """The real-time bars: segmentation bit-exact, depth within 1e-5 relative, every RGB channel of
+  every pixel within 1/255 (the reference's own render tests hold segmentation exact and depth to
+  1e-4 / 1e-5: tests/test_render.py:149-188)."""
+  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
+  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
+  diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
+  print(f"{what}: max RGB diff {diff.max()}/255, {int((diff > 0).sum())} of {diff.size} pixels differ at all")
+  assert diff.max() <= 1, f"{what}: max RGB difference {diff.max()}/255 at {np.argwhere(diff > 1)[:5]}"
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_primitive_config_exact_size_matches_oracle(seed):
+  """The plain real-time configuration at its own size: 16 worlds x 64x64, one directional and one
+  point light (bulb radius 0.05), soft shadows with 4 samples, flat grey sky."""
+  sc = synthetic.primitive_scene(seed=seed, nworld=16, res=64, shadow_samples=4)
+  assert sc.mjm.nlight == 2 and sc.options["cam_res"] == (64, 64)
+  m, d, rc = helpers.gpu_scene(sc)
+  gpu = helpers.render_gpu(m, d, rc, seed=seed + 1)
+  ref = helpers.oracle_render(sc, seed=seed + 1, tables=helpers.gpu_tables(rc))
+  _assert_realtime_parity(gpu, ref, f"primitives 16 x 64^2 seed {seed}")
+
+
 @pytest.mark.parametrize("seed", [0, 5])
 def test_mesh_ibl_scene_matches_oracle(seed):
-  """Meshes, textures with mips, IBL, 2x2 supersampling and the mirror floor."""
+  """Meshes, textures with mips, IBL, 2x2 supersampling and the mirror floor (small assets)."""
   sc = synthetic.mesh_ibl_scene(seed=seed, nworld=2, res=48, tex_size=64, env_width=128)
   m, d, rc = helpers.gpu_scene(sc, render_hdr=True)
   gpu = helpers.render_gpu(m, d, rc, seed=3)
   ref = helpers.oracle_render(sc, seed=3, tables=helpers.gpu_tables(rc), render_hdr=True)
-  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
-  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
-  diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
-  frac = float(np.mean(diff <= 1))
-  print(f"mesh/IBL RGB: max diff {diff.max()}/255, {frac:.5f} of pixels within 1/255")
-  assert frac >= 0.999 and diff.max() <= 8
+  _assert_realtime_parity(gpu, ref, f"mesh/IBL small assets seed {seed}")
+
+
+@pytest.mark.parametrize("seed", [0, 5])
+def test_mesh_ibl_config_full_assets_matches_oracle(seed):
+  """The mesh / IBL configuration at its own asset sizes and resolution on 4 worlds: six displaced
+  icospheres of 5120 triangles, ten primitives, 512x512 albedo / ORM / normal maps with full mip
+  chains, a 1024x512 environment, 128x128 cameras, 2x2 supersampling, mirror floor 0.3."""
+  sc = synthetic.mesh_ibl_scene(seed=seed, nworld=4, res=128)
+  assert sc.mjm.nmesh == 6 and sc.options["cam_res"] == (128, 128) and sc.options["samples_per_pixel"] == 2
+  m, d, rc = helpers.gpu_scene(sc)
+  gpu = helpers.render_gpu(m, d, rc, seed=seed + 4)
+  ref = helpers.oracle_render(sc, seed=seed + 4, tables=helpers.gpu_tables(rc))
+  _assert_realtime_parity(gpu, ref, f"mesh/IBL 4 x 128^2 full assets seed {seed}")
 
 
 def test_texture_mips_and_prefilter_match_oracle():

@@ -111,8 +111,9 @@ def _assert_path_parity(gpu, ref):
   np.testing.assert_array_equal(gpu["seg"], ref["seg"])
   np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
   diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
-  frac = float((diff <= 1).mean())
-  assert frac >= 0.995, f"{100 * (1 - frac):.2f}% of pixels differ by more than 1/255 (max {diff.max()})"
+  # every pixel within 1/255: the paths take the same decisions on both sides (no allowance for
+  # diverging paths; HDR values may differ in the last bits where shading uses fused arithmetic)
+  assert diff.max() <= 1, f"{int((diff > 1).sum())} pixels differ by more than 1/255 (max {diff.max()}) at {np.argwhere(diff > 1)[:5]}"
   mean_err = float(np.abs(gpu["hdr"] - ref["hdr"]).mean())
   assert mean_err <= 0.01 * float(np.abs(ref["hdr"]).mean()) + 1e-6
 

@@ -1,5 +1,13 @@
-"""mjpbr_refit_render_static: refit + render with library-owned static scratch (no allocation),
-called through the C ABI and compared with the allocating entry points on the same scene.
+"""mjpbr_refit_render_static: refit + render for callers that cannot allocate device memory after
+start-up (a host that runs inside a fixed device-memory arena, or a plugin whose host owns every
+allocation). The call keeps the per-world blocks and the work counter in the library's own static
+device memory; the test calls it through the C ABI and compares it with the allocating entry
+points on the same scene, twice in a row.
+
+The caller's own world blocks are filled with NaN and both scratch pointers are left out of the
+descriptor before the static call, so the images can only match if the static memory is what the
+kernels read. The queue schedule of the real-time tier (work counter slot 1) and the path tier
+(slot 0) both run through it.
 
 Collected last (file name) so it also runs after every other GPU test in one process."""
 
@@ -21,30 +29,45 @@ def _outputs(rc):
   )
 
 
-@pytest.mark.parametrize("tier", [0, 1])
-def test_static_scratch_matches_allocating_path(tier):
+@pytest.mark.parametrize(
+  "opts",
+  [
+    {},
+    {"schedule": "queue", "queue_item": 64},
+    {"tier": 1, "path_samples": 3, "max_depth": 3},
+  ],
+  ids=["realtime_grid", "realtime_queue", "path"],
+)
+def test_static_scratch_matches_allocating_path(opts):
   import mujoco_warp_pbr_gb300 as mjpbr
   from mujoco_warp_pbr_gb300 import _lib, synthetic
   from tests import helpers
 
   sc = synthetic.primitive_scene(seed=4, nworld=6, res=40)
-  opts = {"tier": tier, "path_samples": 3, "max_depth": 3} if tier == 1 else {}
   m, d, rc = helpers.gpu_scene(sc, **opts)
   mjpbr.refit_bvh(m, d, rc)
   mjpbr.render(m, d, rc, seed=5)
   torch.cuda.synchronize()
   ref = _outputs(rc)
   lib = _lib.load()
-  s = mjpbr.scene_descriptor(m, d, rc)
+  s = _lib.Scene.from_buffer_copy(mjpbr.scene_descriptor(m, d, rc))  # a copy: the cached one stays intact
+  s.world_blocks = None
+  s.work_counter = None
   stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
   for _ in range(2):
+    rc.world_blocks.fill_(float("nan"))
+    rc.work_counter.fill_(12345)
     for t in (rc.base.rgb_data, rc.base.depth_data, rc.base.seg_data):
       t.zero_()
+    torch.cuda.synchronize()
     assert lib.mjpbr_refit_render_static(ctypes.byref(s), 5, stream) == 0, lib.mjpbr_last_error().decode()
     torch.cuda.synchronize()
     got = _outputs(rc)
     for a, b in zip(got, ref):
       np.testing.assert_array_equal(a, b)
+    # the caller's scratch was not touched
+    assert bool(torch.isnan(rc.world_blocks).all())
+    assert bool((rc.work_counter == 12345).all())
   assert mjpbr.check_errors(rc) == 0
 
 
