@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define MJPBR_ABI_VERSION 1
+#define MJPBR_ABI_VERSION 2
 
 /* Most rendering cameras of one context (the per-camera tables below are inline). */
 #define MJPBR_MAX_RENDER 16
@@ -77,10 +77,12 @@ enum MjpbrToneMapper { MJPBR_TONE_PBR_NEUTRAL = 0, MJPBR_TONE_ACES = 1, MJPBR_TO
 enum MjpbrLightModel { MJPBR_LIGHT_MODEL_PHYSICAL = 0, MJPBR_LIGHT_MODEL_MUJOCO = 1 };
 enum MjpbrTier { MJPBR_TIER_REALTIME = 0, MJPBR_TIER_PATH = 1 };
 enum MjpbrRenderOrder { MJPBR_ORDER_ROW = 0, MJPBR_ORDER_TILED = 1, MJPBR_ORDER_WORLD = 2 };
-/* Real-time tier schedules: one CTA per (camera tile, world), or a persistent launch whose warps
+/* Real-time tier schedules: one CTA per (camera tile, world); a persistent launch whose warps
  * pull work items (settings.queue_item pixels of one camera image of one world) from a device
- * counter (scene.work_counter[1]). */
-enum MjpbrSchedule { MJPBR_SCHEDULE_GRID = 0, MJPBR_SCHEDULE_QUEUE = 1 };
+ * counter (scene.work_counter[1]); or a staged wavefront (primary rays, surfaces, mirror rays,
+ * shadow rays and shading as separate kernels over compacted ray queues, chunks of worlds at a
+ * time in scene.wave_scratch; not for translucent layers). All three render identical images. */
+enum MjpbrSchedule { MJPBR_SCHEDULE_GRID = 0, MJPBR_SCHEDULE_QUEUE = 1, MJPBR_SCHEDULE_WAVEFRONT = 2 };
 /* Texel formats of MjpbrTexture. */
 enum MjpbrTexFormat { MJPBR_TEX_RGBA8 = 0, MJPBR_TEX_RGBA16F = 1 };
 
@@ -331,6 +333,8 @@ typedef struct MjpbrScene {
   int32_t* error_word;             /* device int32, kernels OR error bits into it (may be NULL) */
   int32_t* work_counter;           /* device int32[4] scratch of the persistent kernels' work queues
                                       (the library zeroes it on the stream before each use) */
+  void* wave_scratch;              /* wavefront schedule: device scratch, 256-byte aligned (NULL otherwise) */
+  int64_t wave_scratch_bytes;      /* its size; mjpbr_wave_scratch_bytes gives the size for a chunk of worlds */
 
   MjpbrSettings settings;
 } MjpbrScene;
@@ -349,6 +353,12 @@ void mjpbr_struct_layout(int64_t out[8]);
 
 /* Size in floats of one world's block for a scene with these counts (used to size world_blocks). */
 int32_t mjpbr_world_block_floats(int32_t nbvh_geom, int32_t nnode, int32_t nlight, int32_t nrender);
+
+/* Bytes of wave_scratch the wavefront schedule needs to render `worlds` worlds per chunk of
+ * this scene (more scratch, fewer chunks; the whole frame in one chunk with worlds = nworld),
+ * or -1. Host only; reads the scene's counts and settings, no device pointer. New with the
+ * wavefront schedule (the reference renders every world in one megakernel launch). */
+int64_t mjpbr_wave_scratch_bytes(const MjpbrScene* scene, int32_t worlds);
 
 /* Per-geom world AABBs from the current poses, bottom-up refit of every world's scene BVH, and the
  * per-world blocks (geom, light, camera records and BVH nodes) the render kernels stage into
@@ -421,7 +431,8 @@ int mjpbr_adam(float* param, float* grad, float* m, float* v, uint16_t* copy, ui
 
 /* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
  * caller: the per-world blocks and the path tracer's work counter live in static device memory of
- * the library (scene->world_blocks and scene->work_counter are ignored). For hosts that cannot
+ * the library (scene->world_blocks, scene->work_counter and scene->wave_scratch are ignored; the
+ * wavefront schedule renders as the grid schedule, with the same images). For hosts that cannot
  * give the library device memory after start-up (a fixed device-memory arena, a plugin host that
  * owns every allocation). Limit: nworld * world_block_floats <= 4,194,304 (16 MiB), else
  * MJPBR_ERR_ARG. Calls overlapping in time share the static memory and race. The memory belongs

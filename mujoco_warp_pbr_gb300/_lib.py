@@ -12,7 +12,7 @@ import threading
 from pathlib import Path
 
 LIBRARY = Path(__file__).resolve().parent / "libmjpbr.so"
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_RENDER = 16
 NTEXROLE = 10
 MAX_MIPS = 15
@@ -243,6 +243,8 @@ class Scene(ctypes.Structure):
     # status
     ("error_word", c_vp),
     ("work_counter", c_vp),
+    ("wave_scratch", c_vp),
+    ("wave_scratch_bytes", ctypes.c_int64),
     ("settings", Settings),
   ]
 
@@ -297,6 +299,7 @@ _SIGNATURES = {
   "mjpbr_last_error": (ctypes.c_char_p, []),
   "mjpbr_struct_layout": (None, [ctypes.POINTER(ctypes.c_int64)]),
   "mjpbr_world_block_floats": (c_i32, [c_i32, c_i32, c_i32, c_i32]),
+  "mjpbr_wave_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(Scene), c_i32]),
   "mjpbr_refit_bvh": (ctypes.c_int, [ctypes.POINTER(Scene), c_vp]),
   "mjpbr_render": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),
   "mjpbr_refit_render_static": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.c_uint32, c_vp]),

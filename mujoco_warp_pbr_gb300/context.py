@@ -72,17 +72,18 @@ def _enum(cls: type[enum.IntEnum], value: int, name: str) -> enum.IntEnum:
     raise ValueError(f"{name} must be one of {options}, got {value!r}") from None
 
 
-SCHEDULES = {"grid": 0, "queue": 1}
+SCHEDULES = {"grid": 0, "queue": 1, "wavefront": 2}
 
 
 def _schedule(schedule: str | int) -> int:
-  """The real-time tier's schedule: "grid" (one CTA per camera tile and world) or "queue" (a
-  persistent launch whose warps pull work items from a device counter)."""
+  """The real-time tier's schedule: "grid" (one CTA per camera tile and world), "queue" (a
+  persistent launch whose warps pull work items from a device counter) or "wavefront" (primary,
+  mirror and shadow rays and the shading as separate kernels over compacted ray queues)."""
   if isinstance(schedule, str) and schedule in SCHEDULES:
     return SCHEDULES[schedule]
   if not isinstance(schedule, str) and int(schedule) in SCHEDULES.values():
     return int(schedule)
-  raise ValueError(f'schedule must be "grid" or "queue", got {schedule!r}')
+  raise ValueError(f'schedule must be "grid", "queue" or "wavefront", got {schedule!r}')
 
 
 def _check_at_least(name: str, value: int, low: int) -> None:
@@ -632,6 +633,7 @@ def prepare_context(
   block_dim: int | None = None,
   schedule: str | int = "grid",
   queue_item: int = 64,
+  wave_chunk_worlds: int = 0,
   max_registers: int | None = None,
   mesh_bvh_constructor: str = "cubql",
   mesh_bvh_frame: str = "auto",
@@ -677,6 +679,7 @@ def prepare_context(
   schedule = _schedule(schedule)
   if queue_item not in (32, 64, 128):
     raise ValueError(f"queue_item must be 32, 64 or 128 pixels, got {queue_item}")
+  _check_at_least("wave_chunk_worlds", wave_chunk_worlds, 0)
   if mesh_bvh_frame not in _MESH_BVH_FRAMES:
     raise ValueError(f'mesh_bvh_frame must be "auto" or "mujoco", got {mesh_bvh_frame!r}')
   if mesh_bvh_constructor not in _MESH_BVH_CONSTRUCTORS:
@@ -895,6 +898,7 @@ def prepare_context(
     "render_order": int(render_order),
     "schedule": int(schedule),
     "queue_item": int(queue_item),
+    "wave_chunk_worlds": int(wave_chunk_worlds),
     "tier": int(tier),
     "path_samples": int(path_samples),
     "max_depth": int(max_depth),
@@ -968,7 +972,10 @@ def create_render_context(mjm: Any, nworld: int = 1, **kwargs: Any) -> PbrRender
 
   Keyword arguments, defaults and errors are those of mujoco_warp_pbr.create_render_context
   (mujoco_warp_pbr/_src/io.py:331-504), plus `data`: the host data (HostData) the scene BVH
-  topology is built from (default: every geom at the origin, refit each frame). block_dim,
+  topology is built from (default: every geom at the origin, refit each frame); `schedule`, the
+  real-time tier's launch: "grid", "queue" (with `queue_item` pixels per work item) or
+  "wavefront" (staged kernels over ray queues; `wave_chunk_worlds` worlds per chunk of its
+  scratch, 0: about 16 M samples per chunk); all render the same images. block_dim,
   max_registers, ordered_traversal, use_fast_math, mesh_bvh_constructor and mesh_bvh_frame are
   validated and recorded; the GB300 kernels choose their own launch shapes and traversal.
 
@@ -1055,6 +1062,7 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     render_order=op["render_order"],
     schedule=op["schedule"],
     queue_item=op["queue_item"],
+    wave_chunk_worlds=op["wave_chunk_worlds"],
     tier=op["tier"],
     path_samples=op["path_samples"],
     max_depth=op["max_depth"],

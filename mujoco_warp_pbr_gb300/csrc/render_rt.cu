@@ -14,7 +14,7 @@
 #include <climits>
 
 #include "abi_internal.h"
-#include "kernel_common.cuh"
+#include "rt_shade.cuh"
 
 namespace mjpbr {
 namespace {
@@ -25,122 +25,39 @@ constexpr int kThreads = 256;
 #define MJPBR_RT_MIN_BLOCKS 2
 #endif
 constexpr float kMinThroughput = 1.0f / 255.0f;
-constexpr float kMinTexels = 1.0e-8f;
+
+// Shadow visibility of the megakernel: the shadow rays are traced where the shading asks.
+template <bool kMesh>
+struct TracedVis {
+  MJ_DEV float visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist, uint32_t seed, int32_t stream,
+                          int32_t nlight, int32_t li) {
+    const MjpbrSettings& st = c.s->settings;
+    const V3 origin = point + normal * kRayOffset;
+    const int32_t nray = shadow_ray_count(light, st.shadow_samples);
+    const bool cull = st.cull_backfaces != 0;
+    int32_t visible = 0;
+    for (int32_t k = 0; k < nray; ++k) {
+      Ray r;
+      float max_dist;
+      r.o = origin;
+      shadow_ray(light, st.shadow_samples, origin, l, dist, seed, stream, nlight, li, k, &r.d, &max_dist);
+      if (trace_ray<kMesh>(*c.s, c.st, c.blk, c.L, r, max_dist, cull, true, &c.err).geom == -1) ++visible;
+    }
+    return visible_fraction(light, st.shadow_samples, visible, st.shadow_light_fraction);
+  }
+};
 
 template <bool kMesh, bool kTex>
 struct Rt {
-  static MJ_DEV bool occluded(RtCtx& c, V3 o, V3 d, float max_dist) {
-    Ray r{o, d};
-    return trace_ray<kMesh>(*c.s, c.st, c.blk, c.L, r, max_dist, c.s->settings.cull_backfaces != 0, true, &c.err).geom != -1;
-  }
+  using Shade = RtShade<kTex, TracedVis<kMesh>>;
 
-  // Fraction of the light reaching the point (render.py:81-127).
-  static MJ_DEV float light_visibility(RtCtx& c, const Light& light, V3 point, V3 normal, V3 l, float dist,
-                                       uint32_t seed, int32_t stream, int32_t nlight, int32_t li) {
-    const MjpbrSettings& st = c.s->settings;
-    V3 origin = point + normal * kRayOffset;
-    if (light.type == MJPBR_LIGHT_DIRECTIONAL) {
-      return occluded(c, origin, l, kUnboundedShadow) ? st.shadow_light_fraction : 1.0f;
-    }
-    if (st.shadow_samples <= 1) {
-      return occluded(c, origin, l, dist - kShadowGap) ? st.shadow_light_fraction : 1.0f;
-    }
-    V3 t1, t2;
-    orthonormal_basis(l, &t1, &t2);
-    float visible = 0.0f;
-    const int32_t ns = st.shadow_samples;
-    for (int32_t k = 0; k < ns; ++k) {
-      uint32_t counter = (uint32_t)(((stream * nlight + li) * ns + k) * 2);
-      float u0 = rand01(seed, counter), u1 = rand01(seed, counter + 1u);
-      float r = light.bulbradius * sqrtf(u0);
-      float sn, cs;
-      sincos_turns(u1, &sn, &cs);
-      V3 to = light.pos + (t1 * cs + t2 * sn) * r - origin;
-      float d = length(to);
-      if (!occluded(c, origin, to / d, d - kShadowGap)) visible += 1.0f;
-    }
-    float v = visible / (float)ns;
-    return v + (1.0f - v) * st.shadow_light_fraction;
-  }
-
-  static MJ_DEV V3 shade_light(RtCtx& c, const Light& light, const Lobes& lb, V3 point, V3 normal, V3 view, float nov,
-                               uint32_t seed, int32_t stream, int32_t nlight, int32_t li) {
-    const MjpbrSettings& st = c.s->settings;
-    V3 l, ds, ss;
-    float dist;
-    MJPBR_COUNT(kOpLight);
-    eval_light(light, st.light_model, point, &l, &dist, &ds, &ss);
-    float nol = dot(normal, l);
-    if (nol <= 0.0f || (length_sq(ds) == 0.0f && length_sq(ss) == 0.0f)) return v3(0.0f);
-    float vis = 1.0f;
-    if (st.use_shadows && light.castshadow) vis = light_visibility(c, light, point, normal, l, dist, seed, stream, nlight, li);
-    V3 h = fnormalize(l + view);
-    float noh = fmaxf(fdot(normal, h), 0.0f);
-    float loh = fmaxf(fdot(l, h), 0.0f);
-    V3 fr = cmul(specular_lobe(lb.f0, lb.alpha, noh, nov, nol, loh), lb.energy_comp);
-    V3 fd = lb.diffuse_color * (1.0f / kPi);
-    return (cmul(fd, ds) + cmul(fr, ss)) * (nol * vis);
-  }
-
-  // Outgoing radiance towards view, before exposure (render.py:184-239).
   static MJ_DEV V3 shade_surface(RtCtx& c, const Surface& sf, V3 point, V3 normal, V3 view, V3 head_dir, uint32_t seed,
                                  int32_t stream) {
-    const MjpbrScene& s = *c.s;
-    const MjpbrSettings& st = s.settings;
-    float nov = fmaxf(fdot(normal, view), 1.0e-4f);
-    MJPBR_COUNT(kOpShade);
-    Lobes lb = shading_lobes(s.dfg_lut, s.dfg_size, sf, nov);
-    V3 irradiance = c.ambient, prefiltered = c.ambient;
-    if (kTex && st.has_env) {
-      MJPBR_COUNT(kOpEnv);
-      irradiance = c.ambient + eval_sh9(s.env_sh + c.env * 27, rotate_yaw(normal, -c.env_yaw)) * c.env_scale;
-      V3 r = view - normal * (2.0f * fdot(view, normal));
-      float a2 = lb.alpha * lb.alpha;
-      V3 dominant = fnormalize(-r * (1.0f - a2) + normal * a2);
-      const uint16_t* stack = s.env_prefiltered +
-                              (int64_t)c.env * s.prefilter_levels * s.prefilter_height * s.prefilter_width * 4;
-      V3 blurred = sample_prefiltered(stack, s.prefilter_levels, s.prefilter_height, s.prefilter_width, dominant,
-                                      c.env_yaw, lb.pr);
-      float t = lb.pr * ((float)s.prefilter_levels - 1.0f);
-      V3 spec = blurred;
-      if (t < 1.0f) {
-        V3 sharp = sample_radiance(s.env_radiance[c.env], s.env_data, dominant, c.env_yaw, 0.0f);
-        spec = sharp * (1.0f - t) + blurred * t;
-      }
-      prefiltered = c.ambient + spec * c.env_scale;
-    }
-    float ao = sf.occlusion;
-    float spec_ao = clampf(powf(nov + ao, exp2f(-16.0f * lb.alpha - 1.0f)) - 1.0f + ao, 0.0f, 1.0f);
-    V3 radiance = cmul(irradiance, lb.diffuse_color) * ao + cmul(prefiltered, cmul(lb.spec_albedo, lb.energy_comp)) * spec_ao;
-    // MuJoCo lights, then the headlight (a directional light along the view, no shadow, its
-    // illuminance display-relative), through one shade_light call site.
-    const int32_t nl = c.L.nlight + (st.headlight_active ? 1 : 0);
-#pragma unroll 1
-    for (int32_t li = 0; li < nl; ++li) {
-      Light light;
-      int32_t count = c.L.nlight, index = li;
-      if (li < c.L.nlight) {
-        light = load_light(c.blk + c.L.light_off + li * kLightFloats);
-        if (!light.active) continue;
-      } else {
-        light = make_headlight(st, head_dir, c.exposure);
-        count = 1;
-        index = 0;
-      }
-      radiance += shade_light(c, light, lb, point, normal, view, nov, seed, stream, count, index);
-    }
-    return radiance + sf.emissive / c.exposure;
+    TracedVis<kMesh> vis;
+    return Shade::shade_surface(c, vis, sf, point, normal, view, head_dir, seed, stream);
   }
 
-  static MJ_DEV V3 background(RtCtx& c, V3 d, float spread) {
-    const MjpbrScene& s = *c.s;
-    if (kTex && s.settings.env_background) {
-      MJPBR_COUNT(kOpBackground);
-      float lod = log2f(fmaxf(spread * s.settings.inv_texel_angle, kMinTexels));
-      return sample_radiance(s.env_radiance[c.env], s.env_data, d, c.env_yaw, lod) * c.env_scale;
-    }
-    return V3{s.settings.background[0], s.settings.background[1], s.settings.background[2]} / c.exposure;
-  }
+  static MJ_DEV V3 background(RtCtx& c, V3 d, float spread) { return Shade::background(c, d, spread); }
 
   // Radiance along a camera ray, its first hit, and that surface's base colour and normal
   // (render.py:242-341). Translucent layers and the one-bounce mirror ray of each layer are
@@ -201,8 +118,8 @@ struct Rt {
           }
           if (mirror > 0.0f) {
             // the mirror segment of this layer, then the next layer (if any)
-            V3 r = sd - normal * (2.0f * dot(sd, normal));
-            so = point + normal * kRayOffset;
+            V3 r;
+            mirror_ray(point, normal, sd, &so, &r);
             sd = r;
             smax = kMaxVal;
             sweight = mirror * w;
@@ -564,6 +481,8 @@ bool rt_queue_fits(const MjpbrScene& s) {
 }
 
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
+  // translucent layers are not staged: such scenes render with the grid schedule (same images)
+  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT && !s.settings.has_transparency) return render_wave_launch(s, seed, stream);
   if (s.settings.schedule == MJPBR_SCHEDULE_QUEUE) {
     if (!s.work_counter) return set_error(MJPBR_ERR_ARG, "the queue schedule needs the work_counter scratch");
     if (!rt_queue_fits(s)) {

@@ -5,8 +5,9 @@
 // Who needs it: hosts that cannot hand the library device memory after start-up, e.g. a process
 // that runs inside a fixed device-memory arena (a simulator or game loop that pre-reserves its
 // whole budget), or a plugin whose host owns every allocation and offers none for scratch. They
-// only provide the inputs and the output images; scene->world_blocks and scene->work_counter are
-// ignored.
+// only provide the inputs and the output images; scene->world_blocks, scene->work_counter and
+// scene->wave_scratch are ignored (a real-time scene set to the wavefront schedule renders with
+// the grid schedule, whose images are the same).
 //
 // Limits: the blocks of all worlds must fit kStaticBlockFloats floats (16 MiB), i.e.
 // nworld * world_block_floats <= 4,194,304, else the call fails with MJPBR_ERR_ARG before any
@@ -113,5 +114,7 @@ extern "C" int mjpbr_refit_render_static(const MjpbrScene* scene, uint32_t seed,
   if (rc) return rc;
   // render_pt_launch zeroes the work counter on the stream before its kernel starts
   if (s.settings.tier == MJPBR_TIER_PATH) return render_pt_launch(s, seed, st);
+  // the wavefront schedule keeps its ray queues in caller scratch: render with the grid instead
+  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT) s.settings.schedule = MJPBR_SCHEDULE_GRID;
   return render_rt_launch(s, seed, st);
 }

@@ -181,10 +181,15 @@ class PbrRenderContext:
   ray_origin: torch.Tensor | None = None
   ray_direction: torch.Tensor | None = None
   ray_res: list[tuple[int, int]] | None = None
-  # real-time tier schedule (MJPBR_SCHEDULE_GRID 0 / MJPBR_SCHEDULE_QUEUE 1) and the queue's work
-  # item size in pixels; set by create_render_context or mujoco_warp_pbr_gb300.autotune
+  # real-time tier schedule (MJPBR_SCHEDULE_GRID 0 / QUEUE 1 / WAVEFRONT 2), the queue's work item
+  # size in pixels and the wavefront's worlds per chunk (0: automatic); set by
+  # create_render_context or mujoco_warp_pbr_gb300.autotune
   schedule: int = 0
   queue_item: int = 64
+  wave_chunk_worlds: int = 0
+  # the wavefront schedule's ray queues and records (uint8, allocated at the first render that
+  # needs them, sized by mjpbr_wave_scratch_bytes)
+  wave_scratch: torch.Tensor | None = None
   # accepted for compatibility with the reference's signature; the GB300 kernels choose their own
   block_dim: int | None = None
   max_registers: int | None = None

@@ -218,6 +218,8 @@ def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
       "denoise_iterations": int(rc.denoise_iterations),
       "error_word": rc.error_word,
       "work_counter": rc.work_counter,
+      "wave_scratch": rc.wave_scratch,
+      "wave_scratch_bytes": int(rc.wave_scratch.numel()) if rc.wave_scratch is not None else 0,
       "settings": st,
     }
   )
@@ -261,9 +263,38 @@ def scene(m: Any, d: Any, rc: PbrRenderContext) -> _lib.Scene:
   _warn_ignored_overrides(m, rc)
   fields = scene_fields(m, d, rc)
   struct = _scene.fill_scene(fields)
+  if _ensure_wave_scratch(rc, struct):
+    sources = _sources(m, d, rc)
+    ids = tuple(map(id, sources))
+    fields = scene_fields(m, d, rc)
+    struct = _scene.fill_scene(fields)
   # the cache holds the sources and the converted tensors so their addresses stay valid
   rc._host_cache["scene"] = (sources, ids, struct, fields)
   return struct
+
+
+# samples per chunk of the wavefront schedule when wave_chunk_worlds is 0
+WAVE_CHUNK_SAMPLES = 1 << 24
+
+
+def _ensure_wave_scratch(rc: PbrRenderContext, struct: _lib.Scene) -> bool:
+  """Allocates (or grows) the wavefront schedule's scratch for a real-time context using it:
+  wave_chunk_worlds worlds per chunk, or about WAVE_CHUNK_SAMPLES camera samples. Returns True
+  when rc.wave_scratch changed."""
+  if rc.tier != 0 or rc.schedule != 2 or rc.has_transparency:
+    return False
+  lib = _lib.load()
+  per_world = lib.mjpbr_wave_scratch_bytes(struct, 1) - lib.mjpbr_wave_scratch_bytes(struct, 0)
+  samples = max(1, sum(w * h for (w, h), on in zip(rc.base.cam_res, rc.base.render_rgb) if on) * int(rc.samples_per_pixel) ** 2)
+  chunk = rc.wave_chunk_worlds or max(1, WAVE_CHUNK_SAMPLES // samples)
+  chunk = min(chunk, int(rc.base.rgb_data.shape[0]))
+  need = int(lib.mjpbr_wave_scratch_bytes(struct, chunk))
+  if need < 0 or per_world < 0:
+    raise ValueError("the wavefront schedule cannot render this scene")
+  if rc.wave_scratch is not None and rc.wave_scratch.numel() >= need:
+    return False
+  rc.wave_scratch = torch.empty(need, dtype=torch.uint8, device=rc.device)
+  return True
 
 
 def _warn_ignored_overrides(m: Any, rc: PbrRenderContext) -> None:
