@@ -394,7 +394,16 @@ def run(args) -> None:
   torch.cuda.synchronize()
   assert mjpbr.check_errors(rc) == 0, "kernels reported an error"
 
-  # ---- device-resident timing, per-step events, L2 flushed outside the events
+  # ---- device-resident timing, per-step events, L2 flushed outside the events; the wavefront's
+  # stage boundaries are recorded by the library on the same stream (mjpbr_wave_profile_begin)
+  import ctypes
+
+  from mujoco_warp_pbr_gb300.profile_frame import STAGES
+
+  wave = rc.tier == 0 and rc.schedule == 2 and not rc.has_transparency
+  stage_sum = dict.fromkeys(STAGES, 0.0)
+  stage_buf = (ctypes.c_double * len(STAGES))()
+  chunks = ctypes.c_int32(0)
   starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
   mids = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
   ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -408,8 +417,14 @@ def run(args) -> None:
       starts[i].record(stream)
       _lib.call("mjpbr_refit_bvh", scene, stream.cuda_stream)
       mids[i].record(stream)
+      if wave:
+        _lib.call("mjpbr_wave_profile_begin")
       _lib.call("mjpbr_render", scene, 1000 + i, stream.cuda_stream)
       ends[i].record(stream)
+      if wave:
+        _lib.call("mjpbr_wave_profile_end", stage_buf, ctypes.byref(chunks))
+        for k, name in enumerate(STAGES):
+          stage_sum[name] += stage_buf[k]
     torch.cuda.synchronize()
   if world_size > 1:
     dist.barrier()
@@ -419,17 +434,26 @@ def run(args) -> None:
   value = aggregate_rate(npix * args.steps, total_ms, world_size)
   assert mjpbr.check_errors(rc) == 0
 
-  # ---- end to end through the public API with host buffers
+  # ---- end to end through the public API with host buffers: poses in from pinned memory,
+  # refit + render, get_rgb's float image (the reference's output format) back to pinned memory
   host = {name: getattr(d, name).cpu().pin_memory() for name in ("geom_xpos", "geom_xmat", "cam_xpos", "cam_xmat", "light_xpos", "light_xdir")}
-  out_host = torch.empty(rc.base.rgb_data.shape, dtype=rc.base.rgb_data.dtype).pin_memory()
+  rgb_dev = [torch.empty((sc.nworld, h, w, 3), dtype=torch.float32, device=dev) for (w, h), on in zip(rc.base.cam_res, rc.base.render_rgb) if on]
+  rgb_host = [torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in rgb_dev]
+  rgb_cams = [c for c, on in enumerate(rc.base.render_rgb) if on]
   h2d = sum(t.numel() * t.element_size() for t in host.values())
-  d2h = out_host.numel() * out_host.element_size()
-  e2e_steps = max(3, args.steps // 2)
-  for i in range(2):
+  d2h = sum(t.numel() * t.element_size() for t in rgb_host)
+
+  def e2e_step(seed: int) -> None:
     for name, t in host.items():
       getattr(d, name).copy_(t, non_blocking=True)
-    step(i)
-    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+    step(seed)
+    for cam, td, th in zip(rgb_cams, rgb_dev, rgb_host, strict=True):
+      mjpbr.get_rgb(rc, cam, td)
+      th.copy_(td, non_blocking=True)
+
+  e2e_steps = max(3, args.steps // 2)
+  for i in range(2):
+    e2e_step(i)
   torch.cuda.synchronize()
   if world_size > 1:
     dist.barrier()
@@ -437,10 +461,7 @@ def run(args) -> None:
   e1 = torch.cuda.Event(enable_timing=True)
   e0.record(stream)
   for i in range(e2e_steps):
-    for name, t in host.items():
-      getattr(d, name).copy_(t, non_blocking=True)
-    step(2000 + i)
-    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+    e2e_step(2000 + i)
   e1.record(stream)
   torch.cuda.synchronize()
   e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
@@ -453,6 +474,13 @@ def run(args) -> None:
     achieved = alg / (render_avg / 1000.0) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = _traffic(sc.name)
+    launches = render_launches(rc, int(chunks.value), int(scene.nlight))
+    if args.workload == "path":
+      kernel = "pt_kernel"
+    elif wave:
+      kernel = "wavefront render: wave_primary, wave_surface, wave_mirror, wave_mirror_surface, wave_shadow, wave_resolve per chunk"
+    else:
+      kernel = "rt_kernel"
     line = {
       "metric": PATH_METRIC if args.workload == "path" else METRIC,
       "value": value,
@@ -467,10 +495,11 @@ def run(args) -> None:
       "dtype": "f32",
       "data": "synthetic (seeded scenes; no dataset)",
       "config": _config(args, sc),
-      "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+      "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+              "output": "get_rgb float32 (nworld, H, W, 3) per RGB camera"},
       "roofline": {
         "bound": "hbm",
-        "kernel": "pt_kernel" if args.workload == "path" else "rt_kernel",
+        "kernel": kernel,
         "achieved": achieved,
         "peak": peak,
         "unit": "GB/s",
@@ -482,10 +511,13 @@ def run(args) -> None:
       "render_ms": render_avg,
       "refit_ms": (total_ms / args.steps) - render_avg,
       "rays_note": "rays_per_s: every ray query of the frame (primary, shadow, mirror), counted by the counting build",
-      "gpu_launches": 2 * args.steps,
+      "gpu_launches": (1 + launches) * args.steps,
       "clocks": clocks.summary(),
       "cpu_baseline": baseline,
     }
+    if wave:
+      line["stages_ms"] = {k: v / args.steps for k, v in stage_sum.items()}
+      line["stages_note"] = f"CUDA events the library records at the wavefront's stage boundaries in the timed steps, {int(chunks.value)} chunks of worlds per frame"
     if args.workload in ("mesh_ibl", "primitives"):
       rt = rt_fp32_roofline(args, dev, npix, render_avg)
       line["roofline_fp32"] = rt
@@ -494,9 +526,45 @@ def run(args) -> None:
       line["path_tier"] = path_tier(dev, max(3, args.steps // 2))
       if not args.no_learned:
         line["learned_denoiser"] = learned_denoiser(args)
+    if args.workload == "mesh_ibl" and not args.no_configs:
+      budget = None if args.no_cpu_baseline else 5.0
+      line["batched"] = measure_batched(args, dev, 2048, 10, 3, budget)
+      if WEIGHTS.exists():
+        line["large_path"] = measure_large(args, dev, args.large_worlds, 3, 3, budget)
+        line["large_path"]["note"] = f"{args.large_worlds} of the configuration's 8192 worlds, so the default run stays within minutes (--workload large_path runs all 8192)"
     print(json.dumps(line))
   if world_size > 1:
     dist.destroy_process_group()
+
+
+def frame_chunks(m, d, rc) -> int:
+  """Chunks of worlds a wavefront render of rc takes (one profiled eager render), else 0."""
+  import ctypes
+
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import _lib
+
+  if not (rc.tier == 0 and rc.schedule == 2 and not rc.has_transparency):
+    return 0
+  buf = (ctypes.c_double * 6)()
+  chunks = ctypes.c_int32(0)
+  _lib.call("mjpbr_wave_profile_begin")
+  mjpbr.render(m, d, rc)
+  _lib.call("mjpbr_wave_profile_end", buf, ctypes.byref(chunks))
+  return int(chunks.value)
+
+
+def render_launches(rc, chunks: int, nlight: int) -> int:
+  """Kernels one render call launches: the wavefront's stages per chunk of worlds (primary, and
+  with RGB cameras surface + resolve, mirror + mirror surface with reflections, shadow with
+  shadowing lights), else the single megakernel / path kernel."""
+  if not (rc.tier == 0 and rc.schedule == 2 and not rc.has_transparency):
+    return 1
+  rgb = any(rc.base.render_rgb)
+  per = 1 + (2 if rgb else 0) + (2 if rgb and rc.has_reflection else 0)
+  if rgb and rc.use_shadows and nlight > 0:
+    per += 1
+  return per * max(chunks, 1)
 
 
 def rt_fp32_roofline(args, dev, npix: int, render_ms: float, count_worlds: int = 256) -> dict:
@@ -542,19 +610,18 @@ def learned_denoiser(args) -> dict | None:
   return out
 
 
-def run_large(args) -> None:
-  """Large path-traced run: 8192 worlds x 2 cameras x 256², 2 spp, depth 4, four HDR environments,
-  the learned denoiser (BF16, 512 worlds at a time); every step is one CUDA-graph replay of pose
-  copy -> refit_bvh -> path tracer -> network -> finish pass."""
+def measure_large(args, dev, nworld: int, steps: int, warmup: int, cpu_budget: float | None = None) -> dict:
+  """Large path-traced run: nworld worlds x 2 cameras x 256², 2 spp, depth 4, four HDR
+  environments, the learned denoiser (BF16, args.chunk worlds at a time); every step is one
+  CUDA-graph replay of pose copy -> refit_bvh -> path tracer -> network -> finish pass."""
   import torch
 
   import mujoco_warp_pbr_gb300 as mjpbr
   from mujoco_warp_pbr_gb300 import kpcn
   from mujoco_warp_pbr_gb300 import synthetic
 
-  sc = synthetic.large_path_scene(seed=args.seed, nworld=args.nworld, res=args.res)
-  torch.cuda.set_device(0)
-  dev = torch.device("cuda", 0)
+  sc = synthetic.large_path_scene(seed=args.seed, nworld=nworld, res=256)
+  baseline = cpu_baseline(sc, cpu_budget) if cpu_budget else None
   m = mjpbr.put_model(sc.mjm, device=dev)
   d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld, device=dev)
   opts = {**sc.options, "denoise": True, "render_hdr": False}
@@ -565,157 +632,193 @@ def run_large(args) -> None:
   poses[:, 1:, 2] += 0.01
   graph = mjpbr.capture_frame(m, d, rc, seed=7, step=lambda: d.geom_xpos.copy_(poses), denoiser=lambda: net.denoise(m, d, rc, chunk=args.chunk))
   stream = torch.cuda.current_stream(dev)
-  for _ in range(args.warmup):
+  for _ in range(warmup):
     graph.replay()
   torch.cuda.synchronize()
   assert mjpbr.check_errors(rc) == 0 and int(net.error.item()) == 0
   npix = sc.nworld * sum(w * h for w, h in rc.base.cam_res)
   e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-  with ClockSampler(0) as clocks:
+  with ClockSampler(dev.index or 0) as clocks:
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
       graph.replay()
     e1.record(stream)
     torch.cuda.synchronize()
-  ms = e0.elapsed_time(e1) / args.steps
-  out_host = torch.empty(rc.base.rgb_data.shape, dtype=rc.base.rgb_data.dtype).pin_memory()
+  ms = e0.elapsed_time(e1) / steps
+  # end to end: poses from pinned host memory, the graph, get_rgb's float image back to the host
   host_poses = poses.cpu().pin_memory()
+  rgb_dev = [torch.empty((sc.nworld, h, w, 3), dtype=torch.float32, device=dev) for w, h in rc.base.cam_res]
+  rgb_host = [torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in rgb_dev]
   e0.record(stream)
-  for _ in range(args.steps):
+  for _ in range(steps):
     poses.copy_(host_poses, non_blocking=True)
     graph.replay()
-    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+    for cam, (td, th) in enumerate(zip(rgb_dev, rgb_host, strict=True)):
+      mjpbr.get_rgb(rc, cam, td)
+      th.copy_(td, non_blocking=True)
   e1.record(stream)
   torch.cuda.synchronize()
-  e2e_ms = e0.elapsed_time(e1) / args.steps
-  print(json.dumps({
+  e2e_ms = e0.elapsed_time(e1) / steps
+  peaks = _peaks()
+  alg = algorithmic_bytes(rc)
+  return {
     "metric": PATH_METRIC,
     "value": npix / ms / 1e3,
     "unit": UNIT,
-    "n_gpus": 1,
-    "steps": args.steps,
-    "warmup": args.warmup,
     "ms_per_step": ms,
-    "higher_is_better": True,
-    "scaling": "weak",
-    "vs_baseline": None,
+    "steps": steps,
+    "warmup": warmup,
     "dtype": "f32 path tracing, bf16 network",
-    "data": "synthetic (seeded scenes; no dataset)",
-    "config": {"workload": sc.name, "nworld": sc.nworld, "cameras": 2, "cam_res": [args.res, args.res], "spp": 2, "max_depth": 4,
+    "config": {"workload": sc.name, "nworld": sc.nworld, "cameras": 2, "cam_res": [256, 256], "spp": 2, "max_depth": 4,
                "rr_depth": 2, "envs": 4, "denoiser": "learned (KPCN, BF16)", "chunk_worlds": args.chunk, "graph": "one CUDA graph per frame",
                "l2": "frame working set far above L2"},
-    "e2e": {"value": npix / e2e_ms / 1e3, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4), "d2h_bytes_per_step": int(out_host.numel() * 4)},
+    "e2e": {"value": npix / e2e_ms / 1e3, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4),
+            "d2h_bytes_per_step": int(sum(t.numel() * 4 for t in rgb_host)), "output": "get_rgb float32 (nworld, H, W, 3) per camera"},
+    "roofline": {
+      "bound": "hbm",
+      "kernel": "whole frame graph (path tracer, network, finish pass)",
+      "achieved": alg / (ms / 1000.0) / 1e9,
+      "peak": float(peaks.get("hbm_gbs", 6800.0)),
+      "unit": "GB/s",
+      "frac": alg / (ms / 1000.0) / 1e9 / float(peaks.get("hbm_gbs", 6800.0)),
+      "traffic": None,
+      "algorithmic_bytes_per_launch": alg,
+      "peak_source": "measured" if "fallback" not in peaks else "fallback",
+    },
     "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
     # per replay: refit, path tracer, the denoiser's kernels (the pose copy is a memcpy node)
-    "gpu_launches": (2 + kpcn.denoise_launches(rc, args.chunk)) * args.steps,
+    "gpu_launches": (2 + kpcn.denoise_launches(rc, args.chunk)) * steps,
     "clocks": clocks.summary(),
-  }))
+    "cpu_baseline": baseline,
+  }
 
 
-def run_batched(args) -> None:
-  """Batched uneven workload: autotuned launch shape, and every step is one CUDA-graph replay of
-  step (copy of the next poses) -> refit_bvh -> render."""
+def run_large(args) -> None:
+  import torch
+
+  torch.cuda.set_device(0)
+  dev = torch.device("cuda", 0)
+  out = measure_large(args, dev, args.nworld, args.steps, args.warmup, None if args.no_cpu_baseline else args.cpu_budget)
+  line = {**out, "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded scenes; no dataset)"}
+  print(json.dumps(line))
+
+
+def measure_batched(args, dev, nworld: int, steps: int, warmup: int, cpu_budget: float | None = None, world_size: int = 1) -> dict:
+  """Batched uneven workload (three cameras of 64², 128², 256² per world, one a fisheye bundle,
+  per-world enable masks): autotuned launch shape, every step one CUDA-graph replay of step (a
+  copy of the next poses) -> refit_bvh -> render."""
+  import copy
+
   import torch
 
   import mujoco_warp_pbr_gb300 as mjpbr
   from mujoco_warp_pbr_gb300 import synthetic
 
-  world_size = int(os.environ.get("WORLD_SIZE", "1"))
-  rank = int(os.environ.get("RANK", "0"))
-  local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-  import torch.distributed as dist
-
-  sc = make_scene(args)
-  baseline = None
-  if rank == 0 and not args.no_cpu_baseline:
-    baseline = cpu_baseline(sc, args.cpu_budget)
-  torch.cuda.set_device(local_rank)
-  if world_size > 1:
-    dist.init_process_group("nccl")
-  dev = torch.device("cuda", local_rank)
+  a = copy.copy(args)
+  a.workload, a.nworld = "batched", nworld
+  sc = make_scene(a)
+  baseline = cpu_baseline(sc, cpu_budget) if cpu_budget else None
   m = mjpbr.put_model(sc.mjm, device=dev)
   d = mjpbr.put_data(sc.mjm, sc.mjd, nworld=sc.nworld, device=dev)
   rc = mjpbr.create_render_context(sc.mjm, sc.nworld, data=sc.mjd, device=dev, **sc.options)
   synthetic.apply_per_world(sc, m, rc)
   tuned = mjpbr.autotune(m, d, rc, frames=3)
   npix = sc.nworld * sum(w * h for w, h in rc.base.cam_res)
+  launches = 1 + render_launches(rc, frame_chunks(m, d, rc), int(mjpbr.scene_descriptor(m, d, rc).nlight))  # refit + render
   poses = d.geom_xpos.clone()
   poses[:, 1:, 2] += 0.01  # the "next" poses the step copies in
   graph = mjpbr.capture_frame(m, d, rc, seed=7, step=lambda: d.geom_xpos.copy_(poses))
   stream = torch.cuda.current_stream(dev)
   flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
-  for _ in range(args.warmup):
+  for _ in range(warmup):
     graph.replay()
   torch.cuda.synchronize()
   assert mjpbr.check_errors(rc) == 0
-  starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-  ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+  starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+  ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
   if world_size > 1:
+    import torch.distributed as dist
+
     dist.barrier()
   torch.cuda.synchronize()
-  with ClockSampler(local_rank) as clocks:
-    for i in range(args.steps):
+  with ClockSampler(dev.index or 0) as clocks:
+    for i in range(steps):
       flush.zero_()
       starts[i].record(stream)
       graph.replay()
       ends[i].record(stream)
     torch.cuda.synchronize()
   total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(starts, ends, strict=True)), dev)
-  value = aggregate_rate(npix * args.steps, total_ms, world_size)
-  # end to end: next poses from pinned host memory, the graph, the RGB back to pinned memory
+  value = aggregate_rate(npix * steps, total_ms, world_size)
+  # end to end: next poses from pinned host memory, the graph, get_rgb's float images back
   host_poses = poses.cpu().pin_memory()
-  out_host = torch.empty(rc.base.rgb_data.shape, dtype=rc.base.rgb_data.dtype).pin_memory()
+  rgb_dev = [torch.empty((sc.nworld, h, w, 3), dtype=torch.float32, device=dev) for w, h in rc.base.cam_res]
+  rgb_host = [torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in rgb_dev]
   e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-  e2e_steps = max(3, args.steps // 2)
+  e2e_steps = max(3, steps // 2)
   e0.record(stream)
   for _ in range(e2e_steps):
     poses.copy_(host_poses, non_blocking=True)
     graph.replay()
-    out_host.copy_(rc.base.rgb_data, non_blocking=True)
+    for cam, (td, th) in enumerate(zip(rgb_dev, rgb_host, strict=True)):
+      mjpbr.get_rgb(rc, cam, td)
+      th.copy_(td, non_blocking=True)
   e1.record(stream)
   torch.cuda.synchronize()
   e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
   e2e_value = aggregate_rate(npix * e2e_steps, e2e_ms, world_size)
   assert mjpbr.check_errors(rc) == 0
+  peaks = _peaks()
+  avg = total_ms / steps
+  alg = algorithmic_bytes(rc)
+  achieved = alg / (avg / 1000.0) / 1e9
+  peak = float(peaks.get("hbm_gbs", 6800.0))
+  cfg = _config(a, sc)
+  cfg["launch_shape"] = tuned["best"]
+  return {
+    "metric": METRIC,
+    "value": value,
+    "unit": UNIT,
+    "steps": steps,
+    "warmup": warmup,
+    "ms_per_step": avg,
+    "config": cfg,
+    "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4),
+            "d2h_bytes_per_step": int(sum(t.numel() * 4 for t in rgb_host)), "output": "get_rgb float32 (nworld, H, W, 3) per camera"},
+    "roofline": {
+      "bound": "hbm",
+      "kernel": f"render ({tuned['best']}), whole graph timed",
+      "achieved": achieved,
+      "peak": peak,
+      "unit": "GB/s",
+      "frac": achieved / peak,
+      "traffic": _traffic(sc.name),
+      "algorithmic_bytes_per_launch": alg,
+      "peak_source": "measured" if "fallback" not in peaks else "fallback",
+    },
+    "autotune_ms": tuned.get("ms", {}),
+    "gpu_launches": launches * steps,
+    "clocks": clocks.summary(),
+    "cpu_baseline": baseline,
+  }
+
+
+def run_batched(args) -> None:
+  import torch
+  import torch.distributed as dist
+
+  world_size = int(os.environ.get("WORLD_SIZE", "1"))
+  rank = int(os.environ.get("RANK", "0"))
+  local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+  torch.cuda.set_device(local_rank)
+  if world_size > 1:
+    dist.init_process_group("nccl")
+  dev = torch.device("cuda", local_rank)
+  budget = args.cpu_budget if (rank == 0 and not args.no_cpu_baseline) else None
+  out = measure_batched(args, dev, args.nworld, args.steps, args.warmup, budget, world_size)
   if rank == 0:
-    peaks = _peaks()
-    avg = total_ms / args.steps
-    alg = algorithmic_bytes(rc)
-    achieved = alg / (avg / 1000.0) / 1e9
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    cfg = _config(args, sc)
-    cfg["launch_shape"] = tuned["best"]
-    line = {
-      "metric": METRIC,
-      "value": value,
-      "unit": UNIT,
-      "n_gpus": world_size,
-      "steps": args.steps,
-      "warmup": args.warmup,
-      "ms_per_step": avg,
-      "higher_is_better": True,
-      "scaling": "weak",
-      "vs_baseline": None,
-      "dtype": "f32",
-      "data": "synthetic (seeded scenes; no dataset)",
-      "config": cfg,
-      "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4), "d2h_bytes_per_step": int(out_host.numel() * out_host.element_size())},
-      "roofline": {
-        "bound": "hbm",
-        "kernel": "rt_kernel / rt_queue_kernel (whole graph timed)",
-        "achieved": achieved,
-        "peak": peak,
-        "unit": "GB/s",
-        "frac": achieved / peak,
-        "traffic": _traffic(sc.name),
-        "algorithmic_bytes_per_launch": alg,
-        "peak_source": "measured" if "fallback" not in peaks else "fallback",
-      },
-      "autotune_ms": tuned.get("ms", {}),
-      "gpu_launches": 2 * args.steps,
-      "clocks": clocks.summary(),
-      "cpu_baseline": baseline,
-    }
+    line = {**out, "n_gpus": world_size, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scenes; no dataset)"}
     print(json.dumps(line))
   if world_size > 1:
     dist.destroy_process_group()
@@ -732,6 +835,8 @@ def main() -> None:
   p.add_argument("--spp", type=int, default=2)
   p.add_argument("--no-path-tier", action="store_true")
   p.add_argument("--no-learned", action="store_true")
+  p.add_argument("--no-configs", action="store_true", help="leave the batched and large_path objects out of the default line")
+  p.add_argument("--large-worlds", type=int, default=1024, help="worlds of the default line's large_path object")
   # quality against 4096-spp references on 64 worlds, throughput on the 1024-world path batch
   p.add_argument("--learned-worlds", type=int, default=64)
   p.add_argument("--learned-ref-spp", type=int, default=4096)

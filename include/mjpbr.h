@@ -360,6 +360,16 @@ int32_t mjpbr_world_block_floats(int32_t nbvh_geom, int32_t nnode, int32_t nligh
  * wavefront schedule (the reference renders every world in one megakernel launch). */
 int64_t mjpbr_wave_scratch_bytes(const MjpbrScene* scene, int32_t worlds);
 
+/* Stage profile of the wavefront schedule, for tools: after mjpbr_wave_profile_begin, every
+ * wavefront render issued from this host thread records CUDA events (the library's own, reused) on
+ * the render stream at each stage boundary of each chunk of worlds; mjpbr_wave_profile_end waits
+ * for the last one, writes the milliseconds of the primary, surface, mirror, mirror-surface,
+ * shadow and resolve stages summed over the chunks into stage_ms[6] and the number of chunks into
+ * *chunks, and stops recording. Not for use inside a stream capture. No counterpart in the
+ * reference (its megakernel is a single launch). */
+int mjpbr_wave_profile_begin(void);
+int mjpbr_wave_profile_end(double* stage_ms, int32_t* chunks);
+
 /* Per-geom world AABBs from the current poses, bottom-up refit of every world's scene BVH, and the
  * per-world blocks (geom, light, camera records and BVH nodes) the render kernels stage into
  * shared memory. Replaces mujoco_warp.refit_bvh(m, d, rc.base). Launches one kernel. */

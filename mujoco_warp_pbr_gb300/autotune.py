@@ -1,11 +1,13 @@
 """Autotuner of the real-time tier's launch shape, and CUDA-graph capture of a whole frame.
 
-The real-time kernel has two schedules (include/mjpbr.h, MjpbrSchedule): a grid of one CTA per
-(camera tile, world) with 32 x 8 (RenderOrder.ROW) or 16 x 16 (TILED) pixel tiles, and a
-persistent launch whose warps pull work items of 32, 64 or 128 pixels from a device counter
-(the queue's item size is its ray-sort granularity: the pixels a warp renders back to back from
-one world block). Every candidate renders the same image; the autotuner times each on the
-context's own scene and keeps the fastest. Results are cached per scene signature for the
+The real-time tier has three schedules (include/mjpbr.h, MjpbrSchedule): the megakernel as a grid
+of one CTA per (camera tile, world) with 32 x 8 (RenderOrder.ROW) or 16 x 16 (TILED) pixel
+tiles; the megakernel as a persistent launch whose warps pull work items of 32, 64 or 128 pixels
+from a device counter (the queue's item size is its ray-sort granularity: the pixels a warp
+renders back to back from one world block); and the staged wavefront (one kernel per stage over
+compacted ray queues, a chunk of worlds at a time: the chunk size trades scratch memory and L2
+locality against launches). Every candidate renders the same image; the autotuner times each on
+the context's own scene and keeps the fastest. Results are cached per scene signature for the
 process.
 
 capture_frame() records step -> refit_bvh -> render (-> denoise) into one CUDA graph, so a
@@ -27,22 +29,27 @@ from mujoco_warp_pbr_gb300.render import render
 from mujoco_warp_pbr_gb300.render import scene as scene_descriptor
 
 ROW, TILED = 0, 1
-GRID, QUEUE = 0, 1
+GRID, QUEUE, WAVEFRONT = 0, 1, 2
 
 
 @dataclasses.dataclass(frozen=True)
 class LaunchShape:
-  schedule: int  # GRID or QUEUE
+  schedule: int  # GRID, QUEUE or WAVEFRONT
   render_order: int  # grid tile shape: ROW (32 x 8) or TILED (16 x 16)
   queue_item: int  # queue work item, pixels
+  wave_chunk_worlds: int = 0  # wavefront: worlds per chunk (0: about 16 M samples)
 
   def describe(self) -> str:
     if self.schedule == GRID:
       return "grid 32x8" if self.render_order == ROW else "grid 16x16"
+    if self.schedule == WAVEFRONT:
+      return f"wavefront {self.wave_chunk_worlds or 'auto'} worlds per chunk"
     return f"queue {self.queue_item} px"
 
 
 CANDIDATES = (
+  LaunchShape(WAVEFRONT, TILED, 64, 0),
+  LaunchShape(WAVEFRONT, TILED, 64, 64),
   LaunchShape(GRID, TILED, 64),
   LaunchShape(GRID, ROW, 64),
   LaunchShape(QUEUE, TILED, 32),
@@ -74,6 +81,9 @@ def apply(rc: PbrRenderContext, shape: LaunchShape) -> None:
   rc.schedule = shape.schedule
   rc.render_order = shape.render_order
   rc.queue_item = shape.queue_item
+  if rc.wave_chunk_worlds != shape.wave_chunk_worlds:
+    rc.wave_chunk_worlds = shape.wave_chunk_worlds
+    rc.wave_scratch = None  # sized again for the new chunk at the next render
 
 
 def autotune(m: Any, d: Any, rc: PbrRenderContext, frames: int = 3, candidates: tuple[LaunchShape, ...] = CANDIDATES, use_cache: bool = True) -> dict:

@@ -631,7 +631,7 @@ def prepare_context(
   use_skybox: bool = True,
   render_order: RenderOrder | int = RenderOrder.TILED,
   block_dim: int | None = None,
-  schedule: str | int = "grid",
+  schedule: str | int = "wavefront",
   queue_item: int = 64,
   wave_chunk_worlds: int = 0,
   max_registers: int | None = None,

@@ -26,7 +26,7 @@
 // two shadow entries (64 B); the library renders as many worlds per chunk as the scratch holds.
 #include <algorithm>
 #include <climits>
-#include <mutex>
+#include <vector>
 
 #include "abi_internal.h"
 #include "rt_shade.cuh"
@@ -36,6 +36,14 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTile = 16;  // pixel tiles of 16 x 16, addressed in Z order within the tile
+// Resident CTAs per SM the register allocation of the ray-tracing stages (primary, mirror,
+// shadow: 64 KB of traversal stacks per CTA) and of the surface / shading stages targets.
+#ifndef MJPBR_WAVE_TRACE_CTAS
+#define MJPBR_WAVE_TRACE_CTAS 3
+#endif
+#ifndef MJPBR_WAVE_SHADE_CTAS
+#define MJPBR_WAVE_SHADE_CTAS 2
+#endif
 
 struct __align__(16) HitRec {
   float dist;
@@ -231,7 +239,7 @@ MJ_DEV void emit_shadows(const MjpbrScene& s, const WaveMap& wm, const float* bl
 
 // ---------------------------------------------------------------- 1. primary rays
 template <bool kMesh>
-__global__ void __launch_bounds__(kThreads) wave_primary_kernel(const __grid_constant__ MjpbrScene s,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_primary_kernel(const __grid_constant__ MjpbrScene s,
                                                                 const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   float* blk = smem;
@@ -275,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) wave_primary_kernel(const __grid_con
 
 // ---------------------------------------------------------------- 2. surfaces at primary hits
 template <bool kMesh, bool kTex>
-__global__ void __launch_bounds__(kThreads) wave_surface_kernel(const __grid_constant__ MjpbrScene s,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_surface_kernel(const __grid_constant__ MjpbrScene s,
                                                                 const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   float* blk = smem;
@@ -349,7 +357,7 @@ __global__ void __launch_bounds__(kThreads) wave_surface_kernel(const __grid_con
 
 // ---------------------------------------------------------------- 3. mirror rays (persistent)
 template <bool kMesh>
-__global__ void __launch_bounds__(kThreads) wave_mirror_kernel(const __grid_constant__ MjpbrScene s,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_mirror_kernel(const __grid_constant__ MjpbrScene s,
                                                                const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
@@ -370,7 +378,7 @@ __global__ void __launch_bounds__(kThreads) wave_mirror_kernel(const __grid_cons
 
 // ---------------------------------------------------------------- 4. surfaces at mirror hits
 template <bool kMesh, bool kTex>
-__global__ void __launch_bounds__(kThreads) wave_mirror_surface_kernel(const __grid_constant__ MjpbrScene s,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_mirror_surface_kernel(const __grid_constant__ MjpbrScene s,
                                                                        const __grid_constant__ WaveMap wm) {
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const int32_t count = (int32_t)min((int64_t)*wm.counters, wm.mirror_cap);
@@ -409,7 +417,7 @@ __global__ void __launch_bounds__(kThreads) wave_mirror_surface_kernel(const __g
 
 // ---------------------------------------------------------------- 5. shadow rays (persistent)
 template <bool kMesh>
-__global__ void __launch_bounds__(kThreads) wave_shadow_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_shadow_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
@@ -455,7 +463,7 @@ struct StoredVis {
 
 // ---------------------------------------------------------------- 6. shading and pixel outputs
 template <bool kTex>
-__global__ void __launch_bounds__(kThreads) wave_resolve_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_resolve_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                 const __grid_constant__ WaveMap wm) {
   using Shade = RtShade<kTex, StoredVis>;
   extern __shared__ __align__(16) float smem[];
@@ -555,6 +563,35 @@ __global__ void __launch_bounds__(kThreads) wave_resolve_kernel(const __grid_con
 }
 
 // ---------------------------------------------------------------- host side
+
+// Stage profile of mjpbr_wave_profile_begin / _end (this host thread): per chunk, one event
+// before the primary stage and one after each of the six stages (a stage that does not run still
+// records), from a pool of events the library creates once and reuses.
+constexpr int kStages = 6;
+
+struct StageProfile {
+  bool on = false;
+  std::vector<cudaEvent_t> events;
+  size_t used = 0;
+  ~StageProfile() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  }
+};
+thread_local StageProfile g_profile;
+
+void stage_mark(cudaStream_t stream) {
+  StageProfile& p = g_profile;
+  if (!p.on) return;
+  if (p.used == p.events.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      p.on = false;
+      return;
+    }
+    p.events.push_back(e);
+  }
+  cudaEventRecord(p.events[p.used++], stream);
+}
 
 int64_t align256(int64_t b) { return (b + 255) & ~int64_t(255); }
 
@@ -660,27 +697,40 @@ int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t
   for (int32_t w0 = 0; w0 < s.nworld; w0 += chunk) {
     wm.w0 = w0;
     wm.nw = std::min(chunk, s.nworld - w0);
+    stage_mark(stream);
     if (geo_tiles > 0) {
       k_primary<<<dim3(geo_tiles, wm.nw), kThreads, blk_bytes + stack, stream>>>(s, wm);
       if ((rc = check_launch("wave_primary_kernel"))) return rc;
     }
-    if (rgb_tiles == 0) continue;
-    cudaError_t e = cudaMemsetAsync(wm.counters, 0, 2 * sizeof(int32_t), stream);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "wavefront queue counters: %s", cudaGetErrorString(e));
-    k_surface<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, wm);
-    if ((rc = check_launch("wave_surface_kernel"))) return rc;
-    if (s.settings.has_reflection) {
+    stage_mark(stream);
+    if (rgb_tiles > 0) {
+      cudaError_t e = cudaMemsetAsync(wm.counters, 0, 2 * sizeof(int32_t), stream);
+      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "wavefront queue counters: %s", cudaGetErrorString(e));
+      k_surface<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, wm);
+      if ((rc = check_launch("wave_surface_kernel"))) return rc;
+    }
+    stage_mark(stream);
+    const bool mirrors = rgb_tiles > 0 && s.settings.has_reflection;
+    if (mirrors) {
       k_mirror<<<g_mirror, kThreads, stack, stream>>>(s, wm);
       if ((rc = check_launch("wave_mirror_kernel"))) return rc;
+    }
+    stage_mark(stream);
+    if (mirrors) {
       k_msurface<<<g_msurface, kThreads, 0, stream>>>(s, wm);
       if ((rc = check_launch("wave_mirror_surface_kernel"))) return rc;
     }
-    if (s.nlight > 0 && s.settings.use_shadows) {
+    stage_mark(stream);
+    if (rgb_tiles > 0 && s.nlight > 0 && s.settings.use_shadows) {
       k_shadow<<<g_shadow, kThreads, stack, stream>>>(s, seed, wm);
       if ((rc = check_launch("wave_shadow_kernel"))) return rc;
     }
-    k_resolve<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, seed, wm);
-    if ((rc = check_launch("wave_resolve_kernel"))) return rc;
+    stage_mark(stream);
+    if (rgb_tiles > 0) {
+      k_resolve<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, seed, wm);
+      if ((rc = check_launch("wave_resolve_kernel"))) return rc;
+    }
+    stage_mark(stream);
   }
   return MJPBR_OK;
 }
@@ -738,6 +788,40 @@ int render_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) 
 }
 
 }  // namespace mjpbr
+
+extern "C" int mjpbr_wave_profile_begin(void) {
+  mjpbr::g_profile.on = true;
+  mjpbr::g_profile.used = 0;
+  return MJPBR_OK;
+}
+
+extern "C" int mjpbr_wave_profile_end(double* stage_ms, int32_t* chunks) {
+  using namespace mjpbr;
+  StageProfile& p = g_profile;
+  const bool was_on = p.on;
+  p.on = false;
+  const size_t per = kStages + 1;
+  const size_t used = p.used;
+  p.used = 0;
+  if (!stage_ms || !chunks) return set_error(MJPBR_ERR_ARG, "stage_ms and chunks must not be NULL");
+  for (int k = 0; k < kStages; ++k) stage_ms[k] = 0.0;
+  *chunks = 0;
+  if (!was_on) return set_error(MJPBR_ERR_ARG, "no stage profile was started on this thread");
+  if (used == 0) return MJPBR_OK;
+  if (used % per) return set_error(MJPBR_ERR_CUDA, "stage profile: %zu events for %zu per chunk (an event could not be created)", used, per);
+  cudaError_t e = cudaEventSynchronize(p.events[used - 1]);
+  if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "stage profile: %s", cudaGetErrorString(e));
+  for (size_t c = 0; c < used / per; ++c) {
+    for (int k = 0; k < kStages; ++k) {
+      float ms = 0.0f;
+      e = cudaEventElapsedTime(&ms, p.events[c * per + k], p.events[c * per + k + 1]);
+      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "stage profile: %s", cudaGetErrorString(e));
+      stage_ms[k] += ms;
+    }
+  }
+  *chunks = (int32_t)(used / per);
+  return MJPBR_OK;
+}
 
 extern "C" int64_t mjpbr_wave_scratch_bytes(const MjpbrScene* scene, int32_t worlds) {
   if (!scene) return -1;

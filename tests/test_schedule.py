@@ -68,7 +68,7 @@ def test_queue_schedule_renders_the_grid_images(name):
   from tests import helpers
 
   sc = _scenes()[name]
-  m, d, rc = helpers.gpu_scene(sc)
+  m, d, rc = helpers.gpu_scene(sc, schedule="grid")
   ref = _frame(m, d, rc)
   for item in (32, 64, 128):
     rc.schedule, rc.queue_item = 1, item
@@ -114,8 +114,12 @@ def test_autotune_picks_a_shape_that_renders_the_same_image():
 
 @pytest.mark.gpu
 @pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
-@pytest.mark.parametrize("tier", [0, 1])
-def test_captured_frame_replays_the_eager_frame(tier):
+@pytest.mark.parametrize(
+  "opts",
+  [{"schedule": "queue"}, {"schedule": "wavefront"}, {"tier": 1, "path_samples": 2, "max_depth": 2, "denoise": True}],
+  ids=["queue", "wavefront", "path"],
+)
+def test_captured_frame_replays_the_eager_frame(opts):
   """A graph of step (a copy of the next poses) -> refit -> render (-> denoise) replays to the
   images the eager calls render for those poses."""
   import mujoco_warp_pbr_gb300 as mjpbr
@@ -123,7 +127,6 @@ def test_captured_frame_replays_the_eager_frame(tier):
   from tests import helpers
 
   sc = synthetic.primitive_scene(seed=5, nworld=4, res=32)
-  opts = {"schedule": "queue"} if tier == 0 else {"tier": 1, "path_samples": 2, "max_depth": 2, "denoise": True}
   m, d, rc = helpers.gpu_scene(sc, **opts)
   poses_a = d.geom_xpos.clone()
   poses_b = poses_a.clone()

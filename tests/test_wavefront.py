@@ -173,3 +173,26 @@ def test_wavefront_context_with_translucent_layers_renders_with_the_megakernel()
   assert rc.wave_scratch is None
   for key in ref:
     np.testing.assert_array_equal(got[key], ref[key], err_msg=key)
+
+
+def test_wavefront_tile_mapping_covers_each_sample_once():
+  """The wavefront kernels' sample mapping (csrc/render_wave.cu): index idx of a 16 x 16 tile
+  with nn samples per pixel is pixel q = idx / nn in Z order, sample idx % nn. Every (pixel,
+  sample) of the tile is visited once, a pixel's samples sit on consecutive indices, and 32
+  consecutive pixels form an 8 x 4 block (8 a 4 x 2 block): the rays of a warp stay close."""
+
+  def z_x(q):
+    return (q & 1) | ((q >> 1) & 2) | ((q >> 2) & 4) | ((q >> 3) & 8)
+
+  def z_y(q):
+    return ((q >> 1) & 1) | ((q >> 2) & 2) | ((q >> 3) & 4) | ((q >> 4) & 8)
+
+  assert sorted((z_x(q), z_y(q)) for q in range(256)) == [(x, y) for x in range(16) for y in range(16)]
+  for nn in (1, 4, 9):
+    seen = [(z_x(idx // nn), z_y(idx // nn), idx % nn) for idx in range(256 * nn)]
+    assert len(set(seen)) == 256 * nn
+  for size, (bw, bh) in ((32, (8, 4)), (8, (4, 2))):
+    for start in range(0, 256, size):
+      xs = {z_x(q) for q in range(start, start + size)}
+      ys = {z_y(q) for q in range(start, start + size)}
+      assert len(xs) == bw and len(ys) == bh and max(xs) - min(xs) == bw - 1 and max(ys) - min(ys) == bh - 1

@@ -7,7 +7,8 @@ points on the same scene, twice in a row.
 The caller's own world blocks are filled with NaN and both scratch pointers are left out of the
 descriptor before the static call, so the images can only match if the static memory is what the
 kernels read. The queue schedule of the real-time tier (work counter slot 1) and the path tier
-(slot 0) both run through it.
+(slot 0) both run through it; a context on the wavefront schedule (whose ray queues live in
+caller scratch) renders through it with the grid schedule, to the same images.
 
 Collected last (file name) so it also runs after every other GPU test in one process."""
 
@@ -32,11 +33,12 @@ def _outputs(rc):
 @pytest.mark.parametrize(
   "opts",
   [
-    {},
+    {"schedule": "grid"},
     {"schedule": "queue", "queue_item": 64},
+    {"schedule": "wavefront"},
     {"tier": 1, "path_samples": 3, "max_depth": 3},
   ],
-  ids=["realtime_grid", "realtime_queue", "path"],
+  ids=["realtime_grid", "realtime_queue", "realtime_wavefront", "path"],
 )
 def test_static_scratch_matches_allocating_path(opts):
   import mujoco_warp_pbr_gb300 as mjpbr
