@@ -589,7 +589,8 @@ def rt_fp32_roofline(args, dev, npix: int, render_ms: float, count_worlds: int =
   scene = mjpbr.scene_descriptor(m, d, rc)
   counts = roofline.count_frame(scene, 1000, torch.cuda.current_stream(dev).cuda_stream)
   counted = sc.nworld * sum(w * h for w, h in rc.base.cam_res)
-  return roofline.fp32_roofline(counts, counted, npix, render_ms)
+  kernel = "wavefront render (all stages)" if rc.schedule == 2 and not rc.has_transparency else "rt_kernel"
+  return roofline.fp32_roofline(counts, counted, npix, render_ms, kernel=kernel)
 
 
 WEIGHTS = ROOT / "mujoco_warp_pbr_gb300" / "weights" / "kpcn_path.npz"

@@ -14,8 +14,10 @@
 //
 // Each stage has its own small register budget and instruction footprint, and its warps run one
 // kind of work (the megakernel interleaves traversal, texturing and shading in every warp and is
-// bound by instruction fetch and divergence). Queues are filled with one atomic per warp
-// (__ballot_sync / __popc offsets). The shading of stage 6 is the megakernel's own code (rt_shade.cuh)
+// bound by instruction fetch and divergence). Queues are filled with one atomic per CTA
+// (__ballot_sync / __popc offsets within a warp, a shared-memory scan over the warps), so each
+// CTA's entries form one run in its pixel order and the tracing warps get neighbouring rays of one
+// world. The shading of stage 6 is the megakernel's own code (rt_shade.cuh)
 // with the shadow visibility read from the counts instead of traced where it is needed, and the
 // rays of stages 3-5 are set up by the same functions, so the images are bit-identical to the
 // megakernel's. Translucent layers are not staged: contexts with has_transparency render with the
@@ -173,20 +175,31 @@ MJ_DEV Surface unpack_surface(const SurfRec& r, V3* normal, float* dist) {
   return sf;
 }
 
-// Appends one entry per lane with `want` to a queue: one atomic per warp, entries of a warp
-// contiguous in lane order. Every lane of the warp must make the call. Returns the lane's slot or
-// -1 (no entry, or the queue is full: kErrWorkQueue).
-MJ_DEV int64_t warp_append(bool want, int32_t* counter, int64_t cap, int32_t* err) {
+// Appends one entry per thread with `want` to a queue as one contiguous run per CTA (warps in
+// order, lanes in order within a warp): one atomic per CTA, and the entries of a run stay in the
+// CTA's pixel order, so a warp of the consuming kernel gets neighbouring rays of one world. Every
+// thread of the CTA must make the call; `scan` is kThreads / 32 + 1 ints of shared memory.
+MJ_DEV int64_t cta_append(bool want, int32_t* counter, int64_t cap, int32_t* scan, int32_t* err) {
   const unsigned full = 0xffffffffu;
   const unsigned m = __ballot_sync(full, want);
-  if (m == 0) return -1;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  int32_t base = 0;
-  if (lane == leader) base = atomicAdd(counter, __popc(m));
-  base = __shfl_sync(full, base, leader);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kWarps = kThreads / 32;
+  if (lane == 0) scan[warp] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t total = 0;
+    for (int k = 0; k < kWarps; ++k) {
+      const int32_t c = scan[k];
+      scan[k] = total;
+      total += c;
+    }
+    scan[kWarps] = total > 0 ? atomicAdd(counter, total) : 0;
+  }
+  __syncthreads();
+  const int64_t base = (int64_t)scan[kWarps] + scan[warp];
+  __syncthreads();  // scan is reused by the next call
   if (!want) return -1;
-  const int64_t pos = (int64_t)base + __popc(m & ((1u << lane) - 1u));
+  const int64_t pos = base + __popc(m & ((1u << lane) - 1u));
   if (pos >= cap) {
     *err |= kErrWorkQueue;
     return -1;
@@ -215,9 +228,9 @@ MJ_DEV uint32_t pixel_seed_of(const MjpbrScene& s, uint32_t seed, int32_t w, int
 }
 
 // Shadow entries of a shaded surface: one per model light whose visibility the shading will ask
-// for (shadow_setup), all lanes of the warp calling.
+// for (shadow_setup), every thread of the CTA calling.
 MJ_DEV void emit_shadows(const MjpbrScene& s, const WaveMap& wm, const float* blk, const BlockLayout& L, bool shaded, V3 point,
-                         V3 normal, int32_t sample, int32_t seg, int32_t* err) {
+                         V3 normal, int32_t sample, int32_t seg, int32_t* scan, int32_t* err) {
   const V3 origin = point + normal * kRayOffset;
   for (int32_t li = 0; li < L.nlight; ++li) {
     V3 l = v3(0.0f);
@@ -227,7 +240,7 @@ MJ_DEV void emit_shadows(const MjpbrScene& s, const WaveMap& wm, const float* bl
       const Light light = load_light(blk + L.light_off + li * kLightFloats);
       want = light.active && shadow_setup(s.settings, light, point, normal, &l, &dist);
     }
-    const int64_t pos = warp_append(want, wm.counters + 1, wm.shadow_cap, err);
+    const int64_t pos = cta_append(want, wm.counters + 1, wm.shadow_cap, scan, err);
     if (pos >= 0) {
       ShadowEntry e;
       e.o = make_float4(origin.x, origin.y, origin.z, dist);
@@ -286,6 +299,7 @@ template <bool kMesh, bool kTex>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_surface_kernel(const __grid_constant__ MjpbrScene s,
                                                                 const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
+  __shared__ int32_t scan[kThreads / 32 + 1];
   float* blk = smem;
   const int32_t w = wm.w0 + blockIdx.y;
   stage_world_block(s, w, blk, kThreads);
@@ -342,8 +356,8 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_surface_
         }
       }
     }
-    emit_shadows(s, wm, blk, L, shaded, point, normal, sample, 0, &err);
-    const int64_t pos = warp_append(reflect, wm.counters, wm.mirror_cap, &err);
+    emit_shadows(s, wm, blk, L, shaded, point, normal, sample, 0, scan, &err);
+    const int64_t pos = cta_append(reflect, wm.counters, wm.mirror_cap, scan, &err);
     if (pos >= 0) {
       MirrorEntry e;
       e.o = make_float4(so.x, so.y, so.z, cone);
@@ -380,10 +394,11 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_mirror_k
 template <bool kMesh, bool kTex>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_mirror_surface_kernel(const __grid_constant__ MjpbrScene s,
                                                                        const __grid_constant__ WaveMap wm) {
+  __shared__ int32_t scan[kThreads / 32 + 1];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const int32_t count = (int32_t)min((int64_t)*wm.counters, wm.mirror_cap);
   int32_t err = 0;
-  // uniform trip count per warp (the shadow entries are appended by whole warps)
+  // uniform trip count per CTA (the shadow entries are appended by whole CTAs)
   const int32_t stride = gridDim.x * kThreads;
   const int32_t rounds = (count + stride - 1) / stride;
   for (int32_t r = 0; r < rounds; ++r) {
@@ -410,7 +425,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_mirror_s
         shaded = true;
       }
     }
-    emit_shadows(s, wm, blk, L, shaded, point, normal, sample, 1, &err);
+    emit_shadows(s, wm, blk, L, shaded, point, normal, sample, 1, scan, &err);
   }
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
@@ -827,3 +842,10 @@ extern "C" int64_t mjpbr_wave_scratch_bytes(const MjpbrScene* scene, int32_t wor
   if (!scene) return -1;
   return mjpbr::wave_scratch_bytes(*scene, worlds);
 }
+
+#ifdef MJPBR_COUNT_OPS
+namespace mjpbr {
+// Counting build: this unit's copy of the counter array pointer (see opcount.cuh).
+int wave_count_set(void* counts) { return cudaMemcpyToSymbol(g_op_counts, &counts, sizeof(counts)) == cudaSuccess ? 0 : 1; }
+}  // namespace mjpbr
+#endif
