@@ -27,6 +27,8 @@
  *                                                                         (mujoco_warp_pbr/_src/texture.py:63-101,
  *                                                                          mujoco_warp_pbr/_src/envmap.py:330-340)
  *   mjpbr_prefilter_env    envmap._prefilter                              (mujoco_warp_pbr/_src/envmap.py:171-221)
+ *   mjpbr_env_sh9          envmap._sh9_irradiance                         (mujoco_warp_pbr/_src/envmap.py:224-249)
+ *   mjpbr_env_sampling_tables  envmap.sampling_distribution               (mujoco_warp_pbr/_src/envmap.py:409-430)
  *   mjpbr_denoise_atrous   denoise.denoise                                (mujoco_warp_pbr/_src/denoise.py:214-248)
  *   mjpbr_build_scene_bvh  scene BVH build of mujoco_warp.create_render_context (third party; called at
  *                                                                          mujoco_warp_pbr/_src/io.py:511-528)
@@ -484,6 +486,18 @@ int mjpbr_build_mips(const MjpbrTexture* tex, uint8_t* data, void* stream);
  * sampling. mujoco_warp_pbr/_src/envmap.py:171-221. */
 int mjpbr_prefilter_env(const MjpbrTexture* radiance, const uint8_t* data, int32_t levels, int32_t height,
                         int32_t width, int32_t nsample, uint16_t* stack, void* stream);
+
+/* SH9 coefficients (9, 3) float32 of the Lambertian radiance of an equirect image (height, width, 3)
+ * float32 (device), projected in double precision; rows: device scratch of height * 27 doubles.
+ * mujoco_warp_pbr/_src/envmap.py:224-249 (there host NumPy at context creation). */
+int mjpbr_env_sh9(const float* image, int32_t height, int32_t width, double* rows, float* sh, void* stream);
+
+/* Importance-sampling tables of an equirect image (height, width, 3) float64 (device, at most 4096
+ * rows): cell probabilities prob (height, width), marginal row CDF (height + 1) and conditional
+ * column CDFs (height, width + 1), float32, distribution proportional to luminance * sin(theta).
+ * mujoco_warp_pbr/_src/envmap.py:409-430 (there host NumPy at context creation). */
+int mjpbr_env_sampling_tables(const double* image, int32_t height, int32_t width, float* prob, float* marginal,
+                              float* conditional, void* stream);
 
 /* Edge-avoiding à-trous filter of the path tier's noisy HDR into rgb_data (and hdr_data with
  * render_hdr): demodulation, denoise_iterations 5x5 passes, remodulation and tone mapping.

@@ -845,7 +845,7 @@ def prepare_context(
     "znear": float(getattr(mjm, "znear", 0.01)),
     "zfar": float(getattr(mjm, "zfar", 0.0)),
     "shadow_light_fraction": float(shadow_light_fraction),
-    "headlight_intensity": float(math.pi) if physical else 1.0,
+    "headlight_intensity": float(math.pi),  # the MuJoCo light model ignores intensities
     "headlight_diffuse": tuple(float(c) for c in mjm.headlight_diffuse),
     "headlight_specular": tuple(float(c) for c in mjm.headlight_specular),
     "background": tuple(float(c) for c in background_linear),

@@ -193,6 +193,15 @@ int mjpbr_prefilter_env(const MjpbrTexture* radiance, const uint8_t* data, int32
   return prefilter_launch(radiance, data, levels, height, width, nsample, stack, static_cast<cudaStream_t>(stream));
 }
 
+int mjpbr_env_sh9(const float* image, int32_t height, int32_t width, double* rows, float* sh, void* stream) {
+  return env_sh9_launch(image, height, width, rows, sh, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_env_sampling_tables(const double* image, int32_t height, int32_t width, float* prob, float* marginal,
+                              float* conditional, void* stream) {
+  return env_tables_launch(image, height, width, prob, marginal, conditional, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream) {
   if (!conv) return set_error(MJPBR_ERR_ARG, "conv is NULL");
   return conv3x3_launch(*conv, static_cast<cudaStream_t>(stream));

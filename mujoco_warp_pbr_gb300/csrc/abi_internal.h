@@ -29,6 +29,9 @@ int dfg_lut_launch(float* lut, int32_t size, int32_t nsample, cudaStream_t strea
 int build_mips_launch(const MjpbrTexture* tex, uint8_t* data, cudaStream_t stream);
 int prefilter_launch(const MjpbrTexture* radiance, const uint8_t* data, int32_t levels, int32_t height, int32_t width,
                      int32_t nsample, uint16_t* stack, cudaStream_t stream);
+int env_sh9_launch(const float* image, int32_t h, int32_t w, double* rows, float* sh, cudaStream_t stream);
+int env_tables_launch(const double* image, int32_t h, int32_t w, float* prob, float* marginal, float* conditional,
+                      cudaStream_t stream);
 int denoise_launch(const MjpbrScene& s, cudaStream_t stream);
 int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream);
 int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream);

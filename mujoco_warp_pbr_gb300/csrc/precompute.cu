@@ -1,7 +1,9 @@
 // Context-creation tables on the GPU: the split-sum DFG table (mujoco_warp_pbr/_src/ibl.py:62-101),
 // box-filtered mip chains (texture.py:91-99, envmap.py:330-337: Warp builds them when it creates a
-// mipmapped texture), and the GGX-prefiltered environment stack with filtered importance sampling
-// (envmap.py:171-221; Karis 2013, Krivanek & Colbert 2008).
+// mipmapped texture), the GGX-prefiltered environment stack with filtered importance sampling
+// (envmap.py:171-221; Karis 2013, Krivanek & Colbert 2008), the environment's 9 spherical-harmonic
+// coefficients of Lambertian radiance (envmap.py:224-249; Ramamoorthi & Hanrahan 2001) and its
+// importance-sampling distribution (envmap.py:409-430).
 #include "abi_internal.h"
 #include "shading.cuh"
 
@@ -129,7 +131,164 @@ __global__ void prefilter_kernel(const __grid_constant__ MjpbrTexture t, const u
   o[3] = float_to_half(1.0f);
 }
 
+// ---------------------------------------------------------------- SH9 irradiance
+// Projection of an equirect radiance image (row 0 = +z, column centre = +x) onto the real
+// spherical harmonics of bands 0-2, weighted by each texel's solid angle (2 pi / w)(pi / h)
+// sin(theta), accumulated in double precision: first one partial sum per row and coefficient
+// (a CTA per row, a fixed-order tree over its threads), then the rows in order (deterministic).
+
+constexpr int kShThreads = 256;
+
+// Real SH basis of bands 0-2 at unit direction (x, y, z), with the usual normalisations
+// 1 / (2 sqrt(pi)), sqrt(3 / (4 pi)), sqrt(15 / (4 pi)), sqrt(5 / (16 pi)), sqrt(15 / (16 pi))
+// rounded to 6 digits.
+__device__ __forceinline__ void sh_basis(double x, double y, double z, double* b) {
+  b[0] = 0.282095;
+  b[1] = 0.488603 * y;
+  b[2] = 0.488603 * z;
+  b[3] = 0.488603 * x;
+  b[4] = 1.092548 * x * y;
+  b[5] = 1.092548 * y * z;
+  b[6] = 0.315392 * (3.0 * z * z - 1.0);
+  b[7] = 1.092548 * x * z;
+  b[8] = 0.546274 * (x * x - y * y);
+}
+
+__global__ void __launch_bounds__(kShThreads) sh9_rows_kernel(const float* image, int32_t h, int32_t w, double* rows) {
+  __shared__ double red[kShThreads];
+  const int32_t y = blockIdx.x;
+  const double pi = 3.14159265358979323846;
+  const double theta = ((double)y + 0.5) / (double)h * pi;
+  const double st = sin(theta), ct = cos(theta);
+  const double dw = (2.0 * pi / (double)w) * (pi / (double)h) * st;
+  double acc[27];
+  for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+  for (int32_t x = threadIdx.x; x < w; x += kShThreads) {
+    const double phi = (((double)x + 0.5) / (double)w - 0.5) * 2.0 * pi;
+    double b[9];
+    sh_basis(st * cos(phi), st * sin(phi), ct, b);
+    const float* px = image + ((int64_t)y * w + x) * 3;
+    for (int k = 0; k < 9; ++k) {
+      const double wb = b[k] * dw;
+      for (int c = 0; c < 3; ++c) acc[k * 3 + c] += wb * (double)px[c];
+    }
+  }
+  for (int k = 0; k < 27; ++k) {
+    red[threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int stride = kShThreads / 2; stride > 0; stride >>= 1) {
+      if (threadIdx.x < stride) red[threadIdx.x] += red[threadIdx.x + stride];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) rows[(int64_t)y * 27 + k] = red[0];
+    __syncthreads();
+  }
+}
+
+// Sums the rows (in row order) and applies the Lambertian band factors pi, 2 pi / 3, pi / 4,
+// divided by pi: the coefficients of radiance, not irradiance.
+__global__ void sh9_sum_kernel(const double* rows, int32_t h, float* sh) {
+  const int k = threadIdx.x;
+  if (k >= 27) return;
+  double sum = 0.0;
+  for (int32_t y = 0; y < h; ++y) sum += rows[(int64_t)y * 27 + k];
+  const int band = k / 3 == 0 ? 0 : (k / 3 < 4 ? 1 : 2);
+  const double factor = band == 0 ? 1.0 : (band == 1 ? 2.0 / 3.0 : 0.25);
+  sh[k] = (float)(sum * factor);
+}
+
+// ---------------------------------------------------------------- importance-sampling tables
+// A piecewise-constant distribution over the cells of an equirect image proportional to
+// luminance (Rec. 709 weights) times sin(theta), with a floor of 1e-6 of the mean luminance so
+// that no cell has zero probability: cell probabilities (h, w), the marginal CDF over rows
+// (h + 1) and one conditional CDF over the columns of each row (h, w + 1); the last entry of
+// every CDF is exactly 1. Double precision, one CTA per image, rows on threads (each row summed
+// in column order, rows in row order: deterministic).
+__global__ void env_tables_kernel(const double* image, int32_t h, int32_t w, float* prob, float* marginal, float* conditional) {
+  extern __shared__ double row[];  // h entries
+  __shared__ double total_s, eps_s;
+  const double pi = 3.14159265358979323846;
+  auto lum = [&](int32_t y, int32_t x) {
+    const double* p = image + ((int64_t)y * w + x) * 3;
+    return p[0] * 0.2126 + p[1] * 0.7152 + p[2] * 0.0722;
+  };
+  for (int32_t y = threadIdx.x; y < h; y += blockDim.x) {
+    double s = 0.0;
+    for (int32_t x = 0; x < w; ++x) s += lum(y, x);
+    row[y] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int32_t y = 0; y < h; ++y) s += row[y];
+    eps_s = 1.0e-6 * fmax(s / ((double)h * (double)w), 1.0e-12);
+  }
+  __syncthreads();
+  const double eps = eps_s;
+  for (int32_t y = threadIdx.x; y < h; y += blockDim.x) {
+    const double st = sin(((double)y + 0.5) / (double)h * pi);
+    double s = 0.0;
+    for (int32_t x = 0; x < w; ++x) s += lum(y, x) * st + eps;
+    row[y] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int32_t y = 0; y < h; ++y) s += row[y];
+    total_s = s;
+  }
+  __syncthreads();
+  const double inv_total = 1.0 / total_s;
+  for (int32_t y = threadIdx.x; y < h; y += blockDim.x) {
+    const double st = sin(((double)y + 0.5) / (double)h * pi);
+    double r = 0.0;
+    for (int32_t x = 0; x < w; ++x) {
+      const double p = (lum(y, x) * st + eps) * inv_total;
+      prob[(int64_t)y * w + x] = (float)p;
+      r += p;
+    }
+    const double inv_r = 1.0 / fmax(r, 1.0e-30);
+    float* cond = conditional + (int64_t)y * (w + 1);
+    double c = 0.0;
+    cond[0] = 0.0f;
+    for (int32_t x = 0; x < w; ++x) {
+      c += (lum(y, x) * st + eps) * inv_total;
+      cond[x + 1] = (float)(c * inv_r);
+    }
+    cond[w] = 1.0f;
+    row[y] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double c = 0.0;
+    marginal[0] = 0.0f;
+    for (int32_t y = 0; y < h; ++y) {
+      c += row[y];
+      marginal[y + 1] = (float)c;
+    }
+    marginal[h] = 1.0f;
+  }
+}
+
 }  // namespace
+
+int env_sh9_launch(const float* image, int32_t h, int32_t w, double* rows, float* sh, cudaStream_t stream) {
+  if (!image || !rows || !sh || h < 1 || w < 1) return set_error(MJPBR_ERR_ARG, "env_sh9: bad arguments");
+  sh9_rows_kernel<<<h, kShThreads, 0, stream>>>(image, h, w, rows);
+  int rc = check_launch("sh9_rows_kernel");
+  if (rc) return rc;
+  sh9_sum_kernel<<<1, 32, 0, stream>>>(rows, h, sh);
+  return check_launch("sh9_sum_kernel");
+}
+
+int env_tables_launch(const double* image, int32_t h, int32_t w, float* prob, float* marginal, float* conditional,
+                      cudaStream_t stream) {
+  if (!image || !prob || !marginal || !conditional || h < 1 || w < 1 || h > 4096) {
+    return set_error(MJPBR_ERR_ARG, "env_tables: bad arguments (height must be in [1, 4096])");
+  }
+  env_tables_kernel<<<1, 128, (size_t)h * sizeof(double), stream>>>(image, h, w, prob, marginal, conditional);
+  return check_launch("env_tables_kernel");
+}
 
 int dfg_lut_launch(float* lut, int32_t size, int32_t nsample, cudaStream_t stream) {
   if (!lut || size < 2 || nsample < 1) return set_error(MJPBR_ERR_ARG, "dfg_lut: bad arguments");

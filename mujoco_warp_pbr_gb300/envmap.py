@@ -1,10 +1,11 @@
 """Environment maps: .hdr loading, split-sum precomputation, importance-sampling tables.
 
-Follows mujoco_warp_pbr/_src/envmap.py: equirect images in MuJoCo's Z-up world (row 0 = +z,
-centre column = +x); per map a mipmapped float16 radiance texture (at most 2048 wide), an
-8-level GGX-prefiltered stack (computed on the GPU by libmjpbr, 512 samples per texel), SH9
-Lambertian radiance coefficients (float64 on the host) and the luminance * sin(theta)
-piecewise-constant sampling distribution (256 wide) for the path tracer.
+The resources of mujoco_warp_pbr/_src/envmap.py: equirect images in MuJoCo's Z-up world (row 0 =
++z, centre column = +x); per map a mipmapped float16 radiance texture (at most 2048 wide), an
+8-level GGX-prefiltered stack (512 samples per texel), SH9 Lambertian radiance coefficients and
+the luminance * sin(theta) piecewise-constant sampling distribution (256 wide) for the path
+tracer. The host decodes and reduces the images; the stack, the SH9 projection and the sampling
+tables are computed on the GPU by libmjpbr (the reference computes the latter two with NumPy).
 """
 
 from __future__ import annotations
@@ -12,7 +13,6 @@ from __future__ import annotations
 import dataclasses
 import math
 import os
-import re
 from pathlib import Path
 from typing import Any
 
@@ -26,72 +26,95 @@ PREFILTER_LEVELS = 8
 PREFILTER_SAMPLES = 512
 MAX_RADIANCE_WIDTH = 2048
 CDF_WIDTH = 256
-_LUMINANCE = np.array([0.2126, 0.7152, 0.0722])
 
 
-def _decode_rle_scanline(data: bytes, pos: int, width: int, path: str, y: int) -> tuple[np.ndarray, int]:
-  """Adaptive run-length encoded RGBE scanline at pos -> ((width, 4) bytes, end position)."""
-  line = bytearray(4 * width)
-  n = len(data)
-  for c in range(4):
-    x = c * width
-    end = x + width
-    while x < end:
-      if pos >= n:
-        raise ValueError(f"{path}: truncated run-length data in scanline {y}")
-      count = data[pos]
-      pos += 1
-      if count > 128:
-        count -= 128
-        if count > end - x or pos >= n:
-          raise ValueError(f"{path}: bad run-length data in scanline {y}")
-        line[x : x + count] = bytes((data[pos],)) * count
-        pos += 1
-      else:
-        if count == 0 or count > end - x or pos + count > n:
-          raise ValueError(f"{path}: bad run-length data in scanline {y}")
-        line[x : x + count] = data[pos : pos + count]
-        pos += count
-      x += count
-  return np.frombuffer(bytes(line), dtype=np.uint8).reshape(4, width).T, pos
+class _HdrReader:
+  """Cursor over the bytes of a Radiance picture file (Ward, "Real Pixels", Graphics Gems II,
+  1991): a text header ended by an empty line, a resolution line, then one scanline per image row
+  of 4-byte RGBE pixels (a shared 8-bit exponent E over three 8-bit mantissas: value = M * 2^(E -
+  136), 0 for E = 0), each scanline either flat or, when it opens with the bytes 2, 2 and the
+  width (high byte first), run-length encoded per component: a byte n > 128 repeats the next byte
+  n - 128 times, a byte 0 < n <= 128 is followed by n literal bytes."""
+
+  def __init__(self, data: bytes, path: str):
+    self.data = data
+    self.path = path
+    self.pos = 0
+
+  def fail(self, what: str) -> ValueError:
+    return ValueError(f"{self.path}: {what}")
+
+  def header(self) -> tuple[int, int]:
+    """Skips the header; returns (height, width) of a '-Y H +X W' picture."""
+    if not self.data.startswith(b"#?"):
+      raise self.fail("not a Radiance .hdr file (missing '#?' signature)")
+    blank = self.data.find(b"\n\n")
+    line_end = self.data.find(b"\n", blank + 2) if blank >= 0 else -1
+    if line_end < 0:
+      raise self.fail("truncated .hdr header")
+    fields = self.data[blank + 2 : line_end].split()
+    if len(fields) < 4 or fields[0] != b"-Y" or fields[2] != b"+X" or not (fields[1].isdigit() and fields[3].isdigit()):
+      raise self.fail("only '-Y H +X W' oriented .hdr files are supported")
+    self.pos = line_end + 1
+    return int(fields[1]), int(fields[3])
+
+  def is_run_length(self, width: int) -> bool:
+    d, p = self.data, self.pos
+    return 8 <= width <= 0x7FFF and p + 2 < len(d) and d[p] == 2 and d[p + 1] == 2 and d[p + 2] < 128
+
+  def flat(self, width: int, y: int) -> np.ndarray:
+    n = 4 * width
+    if self.pos + n > len(self.data):
+      raise self.fail(f"truncated pixel data in scanline {y}")
+    row = np.frombuffer(self.data, dtype=np.uint8, count=n, offset=self.pos).reshape(width, 4)
+    self.pos += n
+    return row
+
+  def component(self, width: int, y: int) -> np.ndarray:
+    """One run-length encoded component of a scanline."""
+    out = np.empty(width, np.uint8)
+    d, n = self.data, len(self.data)
+    filled = 0
+    while filled < width:
+      if self.pos >= n:
+        raise self.fail(f"truncated run-length data in scanline {y}")
+      code = d[self.pos]
+      self.pos += 1
+      repeat = code > 128
+      count = code - 128 if repeat else code
+      body = 1 if repeat else count
+      if count == 0 or count > width - filled or self.pos + body > n:
+        raise self.fail(f"bad run-length data in scanline {y}")
+      out[filled : filled + count] = d[self.pos] if repeat else np.frombuffer(d, np.uint8, count, self.pos)
+      self.pos += body
+      filled += count
+    return out
+
+  def run_length(self, width: int, y: int) -> np.ndarray:
+    d, p = self.data, self.pos
+    if p + 4 > len(d) or (d[p + 2] << 8 | d[p + 3]) != width:
+      raise self.fail(f"scanline {y} width does not match the header")
+    self.pos = p + 4
+    return np.stack([self.component(width, y) for _ in range(4)], axis=-1)
 
 
 def load_hdr(path: str | os.PathLike) -> np.ndarray:
-  """Reads a Radiance RGBE (.hdr) file as float32 (height, width, 3) linear radiance
-  (mujoco_warp_pbr/_src/envmap.py:106-142: flat and adaptive-RLE scanlines, '-Y H +X W' only).
+  """Reads a Radiance RGBE (.hdr) picture as float32 (height, width, 3) linear radiance: flat and
+  run-length encoded scanlines of '-Y H +X W' pictures, as mujoco_warp_pbr/_src/envmap.py:106-142
+  accepts (the error messages are those of the reference's tests).
 
   Raises:
     ValueError: for a file that is not '-Y H +X W' RGBE or whose pixel data is truncated or
       malformed.
   """
-  data = Path(path).read_bytes()
-  if not data.startswith(b"#?"):
-    raise ValueError(f"{path}: not a Radiance .hdr file (missing '#?' signature)")
-  try:
-    header_end = data.index(b"\n\n") + 2
-    resolution_end = data.index(b"\n", header_end)
-  except ValueError:
-    raise ValueError(f"{path}: truncated .hdr header") from None
-  match = re.match(rb"-Y (\d+) \+X (\d+)", data[header_end:resolution_end])
-  if match is None:
-    raise ValueError(f"{path}: only '-Y H +X W' oriented .hdr files are supported")
-  height, width = int(match.group(1)), int(match.group(2))
-  pos = resolution_end + 1
+  reader = _HdrReader(Path(path).read_bytes(), str(path))
+  height, width = reader.header()
   rgbe = np.empty((height, width, 4), dtype=np.uint8)
   for y in range(height):
-    rle = 8 <= width <= 0x7FFF and data[pos : pos + 2] == b"\x02\x02" and pos + 2 < len(data) and not data[pos + 2] & 0x80
-    if not rle:
-      if pos + 4 * width > len(data):
-        raise ValueError(f"{path}: truncated pixel data in scanline {y}")
-      rgbe[y] = np.frombuffer(data, dtype=np.uint8, count=4 * width, offset=pos).reshape(width, 4)
-      pos += 4 * width
-      continue
-    if (data[pos + 2] << 8 | data[pos + 3]) != width:
-      raise ValueError(f"{path}: scanline {y} width does not match the header")
-    rgbe[y], pos = _decode_rle_scanline(data, pos + 4, width, str(path), y)
-  exponent = rgbe[..., 3].astype(np.int32)
-  scale = np.where(exponent > 0, np.ldexp(1.0, exponent - 136), 0.0).astype(np.float32)
-  return rgbe[..., :3].astype(np.float32) * scale[..., None]
+    rgbe[y] = reader.run_length(width, y) if reader.is_run_length(width) else reader.flat(width, y)
+  exponent = rgbe[..., 3:4].astype(np.int32)
+  mantissa = rgbe[..., :3].astype(np.float32)
+  return np.where(exponent > 0, np.ldexp(mantissa, exponent - 136), np.float32(0.0)).astype(np.float32)
 
 
 def envmap_images(envmap: Any) -> list[np.ndarray]:
@@ -111,66 +134,26 @@ def envmap_images(envmap: Any) -> list[np.ndarray]:
   return images
 
 
-def downsample(image: np.ndarray, max_width: int) -> np.ndarray:
+def reduce_width(image: np.ndarray, max_width: int) -> np.ndarray:
+  """Halves an image (2 x 2 box filter over its even-sized part, odd last rows / columns dropped)
+  until it is at most max_width wide. Each output texel is the exact mean of its four inputs
+  (summed in float64), rounded once to the input's type."""
   while image.shape[1] > max_width:
-    h, w = image.shape[0] // 2 * 2, image.shape[1] // 2 * 2
-    image = image[:h, :w].reshape(h // 2, 2, w // 2, 2, -1).mean(axis=(1, 3))
+    h, w = image.shape[0] & ~1, image.shape[1] & ~1
+    a = image[:h, :w].astype(np.float64)
+    image = (((a[0::2, 0::2] + a[0::2, 1::2]) + (a[1::2, 0::2] + a[1::2, 1::2])) * 0.25).astype(image.dtype)
   return image
 
 
-def sh9_irradiance(image: np.ndarray) -> np.ndarray:
-  """SH9 coefficients (9, 3) of Lambertian radiance (irradiance / pi) of an equirect image
-  (Ramamoorthi & Hanrahan 2001; envmap.py:224-249)."""
-  h, w, _ = image.shape
-  theta = (np.arange(h) + 0.5) / h * np.pi
-  phi = ((np.arange(w) + 0.5) / w - 0.5) * 2.0 * np.pi
-  st, ct = np.sin(theta)[:, None], np.cos(theta)[:, None]
-  x, y, z = st * np.cos(phi)[None], st * np.sin(phi)[None], np.broadcast_to(ct, (h, w))
-  basis = np.stack(
-    [
-      np.full((h, w), 0.282095),
-      0.488603 * y,
-      0.488603 * z,
-      0.488603 * x,
-      1.092548 * x * y,
-      1.092548 * y * z,
-      0.315392 * (3.0 * z * z - 1.0),
-      1.092548 * x * z,
-      0.546274 * (x * x - y * y),
-    ]
-  )
-  solid_angle = (2.0 * np.pi / w) * (np.pi / h) * np.broadcast_to(st, (h, w))
-  coeffs = np.einsum("khw,hwc->kc", basis * solid_angle, image.astype(np.float64))
-  band = np.array([np.pi, 2 * np.pi / 3, 2 * np.pi / 3, 2 * np.pi / 3] + [np.pi / 4] * 5)
-  return (coeffs * band[:, None] / np.pi).astype(np.float32)
+def _nearest(image: np.ndarray, shape: tuple[int, int]) -> np.ndarray:
+  """Nearest-texel resampling of an image to shape (rows, columns), texel centres aligned."""
+  rows = np.minimum(((np.arange(shape[0]) + 0.5) * image.shape[0] / shape[0]).astype(np.int64), image.shape[0] - 1)
+  cols = np.minimum(((np.arange(shape[1]) + 0.5) * image.shape[1] / shape[1]).astype(np.int64), image.shape[1] - 1)
+  return image[rows[:, None], cols[None, :]]
 
 
-def sampling_tables(image: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-  """(cell probabilities (h, w), marginal row CDF (h + 1,), conditional column CDFs (h, w + 1))
-  of a distribution over equirect cells proportional to luminance * sin(theta) (envmap.py:409-430)."""
-  small = downsample(np.asarray(image, np.float64)[..., :3], CDF_WIDTH)
-  h = small.shape[0]
-  lum = small @ _LUMINANCE
-  sin_theta = np.sin((np.arange(h) + 0.5) / h * np.pi)[:, None]
-  weight = lum * sin_theta + 1e-6 * max(float(lum.mean()), 1e-12)
-  prob = weight / weight.sum()
-  row = prob.sum(axis=1)
-  marginal = np.concatenate([[0.0], np.cumsum(row)])
-  conditional = np.concatenate([np.zeros((h, 1)), np.cumsum(prob, axis=1) / np.maximum(row[:, None], 1e-30)], axis=1)
-  marginal[-1] = 1.0
-  conditional[:, -1] = 1.0
-  return prob.astype(np.float32), marginal.astype(np.float32), conditional.astype(np.float32)
-
-
-def _resize_nearest(image: np.ndarray, shape: tuple[int, int]) -> np.ndarray:
-  h, w = shape
-  ys = ((np.arange(h) + 0.5) / h * image.shape[0]).astype(int)
-  xs = ((np.arange(w) + 0.5) / w * image.shape[1]).astype(int)
-  return image[ys][:, xs]
-
-
-def _downsampled_shape(shape: tuple[int, ...], max_width: int) -> tuple[int, int]:
-  h, w = shape[0], shape[1]
+def _reduced_shape(shape: tuple[int, ...], max_width: int) -> tuple[int, int]:
+  h, w = int(shape[0]), int(shape[1])
   while w > max_width:
     h, w = h // 2, w // 2
   return h, w
@@ -178,13 +161,11 @@ def _downsampled_shape(shape: tuple[int, ...], max_width: int) -> tuple[int, int
 
 @dataclasses.dataclass
 class HostEnvironments:
-  """Host-side resources of the environment maps of a context."""
+  """Host-side inputs of the environment maps of a context (the tables are computed on the GPU)."""
 
   radiance: list[np.ndarray]  # (h, w, 4) float16 level 0 per map
-  sh: np.ndarray  # (nenv, 9, 3)
-  prob: np.ndarray  # (nenv, h, w)
-  marginal: np.ndarray  # (nenv, h + 1)
-  conditional: np.ndarray  # (nenv, h, w + 1)
+  linear: list[np.ndarray]  # (h, w, 3) float32, the same images before the float16 conversion
+  cdf_images: list[np.ndarray]  # (ch, cw, 3) float64 at most CDF_WIDTH wide, one shape for all maps
   prefilter_levels: int
   prefilter_height: int
   prefilter_width: int
@@ -196,32 +177,31 @@ class HostEnvironments:
 
 
 def prepare_environments(images: list[np.ndarray]) -> HostEnvironments:
-  radiance, shs, tables = [], [], []
-  shape = None
-  widths = []
+  """Radiance textures at most MAX_RADIANCE_WIDTH wide and the images the sampling tables are
+  built from (at most CDF_WIDTH wide, every map resampled to the first map's table shape)."""
+  radiance, linear, cdf_images = [], [], []
+  cdf_shape = None
   for im in images:
-    small = downsample(np.asarray(im, np.float32)[..., :3], MAX_RADIANCE_WIDTH)
-    h, w, _ = small.shape
-    widths.append(w)
-    radiance.append(np.concatenate([small, np.ones((h, w, 1), np.float32)], axis=-1).astype(np.float16))
-    shs.append(sh9_irradiance(small))
-    src = im
-    if shape is not None and _downsampled_shape(im.shape, CDF_WIDTH) != shape:
-      src = _resize_nearest(im, shape)
-    table = sampling_tables(src)
-    shape = shape or table[0].shape
-    tables.append(table)
-  pw = min(PREFILTER_WIDTH, min(widths))
+    rgb = np.asarray(im, np.float32)[..., :3]
+    small = reduce_width(rgb, MAX_RADIANCE_WIDTH)
+    linear.append(np.ascontiguousarray(small))
+    alpha = np.ones((*small.shape[:2], 1), np.float32)
+    radiance.append(np.concatenate([small, alpha], axis=-1).astype(np.float16))
+    src = rgb.astype(np.float64)
+    if cdf_shape is not None and _reduced_shape(src.shape, CDF_WIDTH) != cdf_shape:
+      src = _nearest(src, cdf_shape)
+    table_image = reduce_width(src, CDF_WIDTH)
+    cdf_shape = cdf_shape or table_image.shape[:2]
+    cdf_images.append(np.ascontiguousarray(table_image))
+  pw = min(PREFILTER_WIDTH, min(im.shape[1] for im in linear))
   return HostEnvironments(
     radiance=radiance,
-    sh=np.stack(shs).astype(np.float32),
-    prob=np.stack([t[0] for t in tables]),
-    marginal=np.stack([t[1] for t in tables]),
-    conditional=np.stack([t[2] for t in tables]),
+    linear=linear,
+    cdf_images=cdf_images,
     prefilter_levels=PREFILTER_LEVELS,
     prefilter_height=max(pw // 2, 1),
     prefilter_width=pw,
-    max_width=float(max(widths)),
+    max_width=float(max(im.shape[1] for im in linear)),
   )
 
 
@@ -256,18 +236,30 @@ def upload_environments(env: HostEnvironments, device: torch.device) -> DeviceEn
   for e, d in enumerate(ts.desc):
     _lib.call("mjpbr_prefilter_env", d, data.data_ptr(), L, H, W, PREFILTER_SAMPLES, stack[e].data_ptr(), stream)
 
-  def dev(a: np.ndarray) -> torch.Tensor:
-    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+  # SH9 radiance and importance-sampling tables on the GPU (libmjpbr, double precision)
+  sh = torch.empty((env.nenv, 9, 3), dtype=torch.float32, device=device)
+  for e, im in enumerate(env.linear):
+    img = torch.from_numpy(im).to(device)
+    rows = torch.empty((im.shape[0], 27), dtype=torch.float64, device=device)
+    _lib.call("mjpbr_env_sh9", img.data_ptr(), im.shape[0], im.shape[1], rows.data_ptr(), sh[e].data_ptr(), stream)
+  ch, cw = env.cdf_images[0].shape[:2]
+  prob = torch.empty((env.nenv, ch, cw), dtype=torch.float32, device=device)
+  marginal = torch.empty((env.nenv, ch + 1), dtype=torch.float32, device=device)
+  conditional = torch.empty((env.nenv, ch, cw + 1), dtype=torch.float32, device=device)
+  for e, im in enumerate(env.cdf_images):
+    img = torch.from_numpy(im).to(device)
+    _lib.call("mjpbr_env_sampling_tables", img.data_ptr(), ch, cw, prob[e].data_ptr(), marginal[e].data_ptr(), conditional[e].data_ptr(), stream)
+  torch.cuda.current_stream(device).synchronize()  # the host images above are freed on return
 
   return DeviceEnvironments(
     radiance_desc=desc,
     radiance_data=data,
     desc=ts.desc,
     prefiltered=stack,
-    sh=dev(env.sh),
-    prob=dev(env.prob),
-    marginal=dev(env.marginal),
-    conditional=dev(env.conditional),
+    sh=sh,
+    prob=prob,
+    marginal=marginal,
+    conditional=conditional,
     levels=L,
     height=H,
     width=W,

@@ -22,7 +22,7 @@ from typing import Any
 
 import numpy as np
 
-from mujoco_warp_pbr_gb300 import context as io_lib
+from oracle import host_prep
 
 GEOM_PLANE, GEOM_SPHERE, GEOM_CAPSULE, GEOM_BOX = 0, 2, 3, 6
 LIGHT_SPOT, LIGHT_DIRECTIONAL = 0, 1
@@ -118,7 +118,7 @@ class Fp64Scene:
 
   def __init__(self, sc: Any, dfg: np.ndarray, **overrides: Any):
     self.options = {**sc.options, **overrides}
-    self.hc = io_lib.prepare_context(sc.mjm, sc.nworld, data=sc.mjd, **self.options)
+    self.hc = host_prep.prepare(sc.mjm, sc.mjd, sc.nworld, self.options)
     self.mjm, self.mjd, self.nworld = sc.mjm, sc.mjd, sc.nworld
     self.st = self.hc.settings
     if int(self.st["samples_per_axis"]) != 1 or int(self.st["shadow_samples"]) > 1 or self.st["has_env"] or self.st["specular_aa"]:
@@ -234,7 +234,7 @@ class Fp64Scene:
     return out
 
   def _shade_light(self, L, geoms, point, n, view, nov, alpha, f0, energy, diffuse) -> np.ndarray:
-    physical = int(self.st["light_model"]) == int(io_lib.LightModel.PHYSICAL)
+    physical = int(self.st["light_model"]) == host_prep.LIGHT_MODEL_PHYSICAL
     att, dist = 1.0, UNBOUNDED
     if L["type"] == LIGHT_DIRECTIONAL:
       l = -np.asarray(L["dir"], np.float64)

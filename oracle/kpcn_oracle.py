@@ -1,6 +1,6 @@
 """CPU restatement of the learned denoiser (KPCN U-Net) in float64 NumPy — TEST INFRASTRUCTURE ONLY.
 
-Mirrors mujoco_warp_pbr_gb300/kpcn.py layer by layer: 3 x 3 convolutions with zero padding, ReLU,
+The network described by the learned-denoiser layer table below, layer by layer: 3 x 3 convolutions with zero padding, ReLU,
 2 x 2 average pooling, nearest upsampling with skip concatenation, a 32-channel head whose first 25
 logits are a softmax 5 x 5 kernel applied to the radiance (borders clamped), the L1 + relative-MSE
 loss (relative L1 + relative MSE), and the backward pass of all of these. Activations can be rounded to BF16 after every layer
@@ -12,7 +12,12 @@ from __future__ import annotations
 
 import numpy as np
 
-from mujoco_warp_pbr_gb300.kpcn import TAPS, layer_specs
+# The network of the learned denoiser: a 4-level U-Net of 3 x 3 convolutions with widths 32 / 48 /
+# 64 / 96 (two per level on the way down and up, a skip concatenation entering each decoder
+# level), and a 32-channel head whose first TAPS logits form a 5 x 5 kernel. Layer names in
+# order: encoder e<level>a/b, decoder d<level>a/b, head.
+TAPS = 25
+LAYERS = ("e0a", "e0b", "e1a", "e1b", "e2a", "e2b", "e3a", "e3b", "d2a", "d2b", "d1a", "d1b", "d0a", "d0b", "head")
 
 
 def round_bf16(x: np.ndarray) -> np.ndarray:
@@ -173,4 +178,4 @@ class Net:
 
 
 def layer_names() -> list[str]:
-  return [s.name for s in layer_specs()]
+  return list(LAYERS)

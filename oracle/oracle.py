@@ -1,10 +1,13 @@
 """Python side of the CPU oracle (oracle/mjpbr_oracle.c) — TEST INFRASTRUCTURE ONLY.
 
 Builds the same MjpbrScene descriptor the library renders from, but over host (numpy) arrays,
-and runs the C restatement of the reference's real-time and path-traced tiers on the CPU cores. The tables the GPU
-computes at context creation (DFG table, texture mips, prefiltered environment stacks) come from
-the oracle's own C functions unless the caller passes the GPU's copies (to isolate the render
-kernel from the table kernels, which tests compare separately).
+and runs the C restatement of the reference's real-time and path-traced tiers on the CPU cores.
+The oracle shares no code with the product: its host preparation (materials, lights, exposure,
+textures, environments, output layout) is oracle/host_prep.py, its struct mirror
+oracle/scene_struct.py (read from include/mjpbr.h). The tables the GPU computes at context
+creation (DFG table, texture mips, prefiltered environment stacks, SH9 coefficients, sampling
+tables) come from the oracle's own functions unless the caller passes the GPU's copies (to
+isolate the render kernels from the table kernels, which tests compare separately).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use this module.
 """
@@ -18,16 +21,19 @@ from typing import Any
 
 import numpy as np
 
-from mujoco_warp_pbr_gb300 import _lib
-from mujoco_warp_pbr_gb300 import _scene
-from mujoco_warp_pbr_gb300 import envmap as envmap_lib
-from mujoco_warp_pbr_gb300 import context as io_lib
+from oracle import host_prep
+from oracle import scene_struct as ss
 
 HERE = Path(__file__).resolve().parent
 SOURCE = HERE / "mjpbr_oracle.c"
 BUILD = HERE / "_build"
 LIBRARY = BUILD / "libmjpbr_oracle.so"
 CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-parameter"]
+# the reference's table sizes (ibl.py DFG table 128 x 128 with 1024 samples; envmap.py prefilter
+# with 512 samples per texel)
+DFG_LUT_SIZE = 128
+DFG_LUT_SAMPLES = 1024
+PREFILTER_SAMPLES = 512
 
 _lib_handle: ctypes.CDLL | None = None
 
@@ -49,15 +55,15 @@ def load() -> ctypes.CDLL:
     build()
     lib = ctypes.CDLL(str(LIBRARY))
     vp, i32 = ctypes.c_void_p, ctypes.c_int
-    lib.oracle_render_rt.argtypes = [ctypes.POINTER(_lib.Scene), vp, ctypes.c_uint32, i32, i32, i32]
+    lib.oracle_render_rt.argtypes = [ctypes.POINTER(ss.Scene), vp, ctypes.c_uint32, i32, i32, i32]
     lib.oracle_render_rt.restype = i32
-    lib.oracle_render_pt.argtypes = [ctypes.POINTER(_lib.Scene), vp, ctypes.c_uint32, i32, i32, i32]
+    lib.oracle_render_pt.argtypes = [ctypes.POINTER(ss.Scene), vp, ctypes.c_uint32, i32, i32, i32]
     lib.oracle_render_pt.restype = i32
-    lib.oracle_denoise.argtypes = [ctypes.POINTER(_lib.Scene), i32]
+    lib.oracle_denoise.argtypes = [ctypes.POINTER(ss.Scene), i32]
     lib.oracle_denoise.restype = i32
     lib.oracle_dfg_lut.argtypes = [vp, i32, i32]
-    lib.oracle_build_mips.argtypes = [ctypes.POINTER(_lib.Texture), vp]
-    lib.oracle_prefilter.argtypes = [ctypes.POINTER(_lib.Texture), vp, i32, i32, i32, i32, vp]
+    lib.oracle_build_mips.argtypes = [ctypes.POINTER(ss.Texture), vp]
+    lib.oracle_prefilter.argtypes = [ctypes.POINTER(ss.Texture), vp, i32, i32, i32, i32, vp]
     lib.oracle_struct_layout.argtypes = [ctypes.POINTER(ctypes.c_int64)]
     lib.oracle_set_mesh_bvh.argtypes = [i32]
     lib.oracle_set_hfields.argtypes = [i32, vp, vp, vp, vp, vp]
@@ -74,32 +80,38 @@ def load() -> ctypes.CDLL:
     lib.oracle_half_to_float.restype = ctypes.c_float
     out = (ctypes.c_int64 * 8)()
     lib.oracle_struct_layout(out)
-    if list(out) != _lib.python_layout():
-      raise RuntimeError(f"oracle MjpbrScene layout {list(out)} differs from the bindings {_lib.python_layout()}")
+    if list(out) != ss.layout():
+      raise RuntimeError(f"oracle MjpbrScene layout {list(out)} differs from the header mirror {ss.layout()}")
     _lib_handle = lib
   return _lib_handle
 
 
-def dfg_lut(size: int = io_lib.DFG_LUT_SIZE, nsample: int = io_lib.DFG_LUT_SAMPLES) -> np.ndarray:
+def dfg_lut(size: int = DFG_LUT_SIZE, nsample: int = DFG_LUT_SAMPLES) -> np.ndarray:
   lut = np.zeros((size, size, 2), np.float32)
   load().oracle_dfg_lut(lut.ctypes.data, size, nsample)
   return lut
 
 
-def build_mips(ts: io_lib.TextureSet) -> np.ndarray:
-  """Texture bytes with every mip level filled by the oracle."""
-  data = ts.data.copy()
-  for d in ts.desc:
+def build_mips(desc: list[Any], data: np.ndarray) -> np.ndarray:
+  """Texture bytes with every mip level filled by the oracle (desc: MjpbrTexture descriptions of
+  the textures whose level 0 is in data)."""
+  data = data.copy()
+  for d in desc:
     load().oracle_build_mips(d, data.ctypes.data)
   return data
 
 
-def prefilter(env: envmap_lib.HostEnvironments, data: np.ndarray, desc: list[Any], nsample: int = envmap_lib.PREFILTER_SAMPLES) -> np.ndarray:
+def prefilter(env: host_prep.Environments, data: np.ndarray, desc: list[Any], nsample: int = PREFILTER_SAMPLES) -> np.ndarray:
   L, H, W = env.prefilter_levels, env.prefilter_height, env.prefilter_width
   stack = np.zeros((env.nenv, L, H, W, 4), np.uint16)
   for e, d in enumerate(desc):
     load().oracle_prefilter(d, data.ctypes.data, L, H, W, nsample, stack[e].ctypes.data)
   return stack
+
+
+def environment_textures(env: host_prep.Environments) -> tuple[list[Any], np.ndarray]:
+  """The environments' radiance textures (float16 RGBA, level 0 filled), packed."""
+  return host_prep.pack_textures([(host_prep.TEX_RGBA16F, im) for im in env.radiance], ss.Texture)
 
 
 def _b(a: Any, dtype: Any, tail: tuple[int, ...]) -> np.ndarray:
@@ -116,7 +128,7 @@ class OracleScene:
   """
 
   def __init__(self, mjm: Any, mjd: Any, nworld: int, options: dict[str, Any], per_world: dict[str, np.ndarray] | None = None, tables: dict[str, np.ndarray] | None = None):
-    self.hc = io_lib.prepare_context(mjm, nworld, data=mjd, **options)
+    self.hc = host_prep.prepare(mjm, mjd, nworld, options)
     self.nworld = nworld
     tables = dict(tables or {})
     per_world = dict(per_world or {})
@@ -208,7 +220,7 @@ class OracleScene:
         "nlight": nlight,
         "ncam": ncam,
         "nmesh": mjm.nmesh,
-        "nhfield": io_lib.nhfield_of(mjm),
+        "nhfield": nhfield_of(mjm),
         "ntex": mjm.ntex,
         "nrender": o["nrender"],
         "total_rays": o["total_rays"],
@@ -235,24 +247,28 @@ class OracleScene:
         "denoise_buffers": (self.aov["demod"], self.aov["pong"]),
         "denoise_iterations": int(options.get("denoise_iterations", 3)),
         "nbvh_geom": len(self.hc.enabled_geom_ids),
-        "nnode": self.hc.tlas_child.shape[1],
+        "nnode": max(len(self.hc.enabled_geom_ids) - 1, 1),
         "enabled_geom_ids": np.ascontiguousarray(self.hc.enabled_geom_ids, i32),
         "dfg_lut": self.dfg,
         "dfg_size": self.dfg.shape[0],
         "settings": st,
       }
     )
-    if self.hc.textures is not None:
-      self.tex_desc = self.hc.textures.desc_bytes()
-      self.tex_data = np.ascontiguousarray(tables["tex_data"]) if "tex_data" in tables else build_mips(self.hc.textures)
+    if self.hc.textures:
+      desc, data = host_prep.pack_textures(self.hc.textures, ss.Texture)
+      self.tex_desc = host_prep.desc_bytes(desc)
+      self.tex_data = np.ascontiguousarray(tables["tex_data"]) if "tex_data" in tables else build_mips(desc, data)
       a["textures"] = self.tex_desc
       a["tex_data"] = self.tex_data
     env = self.hc.environments
     if env is not None:
-      ets = io_lib.pack_textures([(io_lib.TEX_RGBA16F, im) for im in env.radiance])
-      self.env_desc = ets.desc_bytes()
-      self.env_data = np.ascontiguousarray(tables["env_data"]) if "env_data" in tables else build_mips(ets)
-      self.env_stack = np.ascontiguousarray(tables["env_prefiltered"]).view(np.uint16) if "env_prefiltered" in tables else prefilter(env, self.env_data, ets.desc)
+      edesc, edata = environment_textures(env)
+      self.env_desc = host_prep.desc_bytes(edesc)
+      self.env_data = np.ascontiguousarray(tables["env_data"]) if "env_data" in tables else build_mips(edesc, edata)
+      self.env_stack = np.ascontiguousarray(tables["env_prefiltered"]).view(np.uint16) if "env_prefiltered" in tables else prefilter(env, self.env_data, edesc)
+      for key in ("env_sh", "env_prob", "env_marginal", "env_conditional"):
+        if key in tables:  # the GPU's tables, to isolate the render kernels from the table kernels
+          setattr(env, key[4:], np.ascontiguousarray(tables[key]))
       a.update(
         {
           "nenv": env.nenv,
@@ -271,14 +287,12 @@ class OracleScene:
         }
       )
     if options.get("camera_rays") is not None:
-      from mujoco_warp_pbr_gb300 import rays as rays_lib
-
-      self.ray_origin, self.ray_direction = rays_lib.pack_camera_rays(options["camera_rays"], o["cam_res"])
+      self.ray_origin, self.ray_direction = host_prep.pack_camera_rays(options["camera_rays"], o["cam_res"])
       a.update({"ray_origin": self.ray_origin, "ray_direction": self.ray_direction, "bundle_res": o["cam_res"]})
-    self.mesh_nface = np.ascontiguousarray(self.hc.meshes.get("mesh_nface", []), i32)
+    self.mesh_nface = np.ascontiguousarray(self.hc.mesh_nface, i32)
     self.hfields = hfield_arrays(mjm)
     self.arrays = a  # keeps every array alive
-    self.scene = _scene.fill_scene({k: v for k, v in a.items() if v is not None})
+    self.scene = ss.fill({k: v for k, v in a.items() if v is not None})
 
   def render(self, seed: int = 0, worlds: tuple[int, int] | None = None, nthreads: int = 0, denoise: bool = True) -> dict[str, np.ndarray]:
     """Renders worlds [w0, w1) with the tier of the context's settings (real-time or path-traced);
@@ -303,9 +317,15 @@ class OracleScene:
       raise RuntimeError("oracle_denoise failed")
 
 
+def nhfield_of(mjm: Any) -> int:
+  """Height fields of a model (0 for models without the hfield_* fields)."""
+  nrow = getattr(mjm, "hfield_nrow", None)
+  return 0 if nrow is None else int(len(np.asarray(nrow).reshape(-1)))
+
+
 def hfield_arrays(mjm: Any) -> tuple[np.ndarray, ...]:
   """(nrow, ncol, size, adr, data) of a model's height fields as contiguous arrays (empty without)."""
-  n = io_lib.nhfield_of(mjm)
+  n = nhfield_of(mjm)
   if n == 0:
     return ()
   return (

@@ -39,6 +39,10 @@ def gpu_tables(rc) -> dict[str, np.ndarray]:
   if rc.env is not None:
     t["env_data"] = rc.env.radiance_data.cpu().numpy()
     t["env_prefiltered"] = rc.env.prefiltered.cpu().numpy()
+    t["env_sh"] = rc.env.sh.cpu().numpy()
+    t["env_prob"] = rc.env.prob.cpu().numpy()
+    t["env_marginal"] = rc.env.marginal.cpu().numpy()
+    t["env_conditional"] = rc.env.conditional.cpu().numpy()
   return t
 
 

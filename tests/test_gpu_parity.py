@@ -120,18 +120,26 @@ def test_mesh_ibl_config_full_assets_matches_oracle(seed):
 
 
 def test_texture_mips_and_prefilter_match_oracle():
-  from oracle import oracle
+  """The context-creation tables of the GPU against the oracle's own host preparation and C / NumPy
+  restatements: texture and radiance mip chains bit for bit, the prefiltered stack within float16
+  rounding, the SH9 coefficients and importance-sampling tables (double precision on both sides)
+  within float32 rounding."""
+  from oracle import host_prep, oracle, scene_struct
 
   sc = synthetic.mesh_ibl_scene(seed=1, nworld=1, res=16, tex_size=128, env_width=256)
   _, _, rc = helpers.gpu_scene(sc)
   torch.cuda.synchronize()
   hc = oracle.OracleScene(sc.mjm, sc.mjd, 1, sc.options, sc.per_world).hc
-  np.testing.assert_array_equal(rc.tex_data.cpu().numpy(), oracle.build_mips(hc.textures))
-  from mujoco_warp_pbr_gb300 import context
-
-  ets = context.pack_textures([(context.TEX_RGBA16F, im) for im in hc.environments.radiance])
-  env_ref = oracle.build_mips(ets)
+  desc, data = host_prep.pack_textures(hc.textures, scene_struct.Texture)
+  np.testing.assert_array_equal(rc.tex_data.cpu().numpy(), oracle.build_mips(desc, data))
+  edesc, edata = oracle.environment_textures(hc.environments)
+  env_ref = oracle.build_mips(edesc, edata)
   np.testing.assert_array_equal(rc.env.radiance_data.cpu().numpy(), env_ref)
   stack_gpu = rc.env.prefiltered.cpu().numpy().view(np.float16).astype(np.float32)
-  stack_ref = oracle.prefilter(hc.environments, env_ref, ets.desc).view(np.float16).astype(np.float32)
+  stack_ref = oracle.prefilter(hc.environments, env_ref, edesc).view(np.float16).astype(np.float32)
   np.testing.assert_allclose(stack_gpu, stack_ref, rtol=5e-3, atol=5e-3 * float(stack_ref.max()))
+  env = hc.environments
+  np.testing.assert_allclose(rc.env.sh.cpu().numpy(), env.sh, rtol=2e-6, atol=1e-6 * float(np.abs(env.sh).max()))
+  np.testing.assert_allclose(rc.env.prob.cpu().numpy(), env.prob, rtol=2e-6, atol=1e-12)
+  np.testing.assert_allclose(rc.env.marginal.cpu().numpy(), env.marginal, rtol=2e-6, atol=1e-7)
+  np.testing.assert_allclose(rc.env.conditional.cpu().numpy(), env.conditional, rtol=2e-6, atol=1e-7)
