@@ -499,6 +499,14 @@ int mjpbr_env_sh9(const float* image, int32_t height, int32_t width, double* row
 int mjpbr_env_sampling_tables(const double* image, int32_t height, int32_t width, float* prob, float* marginal,
                               float* conditional, void* stream);
 
+/* Failure-detection check of the library's bounded device waits (the mbarrier waits of the
+ * tensor-core kernels): one CTA whose roles wait on mbarriers that nothing completes, each wait
+ * bounded by `polls` (1 .. 2^20); the first to give up raises the CTA's abort flag, which releases
+ * the other roles, and kErrWaitTimeout (4) is ORed into *error_word (device int32); each of
+ * the three roles adds 1 to *roles_done (device int32) when it returns. The context stays usable.
+ * No counterpart in the reference (its kernels have no device waits). */
+int mjpbr_wait_probe(uint32_t polls, int32_t* error_word, int32_t* roles_done, void* stream);
+
 /* Edge-avoiding à-trous filter of the path tier's noisy HDR into rgb_data (and hdr_data with
  * render_hdr): demodulation, denoise_iterations 5x5 passes, remodulation and tone mapping.
  * mujoco_warp_pbr/_src/denoise.py:214-248. Uses scene.denoise_buffers as scratch. */

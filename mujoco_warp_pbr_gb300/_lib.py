@@ -302,6 +302,7 @@ _SIGNATURES = {
   "mjpbr_wave_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(Scene), c_i32]),
   "mjpbr_env_sh9": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp, c_vp, c_vp]),
   "mjpbr_env_sampling_tables": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
+  "mjpbr_wait_probe": (ctypes.c_int, [ctypes.c_uint32, c_vp, c_vp, c_vp]),
   "mjpbr_wave_profile_begin": (ctypes.c_int, []),
   "mjpbr_wave_profile_end": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_i32)]),
   "mjpbr_refit_bvh": (ctypes.c_int, [ctypes.POINTER(Scene), c_vp]),

@@ -17,6 +17,7 @@ simulation loop replays the whole frame with a single launch from the host.
 from __future__ import annotations
 
 import dataclasses
+import time
 from collections.abc import Callable
 from typing import Any
 
@@ -86,11 +87,16 @@ def apply(rc: PbrRenderContext, shape: LaunchShape) -> None:
     rc.wave_scratch = None  # sized again for the new chunk at the next render
 
 
-def autotune(m: Any, d: Any, rc: PbrRenderContext, frames: int = 3, candidates: tuple[LaunchShape, ...] = CANDIDATES, use_cache: bool = True) -> dict:
+def autotune(
+  m: Any, d: Any, rc: PbrRenderContext, frames: int = 3, candidates: tuple[LaunchShape, ...] = CANDIDATES, use_cache: bool = True,
+  timeout_ms: float = 10_000.0,
+) -> dict:
   """Times every launch shape on this scene (after one warm-up frame each) and applies the
-  fastest to rc. Returns {"best": description, "ms": {description: ms per frame}}. Shapes the
-  library rejects for this scene (the queue's per-warp world blocks must fit shared memory) are
-  skipped. The path-traced tier has a single persistent schedule: nothing to tune."""
+  fastest to rc. Returns {"best": description, "ms": {description: ms per frame}, "skipped":
+  {description: reason}}. Shapes whose launch the library rejects or fails for this scene (the
+  queue's per-warp world blocks must fit shared memory), and shapes whose warm-up frame takes
+  longer than timeout_ms on the host clock, are skipped. The path-traced tier has a single
+  persistent schedule: nothing to tune."""
   if rc.tier != 0:
     return {"best": "path tier: persistent tile queue", "ms": {}}
   key = _signature(rc)
@@ -100,11 +106,19 @@ def autotune(m: Any, d: Any, rc: PbrRenderContext, frames: int = 3, candidates: 
   refit_bvh(m, d, rc)
   stream = torch.cuda.current_stream(rc.device)
   timings: dict[LaunchShape, float] = {}
+  skipped: dict[str, str] = {}
   for shape in candidates:
     apply(rc, shape)
+    t0 = time.perf_counter()
     try:
       render(m, d, rc)
-    except ValueError:
+      torch.cuda.synchronize(rc.device)
+    except (ValueError, _lib.MjpbrError) as e:
+      skipped[shape.describe()] = str(e)
+      continue
+    warm_ms = (time.perf_counter() - t0) * 1000.0
+    if warm_ms > timeout_ms:
+      skipped[shape.describe()] = f"warm-up frame took {warm_ms:.0f} ms (limit {timeout_ms:.0f} ms)"
       continue
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
@@ -115,11 +129,11 @@ def autotune(m: Any, d: Any, rc: PbrRenderContext, frames: int = 3, candidates: 
     end.synchronize()
     timings[shape] = start.elapsed_time(end) / frames
   if not timings:
-    raise RuntimeError("no launch shape could render this scene")
+    raise RuntimeError(f"no launch shape could render this scene: {skipped}")
   best = min(timings, key=timings.get)
   apply(rc, best)
   _cache[key] = best
-  return {"best": best.describe(), "ms": {k.describe(): v for k, v in timings.items()}}
+  return {"best": best.describe(), "ms": {k.describe(): v for k, v in timings.items()}, "skipped": skipped}
 
 
 def capture_frame(

@@ -116,6 +116,38 @@ int validate_scene(const MjpbrScene* s, bool need_outputs) {
       }
       if (s->render_seg[c] && (s->seg_adr[c] < 0 || !s->seg_data)) return set_error(MJPBR_ERR_ARG, "seg buffer missing");
     }
+    // The pixel maps the kernels index with: every camera image must lie inside its output rows and
+    // inside the per-world ray range, and the flattened (world, ray) indices must fit 32 bits.
+    int64_t rays = 0;
+    for (int32_t c = 0; c < s->nrender; ++c) {
+      const int64_t npix = (int64_t)s->cam_res[c][0] * s->cam_res[c][1];
+      rays += npix;
+      if (s->ray_adr[c] < 0 || s->ray_adr[c] + npix > s->total_rays) {
+        return set_error(MJPBR_ERR_ARG, "pixel map: camera %d rays [%d, %lld) outside total_rays %d", c, s->ray_adr[c],
+                         (long long)(s->ray_adr[c] + npix), s->total_rays);
+      }
+      const struct {
+        bool on;
+        int32_t adr, stride;
+        const char* name;
+      } maps[3] = {{s->render_rgb[c] != 0, s->rgb_adr[c], s->rgb_stride, "rgb"},
+                   {s->render_depth[c] != 0, s->depth_adr[c], s->depth_stride, "depth"},
+                   {s->render_seg[c] != 0, s->seg_adr[c], s->seg_stride, "seg"}};
+      for (const auto& m : maps) {
+        if (m.on && (int64_t)m.adr + npix > m.stride) {
+          return set_error(MJPBR_ERR_ARG, "pixel map: camera %d %s pixels [%d, %lld) outside the row of %d", c, m.name, m.adr,
+                           (long long)(m.adr + npix), m.stride);
+        }
+      }
+    }
+    if (rays > s->total_rays || (int64_t)s->total_rays * s->nworld >= (int64_t(1) << 31)) {
+      return set_error(MJPBR_ERR_ARG, "pixel map: %d worlds x %d rays overflow the 32-bit ray index", s->nworld, s->total_rays);
+    }
+    if (st.schedule == MJPBR_SCHEDULE_QUEUE && st.tier == MJPBR_TIER_REALTIME &&
+        st.queue_item != 32 && st.queue_item != 64 && st.queue_item != 128) {
+      return set_error(MJPBR_ERR_ARG, "work queue: items of %d pixels; 32, 64 or 128", st.queue_item);
+    }
+    if (s->wave_scratch_bytes < 0) return set_error(MJPBR_ERR_ARG, "wave_scratch_bytes is negative");
   }
   return MJPBR_OK;
 }
@@ -200,6 +232,10 @@ int mjpbr_env_sh9(const float* image, int32_t height, int32_t width, double* row
 int mjpbr_env_sampling_tables(const double* image, int32_t height, int32_t width, float* prob, float* marginal,
                               float* conditional, void* stream) {
   return env_tables_launch(image, height, width, prob, marginal, conditional, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_wait_probe(uint32_t polls, int32_t* error_word, int32_t* roles_done, void* stream) {
+  return wait_probe_launch(polls, error_word, roles_done, static_cast<cudaStream_t>(stream));
 }
 
 int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream) {

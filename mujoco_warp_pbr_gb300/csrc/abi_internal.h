@@ -35,6 +35,7 @@ int env_tables_launch(const double* image, int32_t h, int32_t w, float* prob, fl
 int denoise_launch(const MjpbrScene& s, cudaStream_t stream);
 int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream);
 int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream);
+int wait_probe_launch(uint32_t polls, int32_t* error_word, int32_t* roles_done, cudaStream_t stream);
 int kpcn_features_launch(const MjpbrScene& s, int32_t cam, int32_t w0, int32_t nw, uint16_t* x0, cudaStream_t st);
 int kpcn_target_launch(const MjpbrScene& s, int32_t cam, const double* hdr_sum, double inv_n, float* target, cudaStream_t st);
 int accumulate_f64_launch(const float* src, double* acc, int64_t n, cudaStream_t st);

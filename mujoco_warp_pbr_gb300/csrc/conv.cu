@@ -275,8 +275,9 @@ __device__ __forceinline__ StageInfo stage_info(int32_t s, int32_t nci, int32_t 
 // Bounded wait that also gives up once another role raised the abort flag. Waiters off the MMA
 // issue path sleep `backoff_ns` between polls, so that polling warps leave the SM's issue slots
 // and memory pipeline to the MMA and copy instructions.
-__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int32_t* abort_flag, uint32_t backoff_ns = 0) {
-  for (uint32_t i = 0; i < umma::kWaitLimit; ++i) {
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int32_t* abort_flag, uint32_t backoff_ns = 0,
+                                        uint32_t limit = umma::kWaitLimit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (umma::mbar_try_wait(bar, parity)) return true;
     if ((i & 255u) == 255u && *abort_flag) return false;
     if (backoff_ns) __nanosleep(backoff_ns);
@@ -1292,6 +1293,56 @@ int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream) {
     return check_launch("bias_grad_kernel");
   }
   return MJPBR_OK;
+}
+
+namespace {
+
+// Failure-detection check of the bounded waits above: one CTA in the roles of the warp-specialised
+// kernels — warp 0 a consumer waiting (ws_wait) on a "full" mbarrier that no producer completes,
+// warp 1 a waiter on a second barrier that only the abort flag releases, warp 2 a plain
+// mbar_wait. Every wait is bounded by `polls`; the first to give up raises the CTA's abort flag,
+// which ends the other role's wait, and the CTA ORs kErrWaitTimeout into the error word and
+// returns. Nothing in it spins without a bound and nothing faults.
+__global__ void __launch_bounds__(96) wait_probe_kernel(uint32_t polls, int32_t* error_word, int32_t* roles_done) {
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ int32_t abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    umma::mbar_init(&bars[0], 1);
+    umma::mbar_init(&bars[1], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  volatile int32_t* abort_v = &abort_flag;
+  bool ok = true;
+  if (lane == 0) {
+    if (warp == 0) {
+      ok = ws_wait(&bars[0], 0, abort_v, 0, polls);
+    } else if (warp == 1) {
+      // released by the abort flag (checked every 256 polls), or gives up after 256 x polls itself
+      ok = ws_wait(&bars[1], 0, abort_v, 0, polls * 256u);
+    } else {
+      ok = umma::mbar_wait(&bars[0], 0, polls);
+    }
+    atomicAdd(roles_done, 1);
+    if (!ok && error_word) atomicOr(error_word, kErrWaitTimeout);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(umma::smem_addr(&bars[0])) : "memory");
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(umma::smem_addr(&bars[1])) : "memory");
+  }
+}
+
+}  // namespace
+
+int wait_probe_launch(uint32_t polls, int32_t* error_word, int32_t* roles_done, cudaStream_t stream) {
+  if (polls < 1 || polls > (1u << 20) || !error_word || !roles_done) {
+    return set_error(MJPBR_ERR_ARG, "wait probe: polls must be in [1, 2^20] and both words given");
+  }
+  wait_probe_kernel<<<1, 96, 0, stream>>>(polls, error_word, roles_done);
+  return check_launch("wait_probe_kernel");
 }
 
 }  // namespace mjpbr

@@ -58,9 +58,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-// Waits for the phase to complete; false if the bounded wait gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+// Waits for the phase to complete; false if the bounded wait gave up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit = kWaitLimit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, phase)) return true;
   }
   return false;
