@@ -79,11 +79,14 @@ enum MjpbrToneMapper { MJPBR_TONE_PBR_NEUTRAL = 0, MJPBR_TONE_ACES = 1, MJPBR_TO
 enum MjpbrLightModel { MJPBR_LIGHT_MODEL_PHYSICAL = 0, MJPBR_LIGHT_MODEL_MUJOCO = 1 };
 enum MjpbrTier { MJPBR_TIER_REALTIME = 0, MJPBR_TIER_PATH = 1 };
 enum MjpbrRenderOrder { MJPBR_ORDER_ROW = 0, MJPBR_ORDER_TILED = 1, MJPBR_ORDER_WORLD = 2 };
-/* Real-time tier schedules: one CTA per (camera tile, world); a persistent launch whose warps
+/* Schedules. Real-time tier: one CTA per (camera tile, world); a persistent launch whose warps
  * pull work items (settings.queue_item pixels of one camera image of one world) from a device
  * counter (scene.work_counter[1]); or a staged wavefront (primary rays, surfaces, mirror rays,
  * shadow rays and shading as separate kernels over compacted ray queues, chunks of worlds at a
- * time in scene.wave_scratch; not for translucent layers). All three render identical images. */
+ * time in scene.wave_scratch; translucent layers render with the grid schedule). Path tier: GRID
+ * and QUEUE select the persistent path kernel, WAVEFRONT the staged bounce loop (extend, shade,
+ * shadow, next-event kernels over compacted path queues in scene.wave_scratch). Every schedule of
+ * a tier renders identical images. */
 enum MjpbrSchedule { MJPBR_SCHEDULE_GRID = 0, MJPBR_SCHEDULE_QUEUE = 1, MJPBR_SCHEDULE_WAVEFRONT = 2 };
 /* Texel formats of MjpbrTexture. */
 enum MjpbrTexFormat { MJPBR_TEX_RGBA8 = 0, MJPBR_TEX_RGBA16F = 1 };
@@ -444,7 +447,7 @@ int mjpbr_adam(float* param, float* grad, float* m, float* v, uint16_t* copy, ui
 /* mjpbr_refit_bvh + mjpbr_render in one call that allocates nothing and takes no scratch from the
  * caller: the per-world blocks and the path tracer's work counter live in static device memory of
  * the library (scene->world_blocks, scene->work_counter and scene->wave_scratch are ignored; the
- * wavefront schedule renders as the grid schedule, with the same images). For hosts that cannot
+ * wavefront schedule renders as the grid schedule / the persistent path kernel, with the same images). For hosts that cannot
  * give the library device memory after start-up (a fixed device-memory arena, a plugin host that
  * owns every allocation). Limit: nworld * world_block_floats <= 4,194,304 (16 MiB), else
  * MJPBR_ERR_ARG. Calls overlapping in time share the static memory and race. The memory belongs

@@ -81,7 +81,7 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
   sources = _sources()
   objects = [BUILD / (src.name + ".o") for src in sources]
   # the counting library: the same objects with the render units compiled with MJPBR_COUNT_OPS
-  counted = {"render_rt.cu", "render_wave.cu", "pathtrace.cu"}
+  counted = {"render_rt.cu", "render_wave.cu", "pathtrace.cu", "pt_wave.cu"}
   count_objs = {name: BUILD / (name + ".count.o") for name in counted}
   jobs_list = [(s, o, ()) for s, o in zip(sources, objects, strict=True) if force or _stale(o, s, newest_header)]
   for name, obj in count_objs.items():

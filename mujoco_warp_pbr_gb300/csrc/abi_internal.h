@@ -22,6 +22,8 @@ int refit_launch(const MjpbrScene& s, cudaStream_t stream);
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
 int render_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
 int64_t wave_scratch_bytes(const MjpbrScene& s, int32_t worlds);
+int render_pt_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
+int64_t pt_wave_scratch_bytes(const MjpbrScene& s, int32_t worlds);
 int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
 int outputs_launch(const MjpbrScene& s, int which, int32_t cam, float depth_scale, void* out, int32_t nworld_out,
                    cudaStream_t stream);

@@ -1,0 +1,648 @@
+// Path-traced tier as a staged wavefront (the schedule MJPBR_SCHEDULE_WAVEFRONT of the path tier):
+// the bounce loop of mujoco_warp_pbr/_src/pathtrace.py:200-421 over every path of a chunk of
+// worlds at once, one kernel per stage and compacted path queues between the bounces:
+//
+//   start    one path per (pixel, sample) of the RGB cameras: the camera ray (pt_bounce.cuh
+//            start_sample); depth / segmentation of cameras without RGB (one ray per pixel)
+//   per bounce, over the queue of live paths:
+//     extend   closest hit of every path; depth / segmentation from sample 0's first hit
+//     shade    the bounce after the hit (PtCore::surface): emission, mirror lobe, next-event
+//              estimation recorded per path (each light's unshadowed contribution and shadow ray,
+//              the environment sample's term and ray), the BSDF sample and Russian roulette;
+//              shadow rays and the paths that continue are appended to queues (one atomic per CTA)
+//     shadow   any hit of every recorded shadow ray
+//     nee      the recorded contributions of the unoccluded rays added to the path's radiance in
+//              light order (the persistent kernel's exact additions)
+//   resolve  one thread per pixel: its samples summed in sample order, tone map / denoiser inputs
+//
+// Each stage runs one kind of work on a full set of lanes and has its own register budget; the
+// image is the persistent kernel's, bit for bit (the random numbers are counter-based per sample
+// and bounce, so the order in which paths run does not matter).
+//
+// Scratch (MjpbrScene.wave_scratch), per path of a chunk: the path state (128 B), its hit (32 B),
+// its next-event record (32 B + 32 B per slot: each light, the headlight, the environment), one
+// visibility byte per slot, two queue entries and up to one shadow entry (32 B) per slot.
+#include <algorithm>
+#include <climits>
+
+#include "abi_internal.h"
+#include "pt_bounce.cuh"
+
+namespace mjpbr {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct __align__(16) PathRec {
+  float4 o;       // origin, max_dist
+  float4 d;       // direction, pdf_prev
+  float4 beta;    // throughput, dcam_z
+  float4 rad;     // radiance, first-hit depth (sample 0)
+  float4 albedo;  // first-surface albedo, depth (int bits)
+  float4 normal;  // first-surface normal, passes (int bits)
+  float4 emis;    // first-surface emission, sample (int bits)
+  float4 base;    // first-surface base colour, flags (int bits: 1 camera ray, 2 delta)
+};
+
+struct __align__(16) HitRec {
+  float dist;
+  int32_t ref;  // -1: miss; else slot | (mesh + 1) << 16
+  int32_t face;
+  float u, v;
+  float nx, ny, nz;
+};
+
+struct __align__(16) ShadowEntry {
+  float4 o;  // origin, ray length
+  float4 d;  // direction, target (int bits): path * nslot + slot
+};
+
+static_assert(sizeof(PathRec) == 128 && sizeof(HitRec) == 32 && sizeof(ShadowEntry) == 32, "record sizes");
+
+// next-event record flags of a slot
+constexpr int32_t kNeeSkip = 0;      // inactive light: nothing added
+constexpr int32_t kNeeZero = 1;      // the light does not reach the point: zero added
+constexpr int32_t kNeeAdd = 2;       // unshadowed contribution: added
+constexpr int32_t kNeeIfVisible = 3; // added if its shadow ray is unoccluded
+
+struct PtWaveMap {
+  int32_t w0, nw;          // worlds of this chunk
+  int32_t nsample;         // samples per pixel
+  int32_t pixels;          // RGB pixels per world
+  int32_t npath;           // paths of this chunk: nw * pixels * nsample
+  int32_t nslot;           // next-event slots: nlight, the headlight, the environment
+  int32_t pix_base[MJPBR_MAX_RENDER];  // first RGB pixel of each camera within a world (-1: no RGB)
+  int32_t geo_base[MJPBR_MAX_RENDER + 1];  // pixels of the cameras without RGB (prefix sums)
+  PathRec* path;
+  HitRec* hit;
+  float4* nee;             // (npath, 2 + 2 * nslot)
+  uint8_t* vis;            // (npath, nslot)
+  int32_t* queue[2];
+  ShadowEntry* shadow;
+  int32_t* counters;       // [0], [1] queue lengths, [2] shadow entries
+  int64_t path_cap, shadow_cap;
+};
+
+MJ_DEV Stack wave_stack(float* base) {
+  Stack st;
+  int32_t* b = reinterpret_cast<int32_t*>(base);
+  st.code = b + threadIdx.x;
+  st.t = reinterpret_cast<float*>(b + kThreads * kStackDepth) + threadIdx.x;
+  st.stride = kThreads;
+  return st;
+}
+
+// World, camera, pixel id and sample of a chunk-local path index (paths: world-major, then RGB
+// pixels in camera order, then samples).
+MJ_DEV void path_pixel(const MjpbrScene& s, const PtWaveMap& wm, int32_t path, int32_t* w, Pixel* p, int32_t* sample) {
+  const int32_t pix_all = path / wm.nsample;
+  *sample = path - pix_all * wm.nsample;
+  const int32_t wl = pix_all / wm.pixels;
+  const int32_t pix = pix_all - wl * wm.pixels;
+  int32_t cam = 0;
+  for (int32_t k = 0; k < s.nrender; ++k) {
+    if (wm.pix_base[k] >= 0 && wm.pix_base[k] <= pix) cam = k;
+  }
+  *w = wm.w0 + wl;
+  p->cam = cam;
+  p->width = s.cam_res[cam][0];
+  p->height = s.cam_res[cam][1];
+  p->pixelid = pix - wm.pix_base[cam];
+  p->px = p->pixelid % p->width;
+  p->py = p->pixelid / p->width;
+}
+
+MJ_DEV const float* world_block(const MjpbrScene& s, int32_t w) { return s.world_blocks + (int64_t)w * s.world_block_floats; }
+
+MJ_DEV uint32_t pixel_seed_of(const MjpbrScene& s, uint32_t seed, int32_t w, const Pixel& p) {
+  return seed + (uint32_t)w * (uint32_t)s.total_rays + (uint32_t)(s.ray_adr[p.cam] + p.pixelid);
+}
+
+MJ_DEV void store_path(PathRec& r, const PathState& ps, float first_depth) {
+  r.o = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.max_dist);
+  r.d = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.pdf_prev);
+  r.beta = make_float4(ps.beta.x, ps.beta.y, ps.beta.z, ps.dcam_z);
+  r.rad = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, first_depth);
+  r.albedo = make_float4(ps.albedo.x, ps.albedo.y, ps.albedo.z, __int_as_float(ps.depth));
+  r.normal = make_float4(ps.normal.x, ps.normal.y, ps.normal.z, __int_as_float(ps.passes));
+  r.emis = make_float4(ps.emission.x, ps.emission.y, ps.emission.z, __int_as_float(ps.sample));
+  r.base = make_float4(ps.base_color.x, ps.base_color.y, ps.base_color.z,
+                       __int_as_float((ps.camera_ray ? 1 : 0) | (ps.delta ? 2 : 0)));
+}
+
+MJ_DEV PathState load_path(const PathRec& r, float* first_depth) {
+  PathState ps;
+  ps.o = V3{r.o.x, r.o.y, r.o.z};
+  ps.max_dist = r.o.w;
+  ps.d = V3{r.d.x, r.d.y, r.d.z};
+  ps.pdf_prev = r.d.w;
+  ps.beta = V3{r.beta.x, r.beta.y, r.beta.z};
+  ps.dcam_z = r.beta.w;
+  ps.radiance = V3{r.rad.x, r.rad.y, r.rad.z};
+  *first_depth = r.rad.w;
+  ps.albedo = V3{r.albedo.x, r.albedo.y, r.albedo.z};
+  ps.depth = __float_as_int(r.albedo.w);
+  ps.normal = V3{r.normal.x, r.normal.y, r.normal.z};
+  ps.passes = __float_as_int(r.normal.w);
+  ps.emission = V3{r.emis.x, r.emis.y, r.emis.z};
+  ps.sample = __float_as_int(r.emis.w);
+  ps.base_color = V3{r.base.x, r.base.y, r.base.z};
+  const int32_t flags = __float_as_int(r.base.w);
+  ps.camera_ray = (flags & 1) != 0;
+  ps.delta = (flags & 2) != 0;
+  return ps;
+}
+
+MJ_DEV HitRec pack_hit(const Hit& h) {
+  HitRec r;
+  r.dist = h.dist;
+  r.ref = h.geom == -1 ? -1 : (h.slot | ((h.mesh + 1) << 16));
+  r.face = h.face;
+  r.u = h.u;
+  r.v = h.v;
+  r.nx = h.normal.x;
+  r.ny = h.normal.y;
+  r.nz = h.normal.z;
+  return r;
+}
+
+MJ_DEV Hit unpack_hit(const HitRec& r, const float* blk, const BlockLayout& L) {
+  Hit h;
+  h.dist = r.dist;
+  if (r.ref == -1) {
+    h.geom = h.slot = h.mesh = h.face = -1;
+    h.u = h.v = 0.0f;
+    h.normal = v3(0.0f);
+    return h;
+  }
+  h.slot = r.ref & 0xffff;
+  h.mesh = (r.ref >> 16) - 1;
+  h.geom = __float_as_int(blk[L.geom_off + h.slot * kGeomFloats + 16]);
+  h.face = r.face;
+  h.u = r.u;
+  h.v = r.v;
+  h.normal = V3{r.nx, r.ny, r.nz};
+  return h;
+}
+
+// Appends one entry per thread with `want` as one contiguous run per CTA (one atomic per CTA;
+// warps in order, lanes in order). Every thread of the CTA must make the call; `scan` holds
+// kThreads / 32 + 1 ints of shared memory. Returns the thread's position or -1.
+MJ_DEV int64_t cta_append(bool want, int32_t* counter, int64_t cap, int32_t* scan, int32_t* err) {
+  const unsigned full = 0xffffffffu;
+  const unsigned m = __ballot_sync(full, want);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kWarps = kThreads / 32;
+  if (lane == 0) scan[warp] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t total = 0;
+    for (int k = 0; k < kWarps; ++k) {
+      const int32_t c = scan[k];
+      scan[k] = total;
+      total += c;
+    }
+    scan[kWarps] = total > 0 ? atomicAdd(counter, total) : 0;
+  }
+  __syncthreads();
+  const int64_t base = (int64_t)scan[kWarps] + scan[warp];
+  __syncthreads();
+  if (!want) return -1;
+  const int64_t pos = base + __popc(m & ((1u << lane) - 1u));
+  if (pos >= cap) {
+    *err |= kErrWorkQueue;
+    return -1;
+  }
+  return pos;
+}
+
+// Next-event estimation of the wavefront: the terms are recorded in the path's record; the
+// shadow rays are traced by the shadow stage and the terms added by the nee stage.
+struct RecordedNee {
+  float4* rec;  // [0] beta, active; [1] origin; per slot [2 + 2k] contribution, flag; [3 + 2k] ray direction, length
+  int32_t nslot;
+  MJ_DEV void begin(const PathState& ps, V3 origin) {
+    rec[0] = make_float4(ps.beta.x, ps.beta.y, ps.beta.z, __int_as_float(0));
+    rec[1] = make_float4(origin.x, origin.y, origin.z, 0.0f);
+    for (int32_t k = 0; k < nslot; ++k) rec[2 + 2 * k].w = __int_as_float(kNeeSkip);
+  }
+  MJ_DEV void none(int32_t slot) { rec[2 + 2 * slot].w = __int_as_float(kNeeZero); }
+  template <class F>
+  MJ_DEV void light(RtCtx&, int32_t slot, bool shadowed, V3, V3 dir, float max_t, F contribution) {
+    const V3 c = contribution();
+    rec[2 + 2 * slot] = make_float4(c.x, c.y, c.z, __int_as_float(shadowed ? kNeeIfVisible : kNeeAdd));
+    rec[3 + 2 * slot] = make_float4(dir.x, dir.y, dir.z, max_t);
+  }
+  MJ_DEV void lights_done(PathState&) { rec[0].w = __int_as_float(1); }
+  template <class F>
+  MJ_DEV void env(RtCtx&, PathState&, V3, V3 dir, F term) {
+    const int32_t slot = nslot - 1;
+    const V3 t = term();
+    rec[2 + 2 * slot] = make_float4(t.x, t.y, t.z, __int_as_float(kNeeIfVisible));
+    rec[3 + 2 * slot] = make_float4(dir.x, dir.y, dir.z, kUnboundedShadow);
+  }
+};
+
+// ---------------------------------------------------------------- start
+__global__ void __launch_bounds__(kThreads) ptw_start_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+                                                             const __grid_constant__ PtWaveMap wm) {
+  const int32_t path = blockIdx.x * kThreads + threadIdx.x;
+  if (path == 0) {
+    wm.counters[0] = wm.npath;
+    wm.counters[1] = 0;
+  }
+  if (path >= wm.npath) return;
+  int32_t w, sample;
+  Pixel p;
+  path_pixel(s, wm, path, &w, &p, &sample);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  p.rec = world_block(s, w) + L.cam_off + p.cam * kCamFloats;
+  const M3 R = cam_mat(p.rec);
+  const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
+  PathState ps;
+  start_sample(ps, s, p, pixel_seed_of(s, seed, w, p), R, cpos, sample);
+  store_path(wm.path[path], ps, 0.0f);
+  wm.queue[0][path] = path;
+}
+
+// ---------------------------------------------------------------- cameras without RGB
+template <bool kMesh>
+__global__ void __launch_bounds__(kThreads) ptw_geometry_kernel(const __grid_constant__ MjpbrScene s,
+                                                                const __grid_constant__ PtWaveMap wm) {
+  extern __shared__ __align__(16) float smem[];
+  const Stack st = wave_stack(smem);
+  const int32_t per_world = wm.geo_base[s.nrender];
+  const int32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= per_world * wm.nw) return;
+  const int32_t wl = i / per_world, pix = i - wl * per_world;
+  int32_t cam = 0;
+  while (cam + 1 < s.nrender && pix >= wm.geo_base[cam + 1]) ++cam;
+  const int32_t w = wm.w0 + wl;
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const float* blk = world_block(s, w);
+  Pixel p;
+  p.cam = cam;
+  p.width = s.cam_res[cam][0];
+  p.height = s.cam_res[cam][1];
+  p.pixelid = pix - wm.geo_base[cam];
+  p.px = p.pixelid % p.width;
+  p.py = p.pixelid / p.width;
+  p.rec = blk + L.cam_off + cam * kCamFloats;
+  const M3 R = cam_mat(p.rec);
+  const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
+  V3 dcam, ocam;
+  float max_dist, depth_z;
+  primary_ray(s, p, kSubpixel, kSubpixel / 2, kSubpixel / 2, &dcam, &ocam, &max_dist, &depth_z);
+  int32_t err = 0;
+  const Hit hit = trace_ray<kMesh>(s, st, blk, L, Ray{cpos + mul(R, ocam), mul(R, dcam)}, max_dist, s.settings.cull_backfaces != 0,
+                                   false, &err);
+  write_geometry(s, w, p, hit, depth_z);
+  if (err && s.error_word) atomicOr(s.error_word, err);
+}
+
+// ---------------------------------------------------------------- extend
+template <bool kMesh>
+__global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_constant__ MjpbrScene s,
+                                                                 const __grid_constant__ PtWaveMap wm, int32_t cur) {
+  extern __shared__ __align__(16) float smem[];
+  const Stack st = wave_stack(smem);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const bool cull = s.settings.cull_backfaces != 0;
+  const int32_t count = (int32_t)min((int64_t)wm.counters[cur], wm.path_cap);
+  int32_t err = 0;
+  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
+    const int32_t path = wm.queue[cur][i];
+    PathRec& r = wm.path[path];
+    const float4 o = r.o, d = r.d;
+    const int32_t sample = __float_as_int(r.emis.w);
+    const int32_t passes = __float_as_int(r.normal.w);
+    const bool camera_ray = (__float_as_int(r.base.w) & 1) != 0;
+    const int32_t pix_all = path / wm.nsample;
+    const int32_t w = wm.w0 + pix_all / wm.pixels;
+    const float* blk = world_block(s, w);
+    const Hit hit = trace_ray<kMesh>(s, st, blk, L, Ray{V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}}, o.w, cull, false, &err);
+    wm.hit[path] = pack_hit(hit);
+    if (camera_ray && passes == 0 && sample == 0) {
+      int32_t ww, smp;
+      Pixel p;
+      path_pixel(s, wm, path, &ww, &p, &smp);
+      const float dcam_z = r.beta.w;
+      write_geometry(s, w, p, hit, dcam_z);
+      if (hit.geom != -1) r.rad.w = hit.dist * -dcam_z;
+    }
+  }
+  if (err && s.error_word) atomicOr(s.error_word, err);
+}
+
+// ---------------------------------------------------------------- shade
+template <bool kMesh, bool kTex>
+__global__ void __launch_bounds__(kThreads, 2) ptw_shade_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+                                                                const __grid_constant__ PtWaveMap wm, int32_t cur) {
+  __shared__ int32_t scan[kThreads / 32 + 1];
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const int32_t next = cur ^ 1;
+  const int32_t count = (int32_t)min((int64_t)wm.counters[cur], wm.path_cap);
+  const int32_t stride = gridDim.x * kThreads;
+  const int32_t rounds = (count + stride - 1) / stride;
+  int32_t err = 0;
+  for (int32_t round = 0; round < rounds; ++round) {
+    const int32_t i = round * stride + blockIdx.x * kThreads + threadIdx.x;
+    int32_t path = -1;
+    bool live = false;
+    float4* rec = nullptr;
+    if (i < count) {
+      path = wm.queue[cur][i];
+      int32_t w, sample;
+      Pixel p;
+      path_pixel(s, wm, path, &w, &p, &sample);
+      const float* blk = world_block(s, w);
+      RtCtx c;
+      init_ctx(c, s, blk, L, w, kTex);
+      p.rec = blk + L.cam_off + p.cam * kCamFloats;
+      const M3 R = cam_mat(p.rec);
+      const V3 head_dir = -V3{R.m[2], R.m[5], R.m[8]};
+      float first_depth;
+      PathState ps = load_path(wm.path[path], &first_depth);
+      const Hit hit = unpack_hit(wm.hit[path], blk, L);
+      rec = wm.nee + (int64_t)path * (2 + 2 * wm.nslot);
+      rec[0].w = __int_as_float(0);
+      RecordedNee nee{rec, wm.nslot};
+      live = !PtCore<kMesh, kTex>::surface(c, nee, ps, hit, pixel_seed_of(s, seed, w, p), head_dir);
+      store_path(wm.path[path], ps, first_depth);
+      err |= c.err;
+    }
+    // the shadow rays of the recorded next-event terms, then the paths that continue
+    const bool active = rec && __float_as_int(rec[0].w) != 0;
+    for (int32_t k = 0; k < wm.nslot; ++k) {
+      const bool want = active && __float_as_int(rec[2 + 2 * k].w) == kNeeIfVisible;
+      const int64_t pos = cta_append(want, wm.counters + 2, wm.shadow_cap, scan, &err);
+      if (pos >= 0) {
+        const float4 o = rec[1], d = rec[3 + 2 * k];
+        ShadowEntry e;
+        e.o = make_float4(o.x, o.y, o.z, d.w);
+        e.d = make_float4(d.x, d.y, d.z, __int_as_float(path * wm.nslot + k));
+        wm.shadow[pos] = e;
+      }
+    }
+    const int64_t pos = cta_append(live, wm.counters + next, wm.path_cap, scan, &err);
+    if (pos >= 0) wm.queue[next][pos] = path;
+  }
+  if (err && s.error_word) atomicOr(s.error_word, err);
+}
+
+// ---------------------------------------------------------------- shadow rays
+template <bool kMesh>
+__global__ void __launch_bounds__(kThreads, 3) ptw_shadow_kernel(const __grid_constant__ MjpbrScene s,
+                                                                 const __grid_constant__ PtWaveMap wm) {
+  extern __shared__ __align__(16) float smem[];
+  const Stack st = wave_stack(smem);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const bool cull = s.settings.cull_backfaces != 0;
+  const int32_t count = (int32_t)min((int64_t)wm.counters[2], wm.shadow_cap);
+  int32_t err = 0;
+  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
+    const ShadowEntry e = wm.shadow[i];
+    const int32_t target = __float_as_int(e.d.w);
+    const int32_t path = target / wm.nslot;
+    const int32_t w = wm.w0 + (path / wm.nsample) / wm.pixels;
+    const Hit hit = trace_ray<kMesh>(s, st, world_block(s, w), L, Ray{V3{e.o.x, e.o.y, e.o.z}, V3{e.d.x, e.d.y, e.d.z}}, e.o.w, cull,
+                                     true, &err);
+    wm.vis[target] = hit.geom == -1 ? 1 : 0;
+  }
+  if (err && s.error_word) atomicOr(s.error_word, err);
+}
+
+// ---------------------------------------------------------------- next-event terms
+__global__ void __launch_bounds__(kThreads) ptw_nee_kernel(const __grid_constant__ MjpbrScene s, const __grid_constant__ PtWaveMap wm,
+                                                           int32_t cur) {
+  const int32_t count = (int32_t)min((int64_t)wm.counters[cur], wm.path_cap);
+  const int32_t nlights = wm.nslot - 1;  // the model's lights and the headlight
+  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
+    const int32_t path = wm.queue[cur][i];
+    const float4* rec = wm.nee + (int64_t)path * (2 + 2 * wm.nslot);
+    const float4 head = rec[0];
+    if (__float_as_int(head.w) == 0) continue;
+    const uint8_t* vis = wm.vis + (int64_t)path * wm.nslot;
+    V3 direct = v3(0.0f);
+    for (int32_t k = 0; k < nlights; ++k) {
+      const float4 c = rec[2 + 2 * k];
+      const int32_t flag = __float_as_int(c.w);
+      if (flag == kNeeSkip) continue;
+      const bool add = flag == kNeeAdd || (flag == kNeeIfVisible && vis[k]);
+      direct += add ? V3{c.x, c.y, c.z} : v3(0.0f);
+    }
+    PathRec& r = wm.path[path];
+    V3 radiance{r.rad.x, r.rad.y, r.rad.z};
+    radiance += cmul(V3{head.x, head.y, head.z}, direct);
+    const float4 e = rec[2 + 2 * nlights];
+    if (__float_as_int(e.w) == kNeeIfVisible && vis[nlights]) radiance += V3{e.x, e.y, e.z};
+    r.rad = make_float4(radiance.x, radiance.y, radiance.z, r.rad.w);
+  }
+}
+
+// ---------------------------------------------------------------- pixels
+template <bool kTex>
+__global__ void __launch_bounds__(kThreads) ptw_resolve_kernel(const __grid_constant__ MjpbrScene s, const __grid_constant__ PtWaveMap wm) {
+  const int32_t pix_all = blockIdx.x * kThreads + threadIdx.x;
+  if (pix_all >= wm.nw * wm.pixels) return;
+  int32_t w, sample;
+  Pixel p;
+  path_pixel(s, wm, pix_all * wm.nsample, &w, &p, &sample);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  RtCtx c;
+  init_ctx(c, s, world_block(s, w), L, w, kTex);
+  PixelAcc acc;
+  clear_pixel(acc);
+  for (int32_t k = 0; k < wm.nsample; ++k) {
+    float first_depth;
+    const PathState ps = load_path(wm.path[(int64_t)pix_all * wm.nsample + k], &first_depth);
+    if (k == 0) acc.first_depth = first_depth;
+    add_sample(acc, ps, s.settings.denoise != 0, c.exposure);
+  }
+  write_pixel(s, c, (int64_t)w * s.rgb_stride + s.rgb_adr[p.cam] + p.pixelid, acc, wm.nsample);
+}
+
+// ---------------------------------------------------------------- host side
+
+int64_t align256(int64_t b) { return (b + 255) & ~int64_t(255); }
+
+int32_t slots_of(const MjpbrScene& s) { return std::max(s.nlight, 0) + 2; }
+
+void rgb_pixels(const MjpbrScene& s, int32_t* pix_base, int32_t* geo_base, int64_t* pixels) {
+  int64_t rgb = 0, geo = 0;
+  geo_base[0] = 0;
+  for (int32_t c = 0; c < s.nrender; ++c) {
+    const int64_t npix = (int64_t)s.cam_res[c][0] * s.cam_res[c][1];
+    pix_base[c] = s.render_rgb[c] ? (int32_t)rgb : -1;
+    if (s.render_rgb[c]) rgb += npix;
+    if (!s.render_rgb[c] && (s.render_depth[c] || s.render_seg[c])) geo += npix;
+    geo_base[c + 1] = (int32_t)geo;
+  }
+  for (int32_t c = s.nrender; c < MJPBR_MAX_RENDER; ++c) pix_base[c] = -1;
+  *pixels = rgb;
+}
+
+int64_t layout(PtWaveMap* wm, char* base, int64_t npath, int32_t nslot) {
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) {
+    char* p = base + off;
+    off += align256(bytes);
+    return p;
+  };
+  char* counters = take(256);
+  char* path = take(npath * (int64_t)sizeof(PathRec));
+  char* hit = take(npath * (int64_t)sizeof(HitRec));
+  char* nee = take(npath * (2 + 2 * (int64_t)nslot) * 16);
+  char* vis = take(npath * nslot);
+  char* q0 = take(npath * 4);
+  char* q1 = take(npath * 4);
+  char* shadow = take(npath * nslot * (int64_t)sizeof(ShadowEntry));
+  if (wm) {
+    wm->counters = reinterpret_cast<int32_t*>(counters);
+    wm->path = reinterpret_cast<PathRec*>(path);
+    wm->hit = reinterpret_cast<HitRec*>(hit);
+    wm->nee = reinterpret_cast<float4*>(nee);
+    wm->vis = reinterpret_cast<uint8_t*>(vis);
+    wm->queue[0] = reinterpret_cast<int32_t*>(q0);
+    wm->queue[1] = reinterpret_cast<int32_t*>(q1);
+    wm->shadow = reinterpret_cast<ShadowEntry*>(shadow);
+    wm->path_cap = npath;
+    wm->shadow_cap = npath * nslot;
+  }
+  return off;
+}
+
+template <class K>
+int resident_ctas(K kern, size_t smem) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kThreads, smem) != cudaSuccess || n < 1) n = 1;
+  return n;
+}
+
+template <class K>
+int set_smem(K kern, size_t smem, const char* what) {
+  if (smem <= 48 * 1024) return MJPBR_OK;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "%s: %zu bytes of shared memory: %s", what, smem, cudaGetErrorString(e));
+  return MJPBR_OK;
+}
+
+template <bool kMesh, bool kTex>
+int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t chunk, int64_t pixels) {
+  const size_t stack = (size_t)kThreads * kStackDepth * 8;
+  auto k_geometry = ptw_geometry_kernel<kMesh>;
+  auto k_extend = ptw_extend_kernel<kMesh>;
+  auto k_shade = ptw_shade_kernel<kMesh, kTex>;
+  auto k_shadow = ptw_shadow_kernel<kMesh>;
+  auto k_resolve = ptw_resolve_kernel<kTex>;
+  int rc = set_smem(k_geometry, stack, "path wavefront geometry");
+  if (!rc) rc = set_smem(k_extend, stack, "path wavefront extend");
+  if (!rc) rc = set_smem(k_shadow, stack, "path wavefront shadow");
+  if (rc) return rc;
+  const int sms = device_sm_count();
+  const int g_extend = sms * resident_ctas(k_extend, stack);
+  const int g_shade = sms * resident_ctas(k_shade, 0);
+  const int g_shadow = sms * resident_ctas(k_shadow, stack);
+  const int g_nee = sms * resident_ctas(ptw_nee_kernel, 0);
+  PtWaveMap wm;
+  wm.nsample = s.settings.path_samples;
+  wm.pixels = (int32_t)pixels;
+  wm.nslot = slots_of(s);
+  rgb_pixels(s, wm.pix_base, wm.geo_base, &pixels);
+  layout(&wm, static_cast<char*>(s.wave_scratch), (int64_t)chunk * pixels * wm.nsample, wm.nslot);
+  const int32_t geo_pixels = wm.geo_base[s.nrender];
+  const int32_t iterations = s.settings.max_depth + 1 + (s.settings.has_transparency ? 4 * s.settings.max_layers : 0);
+  const bool shadows = true;  // every bounce may ask for shadow rays (lights, environment)
+  for (int32_t w0 = 0; w0 < s.nworld; w0 += chunk) {
+    wm.w0 = w0;
+    wm.nw = std::min(chunk, s.nworld - w0);
+    wm.npath = (int32_t)((int64_t)wm.nw * pixels * wm.nsample);
+    if (geo_pixels > 0) {
+      const int64_t n = (int64_t)geo_pixels * wm.nw;
+      k_geometry<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, stack, stream>>>(s, wm);
+      if ((rc = check_launch("ptw_geometry_kernel"))) return rc;
+    }
+    if (wm.npath == 0) continue;
+    ptw_start_kernel<<<(unsigned)((wm.npath + kThreads - 1) / kThreads), kThreads, 0, stream>>>(s, seed, wm);
+    if ((rc = check_launch("ptw_start_kernel"))) return rc;
+    for (int32_t it = 0; it < iterations; ++it) {
+      const int32_t cur = it & 1, next = cur ^ 1;
+      k_extend<<<g_extend, kThreads, stack, stream>>>(s, wm, cur);
+      if ((rc = check_launch("ptw_extend_kernel"))) return rc;
+      cudaError_t e = cudaMemsetAsync(wm.counters + next, 0, sizeof(int32_t), stream);
+      if (e == cudaSuccess) e = cudaMemsetAsync(wm.counters + 2, 0, sizeof(int32_t), stream);
+      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path wavefront queue counters: %s", cudaGetErrorString(e));
+      k_shade<<<g_shade, kThreads, 0, stream>>>(s, seed, wm, cur);
+      if ((rc = check_launch("ptw_shade_kernel"))) return rc;
+      if (shadows) {
+        k_shadow<<<g_shadow, kThreads, stack, stream>>>(s, wm);
+        if ((rc = check_launch("ptw_shadow_kernel"))) return rc;
+      }
+      ptw_nee_kernel<<<g_nee, kThreads, 0, stream>>>(s, wm, cur);
+      if ((rc = check_launch("ptw_nee_kernel"))) return rc;
+    }
+    const int64_t npix = (int64_t)wm.nw * pixels;
+    k_resolve<<<(unsigned)((npix + kThreads - 1) / kThreads), kThreads, 0, stream>>>(s, wm);
+    if ((rc = check_launch("ptw_resolve_kernel"))) return rc;
+  }
+  return MJPBR_OK;
+}
+
+}  // namespace
+
+int64_t pt_wave_scratch_bytes(const MjpbrScene& s, int32_t worlds) {
+  int32_t pix_base[MJPBR_MAX_RENDER], geo_base[MJPBR_MAX_RENDER + 1];
+  int64_t pixels = 0;
+  rgb_pixels(s, pix_base, geo_base, &pixels);
+  if (worlds < 0 || s.settings.path_samples < 1) return -1;
+  return layout(nullptr, nullptr, (int64_t)worlds * pixels * s.settings.path_samples, slots_of(s));
+}
+
+int render_pt_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
+  if (s.nbvh_geom > 0xffff || s.nmesh + s.nhfield >= 0x7fff) {
+    return set_error(MJPBR_ERR_UNSUPPORTED, "the path wavefront packs slots and triangle BVHs in 16 bits");
+  }
+  if (!s.wave_scratch || (reinterpret_cast<uintptr_t>(s.wave_scratch) & 255u)) {
+    return set_error(MJPBR_ERR_ARG, "the path wavefront needs wave_scratch (256-byte aligned)");
+  }
+  int32_t pix_base[MJPBR_MAX_RENDER], geo_base[MJPBR_MAX_RENDER + 1];
+  int64_t pixels = 0;
+  rgb_pixels(s, pix_base, geo_base, &pixels);
+  // worlds per chunk: as many as the scratch holds, with path and shadow-target indices in int32
+  int32_t chunk = s.nworld;
+  if (pixels > 0) {
+    const int64_t per_world = pixels * s.settings.path_samples * slots_of(s);
+    chunk = (int32_t)std::min<int64_t>(chunk, INT32_MAX / std::max<int64_t>(per_world, 1));
+    if (pt_wave_scratch_bytes(s, chunk) > s.wave_scratch_bytes) {
+      int32_t lo = 0, hi = chunk;
+      while (lo < hi) {
+        const int32_t mid = lo + (hi - lo + 1) / 2;
+        if (pt_wave_scratch_bytes(s, mid) <= s.wave_scratch_bytes) {
+          lo = mid;
+        } else {
+          hi = mid - 1;
+        }
+      }
+      chunk = lo;
+    }
+    if (chunk < 1) {
+      return set_error(MJPBR_ERR_ARG, "wave_scratch of %lld bytes holds no world (one needs %lld)", (long long)s.wave_scratch_bytes,
+                       (long long)pt_wave_scratch_bytes(s, 1));
+    }
+  }
+  const bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
+  const bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
+  if (mesh && tex) return launch_pt_wave<true, true>(s, seed, stream, chunk, pixels);
+  if (mesh) return launch_pt_wave<true, false>(s, seed, stream, chunk, pixels);
+  if (tex) return launch_pt_wave<false, true>(s, seed, stream, chunk, pixels);
+  return launch_pt_wave<false, false>(s, seed, stream, chunk, pixels);
+}
+
+}  // namespace mjpbr
+
+#ifdef MJPBR_COUNT_OPS
+namespace mjpbr {
+// Counting build: this unit's copy of the counter array pointer (see opcount.cuh).
+int pt_wave_count_set(void* counts) { return cudaMemcpyToSymbol(g_op_counts, &counts, sizeof(counts)) == cudaSuccess ? 0 : 1; }
+}  // namespace mjpbr
+#endif

@@ -523,12 +523,13 @@ int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
 namespace mjpbr {
 int pt_count_set(void* counts);
 int wave_count_set(void* counts);
+int pt_wave_count_set(void* counts);
 }
 
 // Counting build only: the device array (kOpCountN x kOpCopies uint64) the real-time and path
 // kernels add to, or NULL.
 extern "C" int mjpbr_count_set(void* counts) {
   if (cudaMemcpyToSymbol(mjpbr::g_op_counts, &counts, sizeof(counts)) != cudaSuccess) return 1;
-  return mjpbr::pt_count_set(counts) | mjpbr::wave_count_set(counts);
+  return mjpbr::pt_count_set(counts) | mjpbr::wave_count_set(counts) | mjpbr::pt_wave_count_set(counts);
 }
 #endif

@@ -753,6 +753,7 @@ int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t
 }  // namespace
 
 int64_t wave_scratch_bytes(const MjpbrScene& s, int32_t worlds) {
+  if (s.settings.tier == MJPBR_TIER_PATH) return pt_wave_scratch_bytes(s, worlds);
   const int32_t per_world = samples_per_world(s);
   if (per_world < 0 || worlds < 0) return -1;
   return layout(nullptr, nullptr, worlds, per_world, s.nlight);

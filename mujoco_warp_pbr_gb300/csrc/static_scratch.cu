@@ -105,6 +105,11 @@ extern "C" int mjpbr_refit_render_static(const MjpbrScene* scene, uint32_t seed,
                      (long long)kStaticBlockFloats, (long long)need, scene->nworld, scene->world_block_floats);
   }
   MjpbrScene s = *scene;
+  // the wavefront schedules keep their queues in caller scratch: render with the grid schedule /
+  // the persistent path kernel instead (the same images)
+  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT) s.settings.schedule = MJPBR_SCHEDULE_GRID;
+  s.wave_scratch = nullptr;
+  s.wave_scratch_bytes = 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int rc = static_scratch(st, &s.world_blocks, &s.work_counter);
   if (rc) return rc;
@@ -114,7 +119,5 @@ extern "C" int mjpbr_refit_render_static(const MjpbrScene* scene, uint32_t seed,
   if (rc) return rc;
   // render_pt_launch zeroes the work counter on the stream before its kernel starts
   if (s.settings.tier == MJPBR_TIER_PATH) return render_pt_launch(s, seed, st);
-  // the wavefront schedule keeps its ray queues in caller scratch: render with the grid instead
-  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT) s.settings.schedule = MJPBR_SCHEDULE_GRID;
   return render_rt_launch(s, seed, st);
 }

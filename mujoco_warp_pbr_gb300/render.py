@@ -273,20 +273,26 @@ def scene(m: Any, d: Any, rc: PbrRenderContext) -> _lib.Scene:
   return struct
 
 
-# samples per chunk of the wavefront schedule when wave_chunk_worlds is 0
+# camera samples (real-time tier) or paths (path tier) per chunk of the wavefront schedules when
+# wave_chunk_worlds is 0
 WAVE_CHUNK_SAMPLES = 1 << 24
+WAVE_CHUNK_PATHS = 1 << 23
 
 
 def _ensure_wave_scratch(rc: PbrRenderContext, struct: _lib.Scene) -> bool:
-  """Allocates (or grows) the wavefront schedule's scratch for a real-time context using it:
-  wave_chunk_worlds worlds per chunk, or about WAVE_CHUNK_SAMPLES camera samples. Returns True
-  when rc.wave_scratch changed."""
-  if rc.tier != 0 or rc.schedule != 2 or rc.has_transparency:
+  """Allocates (or grows) the wavefront schedule's scratch for a context using it: wave_chunk_worlds
+  worlds per chunk, or about WAVE_CHUNK_SAMPLES camera samples (real-time tier) / WAVE_CHUNK_PATHS
+  paths (path tier). Returns True when rc.wave_scratch changed."""
+  if rc.schedule != 2 or (rc.tier == 0 and rc.has_transparency):
     return False
   lib = _lib.load()
   per_world = lib.mjpbr_wave_scratch_bytes(struct, 1) - lib.mjpbr_wave_scratch_bytes(struct, 0)
-  samples = max(1, sum(w * h for (w, h), on in zip(rc.base.cam_res, rc.base.render_rgb) if on) * int(rc.samples_per_pixel) ** 2)
-  chunk = rc.wave_chunk_worlds or max(1, WAVE_CHUNK_SAMPLES // samples)
+  pixels = sum(w * h for (w, h), on in zip(rc.base.cam_res, rc.base.render_rgb) if on)
+  if rc.tier == 0:
+    chunk_units, units = WAVE_CHUNK_SAMPLES, pixels * int(rc.samples_per_pixel) ** 2
+  else:
+    chunk_units, units = WAVE_CHUNK_PATHS, pixels * int(rc.path_samples)
+  chunk = rc.wave_chunk_worlds or max(1, chunk_units // max(units, 1))
   chunk = min(chunk, int(rc.base.rgb_data.shape[0]))
   need = int(lib.mjpbr_wave_scratch_bytes(struct, chunk))
   if need < 0 or per_world < 0:

@@ -134,10 +134,13 @@ def test_wait_probe_rejects_bad_arguments_without_a_gpu():
 @pytest.mark.gpu
 @pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
 def test_autotuner_skips_shapes_that_fail_or_run_too_long(monkeypatch):
+  import importlib
+
   import mujoco_warp_pbr_gb300 as mjpbr
-  from mujoco_warp_pbr_gb300 import autotune, synthetic
+  from mujoco_warp_pbr_gb300 import synthetic
   from tests import helpers
 
+  autotune = importlib.import_module("mujoco_warp_pbr_gb300.autotune")  # the module (the package exports the function)
   sc = synthetic.primitive_scene(seed=2, nworld=4, res=24)
   m, d, rc = helpers.gpu_scene(sc)
   for shape in autotune.CANDIDATES:  # load every kernel once, outside the timed warm-up frames

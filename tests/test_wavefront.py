@@ -196,3 +196,106 @@ def test_wavefront_tile_mapping_covers_each_sample_once():
       xs = {z_x(q) for q in range(start, start + size)}
       ys = {z_y(q) for q in range(start, start + size)}
       assert len(xs) == bw and len(ys) == bh and max(xs) - min(xs) == bw - 1 and max(ys) - min(ys) == bh - 1
+
+
+def _pt_outputs(rc):
+  out = {
+    "rgb": rc.base.rgb_data.cpu().numpy().view(np.uint32).copy(),
+    "depth": rc.base.depth_data.cpu().numpy().copy(),
+    "seg": rc.base.seg_data.cpu().numpy().copy(),
+    "hdr": rc.hdr_data.cpu().numpy().copy(),
+  }
+  if rc.render_guides:
+    out["albedo"] = rc.guide_albedo.cpu().numpy().copy()
+    out["normal"] = rc.guide_normal.cpu().numpy().copy()
+  if rc.denoise:
+    out["guide"] = rc.aov_guide.cpu().numpy().copy()
+    out["emission"] = rc.aov_emission.cpu().numpy().copy()
+    out["demod"] = rc.denoise_buffers[0].cpu().numpy().copy()
+  return out
+
+
+def _pt_frame(m, d, rc, seed):
+  import mujoco_warp_pbr_gb300 as mjpbr
+
+  for t in (rc.base.rgb_data, rc.base.depth_data, rc.base.seg_data, rc.hdr_data, rc.guide_albedo, rc.guide_normal, rc.aov_guide,
+            rc.aov_emission, rc.denoise_buffers[0]):
+    t.zero_()
+  mjpbr.refit_bvh(m, d, rc)
+  mjpbr.render(m, d, rc, seed=seed, denoise=False)
+  torch.cuda.synchronize()
+  assert mjpbr.check_errors(rc) == 0
+  return _pt_outputs(rc)
+
+
+def _pt_scene(name):
+  from mujoco_warp_pbr_gb300 import synthetic
+
+  pt = {"tier": 1, "render_hdr": True}
+  if name == "path":
+    return synthetic.path_scene(seed=3, nworld=5, res=24, spp=3), {**pt, "path_samples": 3, "render_guides": True}
+  if name == "path_denoise":
+    return synthetic.path_scene(seed=4, nworld=3, res=32, spp=2), {**pt, "path_samples": 2, "denoise": True}
+  if name == "mesh_ibl":
+    return synthetic.mesh_ibl_scene(seed=1, nworld=3, res=24, tex_size=64, env_width=128), {**pt, "path_samples": 4, "max_depth": 3, "rr_depth": 2}
+  if name == "primitives_mirror":
+    return synthetic.primitive_scene(seed=2, nworld=3, res=24), {**pt, "path_samples": 2, "max_depth": 4, "rr_depth": 1}
+  if name == "large_path_envs":
+    return synthetic.large_path_scene(seed=1, nworld=4, res=16, env_width=128), {**pt, "path_samples": 2}
+  if name == "hfield":
+    return synthetic.hfield_scene(seed=2, nworld=2, res=20), {**pt, "path_samples": 2}
+  raise KeyError(name)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("name", ["path", "path_denoise", "mesh_ibl", "primitives_mirror", "large_path_envs", "hfield"])
+def test_path_wavefront_renders_the_persistent_kernel_images(name):
+  """The staged path tracer (extend / shade / shadow / next-event kernels over path queues) and the
+  persistent path kernel give bit-identical images, HDR, guides and denoiser inputs, for one chunk
+  of worlds and for chunks of one and two worlds."""
+  from tests import helpers
+
+  sc, opts = _pt_scene(name)
+  m, d, rc = helpers.gpu_scene(sc, **opts)
+  rc.schedule = 0
+  ref = _pt_frame(m, d, rc, seed=5)
+  rc.schedule = 2
+  for chunk in (0, 1, 2):
+    rc.wave_chunk_worlds = chunk
+    rc.wave_scratch = None
+    got = _pt_frame(m, d, rc, seed=5)
+    for key in ref:
+      np.testing.assert_array_equal(got[key], ref[key], err_msg=f"{name}: {key} differs (chunk {chunk})")
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+def test_path_wavefront_translucent_layers_and_depth_only_camera():
+  """Stochastic alpha pass-through (extra bounce iterations) and a second camera without RGB."""
+  from mujoco_warp_pbr_gb300 import synthetic
+  from mujoco_warp_pbr_gb300.synthetic import GEOM_BOX, GEOM_PLANE, GEOM_SPHERE, LIGHT_POINT, Builder
+  from tests import helpers
+
+  b = Builder()
+  b.geom(GEOM_PLANE, (2, 2, 0.1), rgba=(0.7, 0.7, 0.7, 1))
+  b.geom(GEOM_SPHERE, (0.3, 0, 0), pos=(0, 0, 0.3), rgba=(0.8, 0.2, 0.2, 0.5))
+  b.geom(GEOM_BOX, (0.2, 0.2, 0.2), pos=(0.5, 0.3, 0.2), rgba=(0.2, 0.8, 0.2, 1))
+  b.light(LIGHT_POINT, pos=(0.5, -0.5, 2.0), diffuse=(0.6, 0.6, 0.6), range=10.0, bulbradius=0.05, castshadow=True)
+  b.camera(pos=(0.0, -2.5, 1.5), target=(0, 0, 0.3), resolution=(23, 17))
+  b.camera(pos=(0.3, -2.0, 1.5), target=(0, 0, 0.3), resolution=(19, 13))
+  mjm, mjd = b.build()
+  sc = synthetic.SyntheticScene(
+    name="translucent", mjm=mjm, mjd=mjd, nworld=3,
+    options={"render_depth": True, "render_seg": True, "render_rgb": [True, False], "tier": 1, "path_samples": 3, "max_layers": 2,
+             "render_hdr": True},
+    per_world={}, seed=0,
+  )
+  m, d, rc = helpers.gpu_scene(sc)
+  assert rc.has_transparency
+  rc.schedule = 0
+  ref = _pt_frame(m, d, rc, seed=8)
+  rc.schedule = 2
+  got = _pt_frame(m, d, rc, seed=8)
+  for key in ref:
+    np.testing.assert_array_equal(got[key], ref[key], err_msg=key)
