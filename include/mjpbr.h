@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define MJPBR_ABI_VERSION 2
+#define MJPBR_ABI_VERSION 3
 
 /* Most rendering cameras of one context (the per-camera tables below are inline). */
 #define MJPBR_MAX_RENDER 16
@@ -176,6 +176,8 @@ typedef struct MjpbrSettings {
   int32_t denoise;           /* path tier: write denoiser features instead of RGB */
   int32_t schedule;          /* real-time tier: MjpbrSchedule */
   int32_t queue_item;        /* queue schedule: pixels per work item (32, 64 or 128) */
+  int32_t stack_depth;       /* traversal stack entries per ray: 0 (32) or 8..32; the scene BVH's
+                                inner levels + the deepest mesh BVH's + 1 always suffice */
   float znear;
   float zfar;                /* <= 0: unbounded */
   float shadow_light_fraction;

@@ -12,7 +12,7 @@ import threading
 from pathlib import Path
 
 LIBRARY = Path(__file__).resolve().parent / "libmjpbr.so"
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_RENDER = 16
 NTEXROLE = 10
 MAX_MIPS = 15
@@ -89,6 +89,7 @@ class Settings(ctypes.Structure):
       "denoise",
       "schedule",
       "queue_item",
+      "stack_depth",
     )
   ] + [
     ("znear", c_f32),

@@ -356,6 +356,51 @@ def build_scene_topology(lo: np.ndarray, hi: np.ndarray) -> np.ndarray:
   return out
 
 
+def scene_tree_levels(topo: np.ndarray) -> int:
+  """Inner-node levels of the deepest scene tree: topo (nworld or 1, nnode, 2) child refs (>= 0 an
+  inner node, < 0 a leaf or empty), nodes in pre-order (every child after its parent)."""
+  topo = np.asarray(topo).reshape(-1, topo.shape[-2], 2)
+  depth = np.zeros(topo.shape[:2], np.int32)
+  rows = np.arange(topo.shape[0])
+  for i in range(topo.shape[1]):
+    for k in (0, 1):
+      c = topo[:, i, k]
+      inner = c >= 0
+      depth[rows[inner], c[inner]] = depth[inner, i] + 1
+  return int(depth.max()) + 1
+
+
+def mesh_tree_levels(nodes: np.ndarray) -> int:
+  """Inner-node levels of one mesh BVH: nodes (nnode, 16) float32 in the child-bounds layout of
+  libmjpbr's mesh builder (child k: ref bits at 8k + 3, count bits at 8k + 7; count 0 an inner node,
+  root 0)."""
+  bits = np.ascontiguousarray(nodes, np.float32).view(np.int32)
+  levels, frontier = 0, np.array([0])
+  while frontier.size:
+    levels += 1
+    kids = []
+    for k in (0, 1):
+      ref, cnt = bits[frontier, 8 * k + 3], bits[frontier, 8 * k + 7]
+      kids.append(ref[cnt == 0])
+    frontier = np.concatenate(kids)
+  return levels
+
+
+def traversal_stack_depth(scene_levels: int, mesh_levels: int) -> int:
+  """Stack entries a nearest-first traversal can hold: a node popped at stack position p sits at
+  depth >= p, so at a scene leaf at most scene_levels entries wait below the mesh traversal, which
+  adds at most mesh_levels + 1 (the far children of its path plus both children of its deepest
+  inner node). Clamped to the 8..32 entries the kernels support."""
+  need = scene_levels + mesh_levels + 1
+  if need > 32:
+    warnings.warn(
+      f"BVHs of {scene_levels} scene and {mesh_levels} mesh levels can need {need} traversal stack entries, more than 32; "
+      "a ray that overflows is reported in the error word",
+      stacklevel=3,
+    )
+  return min(max(need, 8), 32)
+
+
 def nhfield_of(mjm: Any) -> int:
   """Height fields of a model (0 for models without the hfield_* fields)."""
   nrow = getattr(mjm, "hfield_nrow", None)
@@ -426,7 +471,7 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
   """Triangle BVHs concatenated, one per mesh, then one per height field (hfield_mesh): nodes
   (nnode, 16), tris (ntri, 12), root / tri_base per BVH, local AABBs (nmesh + nhfield, 6)."""
   lib = _lib.load()
-  nodes, tris, roots, bases, bounds, nfaces = [], [], [], [], [], []
+  nodes, tris, roots, bases, bounds, nfaces, levels = [], [], [], [], [], [], []
   node_total = tri_total = 0
   vert_all = np.asarray(mjm.mesh_vert, np.float32).reshape(-1, 3)
   face_all = np.asarray(mjm.mesh_face, np.int32).reshape(-1, 3)
@@ -452,6 +497,7 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
     if status != 0:
       raise ValueError(f"{name}: BVH build failed (status {status})")
     nodes.append(node_buf[: nnode.value])
+    levels.append(mesh_tree_levels(node_buf[: nnode.value]))
     tris.append(tri_buf)
     roots.append(node_total)
     bases.append(tri_total)
@@ -467,6 +513,7 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
     "mesh_bounds": np.stack(bounds).astype(np.float32) if bounds else None,
     "mesh_nface": nfaces[: mjm.nmesh],
     "nhfield": nhfield_of(mjm),
+    "mesh_levels": max(levels) if levels else 0,
   }
 
 
@@ -842,6 +889,7 @@ def prepare_context(
     "max_depth": int(max_depth),
     "rr_depth": int(rr_depth),
     "denoise": int(bool(denoise)),
+    "stack_depth": traversal_stack_depth(scene_tree_levels(topo), int(meshes.get("mesh_levels", 0))),
     "znear": float(getattr(mjm, "znear", 0.01)),
     "zfar": float(getattr(mjm, "zfar", 0.0)),
     "shadow_light_fraction": float(shadow_light_fraction),

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "abi_internal.h"
+#include "common.cuh"
 #include "world_block.cuh"
 
 namespace mjpbr {
@@ -148,6 +149,9 @@ int validate_scene(const MjpbrScene* s, bool need_outputs) {
       return set_error(MJPBR_ERR_ARG, "work queue: items of %d pixels; 32, 64 or 128", st.queue_item);
     }
     if (s->wave_scratch_bytes < 0) return set_error(MJPBR_ERR_ARG, "wave_scratch_bytes is negative");
+    if (st.stack_depth != 0 && (st.stack_depth < 8 || st.stack_depth > kStackDepth)) {
+      return set_error(MJPBR_ERR_ARG, "settings.stack_depth %d: 0 or 8..%d entries", st.stack_depth, kStackDepth);
+    }
   }
   return MJPBR_OK;
 }

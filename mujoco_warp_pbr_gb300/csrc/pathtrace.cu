@@ -86,12 +86,7 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
   const int lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
   RtCtx c;
-  {
-    int32_t* stack_base = reinterpret_cast<int32_t*>(smem + s.world_block_floats);
-    c.st.code = stack_base + threadIdx.x;
-    c.st.t = reinterpret_cast<float*>(stack_base + kThreads * kStackDepth) + threadIdx.x;
-    c.st.stride = kThreads;
-  }
+  c.st = shared_stack(smem + s.world_block_floats, kThreads, stack_entries(st.stack_depth));
   int32_t err = 0;
   for (;;) {
     if (threadIdx.x == 0) s_tile = atomicAdd(s.work_counter, 1);
@@ -179,7 +174,7 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
 
 template <bool kMesh, bool kTex>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const PtTiles& tm, cudaStream_t stream) {
-  size_t smem = (size_t)s.world_block_floats * sizeof(float) + (size_t)kThreads * kStackDepth * 8;
+  size_t smem = (size_t)s.world_block_floats * sizeof(float) + (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
   auto kern = pt_kernel<kMesh, kTex>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path tracer: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));

@@ -11,8 +11,9 @@
 //              the environment sample's term and ray), the BSDF sample and Russian roulette;
 //              shadow rays and the paths that continue are appended to queues (one atomic per CTA)
 //     shadow   any hit of every recorded shadow ray
-//     nee      the recorded contributions of the unoccluded rays added to the path's radiance in
-//              light order (the persistent kernel's exact additions)
+//   (the recorded terms of the unoccluded rays are added to the path's radiance, in light order,
+//   by the next bounce's extend stage, or by the resolve stage for a path that ended: the
+//   persistent kernel's exact additions in its order)
 //   resolve  one thread per pixel: its samples summed in sample order, tone map / denoiser inputs
 //
 // Each stage runs one kind of work on a full set of lanes and has its own register budget; the
@@ -32,6 +33,10 @@ namespace mjpbr {
 namespace {
 
 constexpr int kThreads = 256;
+// Resident CTAs per SM the shade stage's register allocation targets.
+#ifndef MJPBR_PTW_SHADE_CTAS
+#define MJPBR_PTW_SHADE_CTAS 3
+#endif
 
 struct __align__(16) PathRec {
   float4 o;       // origin, max_dist
@@ -83,13 +88,8 @@ struct PtWaveMap {
   int64_t path_cap, shadow_cap;
 };
 
-MJ_DEV Stack wave_stack(float* base) {
-  Stack st;
-  int32_t* b = reinterpret_cast<int32_t*>(base);
-  st.code = b + threadIdx.x;
-  st.t = reinterpret_cast<float*>(b + kThreads * kStackDepth) + threadIdx.x;
-  st.stride = kThreads;
-  return st;
+MJ_DEV Stack wave_stack(const MjpbrScene& s, float* base) {
+  return shared_stack(base, kThreads, stack_entries(s.settings.stack_depth));
 }
 
 // World, camera, pixel id and sample of a chunk-local path index (paths: world-major, then RGB
@@ -243,6 +243,34 @@ struct RecordedNee {
   }
 };
 
+// ---------------------------------------------------------------- next-event terms
+// Adds a path's recorded next-event terms of its last shaded bounce to its radiance (the light
+// terms in light order, times the bounce's throughput, then the environment term), each one only
+// if its shadow ray was unoccluded, and marks the record applied. Run by the next bounce's extend
+// stage before the path's next hit, and by the resolve stage for the paths that ended: the same
+// additions in the same order as the persistent kernel.
+MJ_DEV void apply_nee(const PtWaveMap& wm, int32_t path, PathRec& r) {
+  float4* rec = wm.nee + (int64_t)path * (2 + 2 * wm.nslot);
+  const float4 head = rec[0];
+  if (__float_as_int(head.w) == 0) return;
+  const int32_t nlights = wm.nslot - 1;  // the model's lights and the headlight
+  const uint8_t* vis = wm.vis + (int64_t)path * wm.nslot;
+  V3 direct = v3(0.0f);
+  for (int32_t k = 0; k < nlights; ++k) {
+    const float4 c = rec[2 + 2 * k];
+    const int32_t flag = __float_as_int(c.w);
+    if (flag == kNeeSkip) continue;
+    const bool add = flag == kNeeAdd || (flag == kNeeIfVisible && vis[k]);
+    direct += add ? V3{c.x, c.y, c.z} : v3(0.0f);
+  }
+  V3 radiance{r.rad.x, r.rad.y, r.rad.z};
+  radiance += cmul(V3{head.x, head.y, head.z}, direct);
+  const float4 e = rec[2 + 2 * nlights];
+  if (__float_as_int(e.w) == kNeeIfVisible && vis[nlights]) radiance += V3{e.x, e.y, e.z};
+  r.rad = make_float4(radiance.x, radiance.y, radiance.z, r.rad.w);
+  rec[0].w = __int_as_float(0);
+}
+
 // ---------------------------------------------------------------- start
 __global__ void __launch_bounds__(kThreads) ptw_start_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                              const __grid_constant__ PtWaveMap wm) {
@@ -270,7 +298,7 @@ template <bool kMesh>
 __global__ void __launch_bounds__(kThreads) ptw_geometry_kernel(const __grid_constant__ MjpbrScene s,
                                                                 const __grid_constant__ PtWaveMap wm) {
   extern __shared__ __align__(16) float smem[];
-  const Stack st = wave_stack(smem);
+  const Stack st = wave_stack(s, smem);
   const int32_t per_world = wm.geo_base[s.nrender];
   const int32_t i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= per_world * wm.nw) return;
@@ -303,9 +331,9 @@ __global__ void __launch_bounds__(kThreads) ptw_geometry_kernel(const __grid_con
 // ---------------------------------------------------------------- extend
 template <bool kMesh>
 __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_constant__ MjpbrScene s,
-                                                                 const __grid_constant__ PtWaveMap wm, int32_t cur) {
+                                                                 const __grid_constant__ PtWaveMap wm, int32_t cur, bool pending_nee) {
   extern __shared__ __align__(16) float smem[];
-  const Stack st = wave_stack(smem);
+  const Stack st = wave_stack(s, smem);
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const bool cull = s.settings.cull_backfaces != 0;
   const int32_t count = (int32_t)min((int64_t)wm.counters[cur], wm.path_cap);
@@ -313,6 +341,7 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_co
   for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
     const int32_t path = wm.queue[cur][i];
     PathRec& r = wm.path[path];
+    if (pending_nee) apply_nee(wm, path, r);
     const float4 o = r.o, d = r.d;
     const int32_t sample = __float_as_int(r.emis.w);
     const int32_t passes = __float_as_int(r.normal.w);
@@ -336,7 +365,7 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_co
 
 // ---------------------------------------------------------------- shade
 template <bool kMesh, bool kTex>
-__global__ void __launch_bounds__(kThreads, 2) ptw_shade_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+__global__ void __launch_bounds__(kThreads, MJPBR_PTW_SHADE_CTAS) ptw_shade_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                 const __grid_constant__ PtWaveMap wm, int32_t cur) {
   __shared__ int32_t scan[kThreads / 32 + 1];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
@@ -395,7 +424,7 @@ template <bool kMesh>
 __global__ void __launch_bounds__(kThreads, 3) ptw_shadow_kernel(const __grid_constant__ MjpbrScene s,
                                                                  const __grid_constant__ PtWaveMap wm) {
   extern __shared__ __align__(16) float smem[];
-  const Stack st = wave_stack(smem);
+  const Stack st = wave_stack(s, smem);
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const bool cull = s.settings.cull_backfaces != 0;
   const int32_t count = (int32_t)min((int64_t)wm.counters[2], wm.shadow_cap);
@@ -410,34 +439,6 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_shadow_kernel(const __grid_co
     wm.vis[target] = hit.geom == -1 ? 1 : 0;
   }
   if (err && s.error_word) atomicOr(s.error_word, err);
-}
-
-// ---------------------------------------------------------------- next-event terms
-__global__ void __launch_bounds__(kThreads) ptw_nee_kernel(const __grid_constant__ MjpbrScene s, const __grid_constant__ PtWaveMap wm,
-                                                           int32_t cur) {
-  const int32_t count = (int32_t)min((int64_t)wm.counters[cur], wm.path_cap);
-  const int32_t nlights = wm.nslot - 1;  // the model's lights and the headlight
-  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
-    const int32_t path = wm.queue[cur][i];
-    const float4* rec = wm.nee + (int64_t)path * (2 + 2 * wm.nslot);
-    const float4 head = rec[0];
-    if (__float_as_int(head.w) == 0) continue;
-    const uint8_t* vis = wm.vis + (int64_t)path * wm.nslot;
-    V3 direct = v3(0.0f);
-    for (int32_t k = 0; k < nlights; ++k) {
-      const float4 c = rec[2 + 2 * k];
-      const int32_t flag = __float_as_int(c.w);
-      if (flag == kNeeSkip) continue;
-      const bool add = flag == kNeeAdd || (flag == kNeeIfVisible && vis[k]);
-      direct += add ? V3{c.x, c.y, c.z} : v3(0.0f);
-    }
-    PathRec& r = wm.path[path];
-    V3 radiance{r.rad.x, r.rad.y, r.rad.z};
-    radiance += cmul(V3{head.x, head.y, head.z}, direct);
-    const float4 e = rec[2 + 2 * nlights];
-    if (__float_as_int(e.w) == kNeeIfVisible && vis[nlights]) radiance += V3{e.x, e.y, e.z};
-    r.rad = make_float4(radiance.x, radiance.y, radiance.z, r.rad.w);
-  }
 }
 
 // ---------------------------------------------------------------- pixels
@@ -455,7 +456,9 @@ __global__ void __launch_bounds__(kThreads) ptw_resolve_kernel(const __grid_cons
   clear_pixel(acc);
   for (int32_t k = 0; k < wm.nsample; ++k) {
     float first_depth;
-    const PathState ps = load_path(wm.path[(int64_t)pix_all * wm.nsample + k], &first_depth);
+    const int32_t path = pix_all * wm.nsample + k;
+    apply_nee(wm, path, wm.path[path]);
+    const PathState ps = load_path(wm.path[path], &first_depth);
     if (k == 0) acc.first_depth = first_depth;
     add_sample(acc, ps, s.settings.denoise != 0, c.exposure);
   }
@@ -529,7 +532,7 @@ int set_smem(K kern, size_t smem, const char* what) {
 
 template <bool kMesh, bool kTex>
 int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t chunk, int64_t pixels) {
-  const size_t stack = (size_t)kThreads * kStackDepth * 8;
+  const size_t stack = (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
   auto k_geometry = ptw_geometry_kernel<kMesh>;
   auto k_extend = ptw_extend_kernel<kMesh>;
   auto k_shade = ptw_shade_kernel<kMesh, kTex>;
@@ -543,7 +546,6 @@ int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int3
   const int g_extend = sms * resident_ctas(k_extend, stack);
   const int g_shade = sms * resident_ctas(k_shade, 0);
   const int g_shadow = sms * resident_ctas(k_shadow, stack);
-  const int g_nee = sms * resident_ctas(ptw_nee_kernel, 0);
   PtWaveMap wm;
   wm.nsample = s.settings.path_samples;
   wm.pixels = (int32_t)pixels;
@@ -567,7 +569,7 @@ int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int3
     if ((rc = check_launch("ptw_start_kernel"))) return rc;
     for (int32_t it = 0; it < iterations; ++it) {
       const int32_t cur = it & 1, next = cur ^ 1;
-      k_extend<<<g_extend, kThreads, stack, stream>>>(s, wm, cur);
+      k_extend<<<g_extend, kThreads, stack, stream>>>(s, wm, cur, it > 0);
       if ((rc = check_launch("ptw_extend_kernel"))) return rc;
       cudaError_t e = cudaMemsetAsync(wm.counters + next, 0, sizeof(int32_t), stream);
       if (e == cudaSuccess) e = cudaMemsetAsync(wm.counters + 2, 0, sizeof(int32_t), stream);
@@ -578,8 +580,6 @@ int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int3
         k_shadow<<<g_shadow, kThreads, stack, stream>>>(s, wm);
         if ((rc = check_launch("ptw_shadow_kernel"))) return rc;
       }
-      ptw_nee_kernel<<<g_nee, kThreads, 0, stream>>>(s, wm, cur);
-      if ((rc = check_launch("ptw_nee_kernel"))) return rc;
     }
     const int64_t npix = (int64_t)wm.nw * pixels;
     k_resolve<<<(unsigned)((npix + kThreads - 1) / kThreads), kThreads, 0, stream>>>(s, wm);

@@ -290,13 +290,8 @@ MJ_DEV void render_pixel_lanes(const MjpbrScene& s, uint32_t seed, const float* 
   if (c.err && s.error_word) atomicOr(s.error_word, c.err);
 }
 
-MJ_DEV Stack thread_stack(float* stacks) {
-  Stack st;
-  int32_t* base = reinterpret_cast<int32_t*>(stacks);
-  st.code = base + threadIdx.x;
-  st.t = reinterpret_cast<float*>(base + kThreads * kStackDepth) + threadIdx.x;
-  st.stride = kThreads;
-  return st;
+MJ_DEV Stack thread_stack(const MjpbrScene& s, float* stacks) {
+  return shared_stack(stacks, kThreads, stack_entries(s.settings.stack_depth));
 }
 
 // Grid schedule: one CTA per (camera tile, world); the hardware scheduler balances the CTAs.
@@ -322,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   if (s.settings.samples_per_axis == 2 && s.render_rgb[cam] != 0) {
     // sample lanes: 4 passes of 64 pixels, each warp a 4 x 2 pixel block (ROW tiles of 32 x 8 in
     // passes of 2 rows, TILED tiles of 16 x 16 in 8 x 8 quadrants)
-    const Stack st = thread_stack(smem + s.world_block_floats);
+    const Stack st = thread_stack(s, smem + s.world_block_floats);
     const bool row = s.settings.render_order == MJPBR_ORDER_ROW;
     const int32_t smp = lane & 3, pix = lane >> 2;
 #pragma unroll 1
@@ -348,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
     p.py = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
   }
   if (p.px >= p.width || p.py >= p.height) return;
-  render_pixel<kMesh, kTex>(s, seed, blk, L, w, p, thread_stack(smem + s.world_block_floats));
+  render_pixel<kMesh, kTex>(s, seed, blk, L, w, p, thread_stack(s, smem + s.world_block_floats));
 }
 
 // Work items of the queue schedule: runs of `per_item` warp tiles (8 x 4 pixels) of one camera
@@ -374,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_queue_kernel
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
   float* blk = smem + warp * s.world_block_floats;
-  const Stack stack = thread_stack(smem + (kThreads / 32) * s.world_block_floats);
+  const Stack stack = thread_stack(s, smem + (kThreads / 32) * s.world_block_floats);
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   int32_t staged = -1;
   for (;;) {
@@ -414,12 +409,12 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_queue_kernel
 constexpr size_t kSmemPerSm = 228 * 1024;
 constexpr size_t kQueueSmemLimit = kSmemPerSm / MJPBR_RT_MIN_BLOCKS - 2048;
 
-size_t stack_bytes() { return (size_t)kThreads * kStackDepth * 8; }
+size_t stack_bytes(const MjpbrScene& s) { return (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8; }
 
 template <bool kMesh, bool kTex>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaStream_t stream) {
   static size_t smem_set = 0;
-  const size_t smem = (size_t)s.world_block_floats * sizeof(float) + stack_bytes();
+  const size_t smem = (size_t)s.world_block_floats * sizeof(float) + stack_bytes(s);
   auto kern = rt_kernel<kMesh, kTex>;
   if (smem > smem_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -434,7 +429,7 @@ int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaSt
 template <bool kMesh, bool kTex>
 int launch_queue_variant(const MjpbrScene& s, uint32_t seed, const QueueMap& qm, cudaStream_t stream) {
   static size_t smem_set = 0;
-  const size_t smem = (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes();
+  const size_t smem = (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes(s);
   auto kern = rt_queue_kernel<kMesh, kTex>;
   if (smem > smem_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -477,7 +472,7 @@ int render_rt_queue(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
 
 // True when the queue schedule's per-warp world blocks fit the shared memory of the resident CTAs.
 bool rt_queue_fits(const MjpbrScene& s) {
-  return (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes() <= kQueueSmemLimit;
+  return (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes(s) <= kQueueSmemLimit;
 }
 
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {

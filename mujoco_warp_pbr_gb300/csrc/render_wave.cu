@@ -98,13 +98,8 @@ struct WaveMap {
 MJ_DEV int32_t z_x(int32_t q) { return (q & 1) | ((q >> 1) & 2) | ((q >> 2) & 4) | ((q >> 3) & 8); }
 MJ_DEV int32_t z_y(int32_t q) { return ((q >> 1) & 1) | ((q >> 2) & 2) | ((q >> 3) & 4) | ((q >> 4) & 8); }
 
-MJ_DEV Stack wave_stack(float* base) {
-  Stack st;
-  int32_t* b = reinterpret_cast<int32_t*>(base);
-  st.code = b + threadIdx.x;
-  st.t = reinterpret_cast<float*>(b + kThreads * kStackDepth) + threadIdx.x;
-  st.stride = kThreads;
-  return st;
+MJ_DEV Stack wave_stack(const MjpbrScene& s, float* base) {
+  return shared_stack(base, kThreads, stack_entries(s.settings.stack_depth));
 }
 
 // Camera and tile coordinates of CTA tile `tile` in a tile map.
@@ -260,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_primary_
   stage_world_block(s, w, blk, kThreads);
   __syncthreads();
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-  const Stack st = wave_stack(smem + s.world_block_floats);
+  const Stack st = wave_stack(s, smem + s.world_block_floats);
   int32_t cam, tx, ty;
   tile_of(wm.geo, blockIdx.x, &cam, &tx, &ty);
   Pixel p;
@@ -375,7 +370,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_mirror_k
                                                                const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-  const Stack st = wave_stack(smem);
+  const Stack st = wave_stack(s, smem);
   const bool cull = s.settings.cull_backfaces != 0;
   const int32_t count = (int32_t)min((int64_t)*wm.counters, wm.mirror_cap);
   int32_t err = 0;
@@ -436,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_shadow_k
                                                                const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-  const Stack st = wave_stack(smem);
+  const Stack st = wave_stack(s, smem);
   const bool cull = s.settings.cull_backfaces != 0;
   const int32_t ns = s.settings.shadow_samples;
   const int32_t count = (int32_t)min((int64_t)wm.counters[1], wm.shadow_cap);
@@ -678,7 +673,7 @@ int set_smem(K kern, size_t smem, const char* what) {
 
 template <bool kMesh, bool kTex>
 int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t chunk, int32_t per_world) {
-  const size_t stack = (size_t)kThreads * kStackDepth * 8;
+  const size_t stack = (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
   const size_t blk_bytes = (size_t)s.world_block_floats * sizeof(float);
   auto k_primary = wave_primary_kernel<kMesh>;
   auto k_surface = wave_surface_kernel<kMesh, kTex>;

@@ -16,14 +16,29 @@
 
 namespace mjpbr {
 
-// Stack entries per thread.
-constexpr int kStackDepth = 32;
+// Stack entries per thread of a launch: settings.stack_depth clamped to [8, kStackDepth] (0: the most).
+MJ_HD int32_t stack_entries(int32_t requested) {
+  return requested <= 0 ? kStackDepth : (requested < 8 ? 8 : (requested > kStackDepth ? kStackDepth : requested));
+}
 
 struct Stack {
   int32_t* code;  // (ref << 3) | count, see world_block.cuh
   float* t;       // entry distance of the pushed child
   int32_t stride;
+  int32_t cap;    // entries per thread
 };
+
+// The stack of thread threadIdx.x among nthreads in shared memory at base (nthreads * cap codes,
+// then nthreads * cap distances).
+MJ_DEV Stack shared_stack(float* base, int32_t nthreads, int32_t cap) {
+  Stack st;
+  int32_t* b = reinterpret_cast<int32_t*>(base);
+  st.code = b + threadIdx.x;
+  st.t = reinterpret_cast<float*>(b + nthreads * cap) + threadIdx.x;
+  st.stride = nthreads;
+  st.cap = cap;
+  return st;
+}
 
 MJ_DEV GeomFrame geom_frame(const float* g) {
   GeomFrame f;
@@ -44,7 +59,7 @@ MJ_DEV GeomFrame geom_frame(const float* g) {
 MJ_DEV float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
 MJ_DEV void push(const Stack& st, int& sp, int32_t code, float t, int32_t* err) {
-  if (sp < kStackDepth) {
+  if (sp < st.cap) {
     st.code[sp * st.stride] = code;
     st.t[sp * st.stride] = t;
     ++sp;

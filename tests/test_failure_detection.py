@@ -87,6 +87,8 @@ def test_a_valid_host_descriptor_passes_validation():
     (lambda s: setattr(s.settings, "queue_item", 48), b"work queue"),
     (lambda s: setattr(s, "wave_scratch_bytes", -1), b"wave_scratch_bytes"),
     (lambda s: setattr(s.settings, "schedule", 7), b"settings.schedule"),
+    (lambda s: setattr(s.settings, "stack_depth", 33), b"settings.stack_depth"),
+    (lambda s: setattr(s.settings, "stack_depth", 4), b"settings.stack_depth"),
   ],
 )
 def test_corrupted_pixel_maps_and_queues_are_rejected_before_launch(corrupt, fragment):
