@@ -166,8 +166,8 @@ def algorithmic_bytes(rc) -> int:
 
 
 def _traffic(workload: str) -> float | None:
-  """DRAM bytes per launch of the workload's render kernel from an ncu capture
-  (profiles/ncu_traffic.txt: workload, bytes per launch, kernel), or None."""
+  """DRAM bytes of one frame's render kernels from an ncu launch list (profiles/ncu_traffic.txt:
+  workload, bytes per frame, kernels), or None."""
   p = ROOT / "profiles" / "ncu_traffic.txt"
   if not p.exists():
     return None
@@ -236,7 +236,8 @@ def path_tier(dev, steps: int, nworld: int = 1024, res: int = 128, spp: int = 2)
   rcs = mjpbr.create_render_context(small.mjm, small.nworld, data=small.mjd, device=dev, **small.options)
   synthetic.apply_per_world(small, ms_, rcs)
   counts = roofline.count_frame(mjpbr.scene_descriptor(ms_, ds_, rcs), 100, stream.cuda_stream)
-  fp32 = roofline.fp32_roofline(counts, small.nworld * res * res, npix, avg, kernel="pt_kernel")
+  fp32 = roofline.fp32_roofline(counts, small.nworld * res * res, npix, avg,
+                               kernel="path wavefront: ptw_start, ptw_extend, ptw_shade, ptw_shadow, ptw_resolve per chunk")
   return {
     "workload": sc.name,
     "value": npix / (avg / 1000.0) / 1e6,
@@ -476,9 +477,9 @@ def run(args) -> None:
     traffic = _traffic(sc.name)
     launches = render_launches(rc, int(chunks.value), int(scene.nlight))
     if args.workload == "path":
-      kernel = "pt_kernel"
+      kernel = "path wavefront: ptw_start, ptw_extend, ptw_shade, ptw_shadow, ptw_resolve per chunk, one frame"
     elif wave:
-      kernel = "wavefront render: wave_primary, wave_surface, wave_mirror, wave_mirror_surface, wave_shadow, wave_resolve per chunk"
+      kernel = "wavefront render: wave_primary, wave_surface, wave_mirror, wave_mirror_surface, wave_shadow, wave_resolve per chunk, one frame"
     else:
       kernel = "rt_kernel"
     line = {

@@ -44,7 +44,7 @@ constexpr int kTile = 16;  // pixel tiles of 16 x 16, addressed in Z order withi
 #define MJPBR_WAVE_TRACE_CTAS 3
 #endif
 #ifndef MJPBR_WAVE_SHADE_CTAS
-#define MJPBR_WAVE_SHADE_CTAS 2
+#define MJPBR_WAVE_SHADE_CTAS 3
 #endif
 
 struct __align__(16) HitRec {
