@@ -91,7 +91,7 @@ struct WaveMap {
   int32_t* vis;          // (sample, segment, light) unoccluded shadow rays
   MirrorEntry* mirror;
   ShadowEntry* shadow;
-  int32_t* counters;     // [0] mirror entries, [1] shadow entries
+  int32_t* counters;     // [0] mirror entries, [1] shadow entries, [2..3] the shadow stage's fetch counter (64-bit)
   int64_t mirror_cap, shadow_cap;
 };
 
@@ -241,6 +241,7 @@ MJ_DEV void emit_shadows(const MjpbrScene& s, const WaveMap& wm, const float* bl
       e.o = make_float4(origin.x, origin.y, origin.z, dist);
       e.l = make_float4(l.x, l.y, l.z, __int_as_float((sample * 2 + seg) * wm.nl + li));
       wm.shadow[pos] = e;
+      wm.vis[(sample * 2 + seg) * wm.nl + li] = 0;  // the shadow stage adds its unoccluded rays
     }
   }
 }
@@ -426,6 +427,23 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_mirror_s
 }
 
 // ---------------------------------------------------------------- 5. shadow rays (persistent)
+// Steps a lane runs between refills of the warp's idle lanes.
+#ifndef MJPBR_WAVE_SHADOW_STEPS
+#define MJPBR_WAVE_SHADOW_STEPS 32
+#endif
+constexpr int32_t kMaxRaySteps = 1 << 20;        // steps of one shadow ray: far above any traversal of the scene
+constexpr uint64_t kShadowTimeLimitNs = 4000000000ull;
+
+MJ_DEV uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Work items: (entry, ray k < shadow_samples); the lanes of a warp take items from a counter as
+// soon as their last ray is done (one atomic per warp per refill), trace them as resumable any-hit
+// queries and add each unoccluded ray to its entry's count (an integer sum, so the counts do not
+// depend on the order).
 template <bool kMesh>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_shadow_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                const __grid_constant__ WaveMap wm) {
@@ -433,31 +451,80 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_shadow_k
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const Stack st = wave_stack(s, smem);
   const bool cull = s.settings.cull_backfaces != 0;
-  const int32_t ns = s.settings.shadow_samples;
-  const int32_t count = (int32_t)min((int64_t)wm.counters[1], wm.shadow_cap);
+  const int32_t ns = max(s.settings.shadow_samples, 1);
+  const int64_t items = min((int64_t)wm.counters[1], wm.shadow_cap) * ns;
+  unsigned long long* fetch = reinterpret_cast<unsigned long long*>(wm.counters + 2);
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   int32_t err = 0;
-  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
-    const ShadowEntry e = wm.shadow[i];
-    const int32_t target = __float_as_int(e.l.w);
-    const int32_t li = target % wm.nl;
-    const int32_t sample = target / (2 * wm.nl);
-    const int32_t seg = (target / wm.nl) & 1;
-    int32_t w, cam, pixelid, smp;
-    sample_pixel(s, wm, sample, &w, &cam, &pixelid, &smp);
-    const float* blk = s.world_blocks + (int64_t)w * s.world_block_floats;
-    const Light light = load_light(blk + L.light_off + li * kLightFloats);
-    const uint32_t pseed = pixel_seed_of(s, seed, w, cam, pixelid);
-    const V3 origin{e.o.x, e.o.y, e.o.z}, l{e.l.x, e.l.y, e.l.z};
-    const int32_t nray = shadow_ray_count(light, ns);
-    int32_t visible = 0;
-    for (int32_t k = 0; k < nray; ++k) {
-      Ray r;
-      float max_dist;
-      r.o = origin;
-      shadow_ray(light, ns, origin, l, e.o.w, pseed, 2 * smp + seg, L.nlight, li, k, &r.d, &max_dist);
-      if (trace_ray<kMesh>(s, st, blk, L, r, max_dist, cull, true, &err).geom == -1) ++visible;
+  AnyQuery q;
+  const float* blk = nullptr;
+  int32_t steps = 0;
+  int32_t target = -1;  // the count the lane's ray adds to; -1: no ray
+  bool exhausted = false;
+  // every trip takes new items or advances a ray, so the loop ends; a launch still running after
+  // kShadowTimeLimitNs (three orders of magnitude above the largest chunk's) reports a broken queue
+  // and returns instead of spinning
+  const uint64_t t_start = global_ns();
+  for (;;) {
+    if (__any_sync(full, global_ns() - t_start > kShadowTimeLimitNs)) {
+      err |= kErrWorkQueue;
+      break;
     }
-    wm.vis[target] = visible;
+    const bool need = target < 0 && !exhausted;
+    const unsigned m = __ballot_sync(full, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(fetch, (unsigned long long)__popc(m));
+      base = __shfl_sync(full, base, leader);
+      if (need) {
+        const int64_t item = (int64_t)base + __popc(m & ((1u << lane) - 1u));
+        if (item >= items) {
+          exhausted = true;
+        } else {
+          const int32_t ei = (int32_t)(item / ns), k = (int32_t)(item - (int64_t)ei * ns);
+          const ShadowEntry e = wm.shadow[ei];
+          const int32_t tgt = __float_as_int(e.l.w);
+          const int32_t li = tgt % wm.nl;
+          const int32_t sample = tgt / (2 * wm.nl);
+          const int32_t seg = (tgt / wm.nl) & 1;
+          int32_t w, cam, pixelid, smp;
+          sample_pixel(s, wm, sample, &w, &cam, &pixelid, &smp);
+          blk = s.world_blocks + (int64_t)w * s.world_block_floats;
+          const Light light = load_light(blk + L.light_off + li * kLightFloats);
+          if (k < shadow_ray_count(light, ns)) {
+            steps = 0;
+            Ray r;
+            float max_dist;
+            r.o = V3{e.o.x, e.o.y, e.o.z};
+            shadow_ray(light, ns, r.o, V3{e.l.x, e.l.y, e.l.z}, e.o.w, pixel_seed_of(s, seed, w, cam, pixelid), 2 * smp + seg, L.nlight, li,
+                       k, &r.d, &max_dist);
+            any_begin(q, st, r, max_dist, &err);
+            target = tgt;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(full, target >= 0) == 0) {
+      if (__all_sync(full, exhausted)) break;
+      continue;
+    }
+    if (target >= 0) {
+#pragma unroll 1
+      for (int32_t step = 0; step < MJPBR_WAVE_SHADOW_STEPS; ++step) {
+        int32_t res = any_step<kMesh>(q, s, st, blk, L, cull, &err);
+        if (++steps > kMaxRaySteps) {  // more steps than any tree of the scene can take
+          err |= kErrWorkQueue;
+          res = kAnyHit;
+        }
+        if (res != kAnyRunning) {
+          if (res == kAnyClear) atomicAdd(&wm.vis[target], 1);
+          target = -1;
+          break;
+        }
+      }
+    }
   }
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
@@ -714,7 +781,7 @@ int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t
     }
     stage_mark(stream);
     if (rgb_tiles > 0) {
-      cudaError_t e = cudaMemsetAsync(wm.counters, 0, 2 * sizeof(int32_t), stream);
+      cudaError_t e = cudaMemsetAsync(wm.counters, 0, 4 * sizeof(int32_t), stream);  // queue lengths, shadow fetch counter
       if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "wavefront queue counters: %s", cudaGetErrorString(e));
       k_surface<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, wm);
       if ((rc = check_launch("wave_surface_kernel"))) return rc;

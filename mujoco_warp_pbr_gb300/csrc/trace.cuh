@@ -255,4 +255,131 @@ __device__ __noinline__ Hit trace_ray(const MjpbrScene& sc, const Stack& st, con
   return h;
 }
 
+// Primitive geom g (plane, sphere, ellipsoid, capsule, cylinder, box) against the ray: distance or -1,
+// world normal in *n; -1 for the geoms traced through a triangle BVH.
+MJ_DEV float intersect_primitive(const float* g, const Ray& r, V3* n) {
+  const GeomFrame f = geom_frame(g);
+  switch (__float_as_int(g[3])) {
+    case MJPBR_GEOM_PLANE:
+      MJPBR_COUNT(kOpPlane);
+      return ray_plane(f, r, n);
+    case MJPBR_GEOM_SPHERE:
+      MJPBR_COUNT(kOpSphere);
+      return ray_sphere(f, r, n);
+    case MJPBR_GEOM_ELLIPSOID:
+      MJPBR_COUNT(kOpEllipsoid);
+      return ray_ellipsoid(f, r, n);
+    case MJPBR_GEOM_CAPSULE:
+      MJPBR_COUNT(kOpCapsule);
+      return ray_capsule(f, r, n);
+    case MJPBR_GEOM_CYLINDER:
+      MJPBR_COUNT(kOpCylinder);
+      return ray_cylinder(f, r, n);
+    case MJPBR_GEOM_BOX:
+      MJPBR_COUNT(kOpBoxPrim);
+      return ray_box(f, r, n);
+    default:
+      return -1.0f;
+  }
+}
+
+// Triangle BVH of geom g (a mesh's, an SDF's mesh or a height field's), -1 for none.
+MJ_DEV int32_t geom_bvh(const float* g) {
+  const int32_t type = __float_as_int(g[3]);
+  if (type != MJPBR_GEOM_MESH && type != MJPBR_GEOM_SDF && type != MJPBR_GEOM_HFIELD) return -1;
+  return __float_as_int(g[17]);
+}
+
+// Any-hit query as a resumable state machine, for persistent kernels whose lanes take a new ray
+// as soon as their last one is done instead of waiting for the warp's slowest ray: any_begin sets
+// up the ray, any_step advances it by one step (a scene node, one geom of a scene leaf, a mesh node
+// or a mesh leaf) and returns kAnyRunning, kAnyClear (no hit before max_dist) or kAnyHit. The
+// tests and their order are trace_ray's with any = true, step for step (including the op counts).
+constexpr int32_t kAnyRunning = 0, kAnyClear = 1, kAnyHit = 2;
+
+struct AnyQuery {
+  Ray r;
+  RayInv ri;
+  float max_dist, cut;
+  int32_t sp, leaf, leaf_end;
+  int32_t m_base;  // the mesh traversal's stack base while a mesh is being traced, else -1
+  const float* m_nodes;
+  const float* m_tris;
+  WoopRay m_w;
+  RayInv m_ri;
+};
+
+MJ_DEV void any_begin(AnyQuery& q, const Stack& st, const Ray& r, float max_dist, int32_t* err) {
+  MJPBR_COUNT(kOpRayAny);
+  q.r = r;
+  q.ri = make_inv(r);
+  q.max_dist = max_dist;
+  q.cut = max_dist * (1.0f + kRayTolRel) + kRayTolAbs;
+  q.sp = 0;
+  q.leaf = q.leaf_end = 0;
+  q.m_base = -1;
+  push(st, q.sp, 0, 0.0f, err);
+}
+
+template <bool kMesh>
+MJ_DEV int32_t any_step(AnyQuery& q, const MjpbrScene& sc, const Stack& st, const float* blk, const BlockLayout& L, bool cull,
+                        int32_t* err) {
+  if (kMesh && q.m_base >= 0) {
+    if (q.sp == q.m_base) {  // the mesh is done without a hit
+      q.m_base = -1;
+      return kAnyRunning;
+    }
+    --q.sp;
+    if (st.t[q.sp * st.stride] >= q.max_dist) return kAnyRunning;
+    const int32_t code = st.code[q.sp * st.stride];
+    const int32_t ref = code >> 3, cnt = code & 7;
+    if (cnt == 0) {
+      const float* nd = q.m_nodes + (int64_t)ref * kNodeFloats;
+      expand(st, q.sp, q.m_ri, ldg4(nd), ldg4(nd + 4), ldg4(nd + 8), ldg4(nd + 12), q.max_dist, err);
+      return kAnyRunning;
+    }
+    for (int32_t i = ref; i < ref + cnt; ++i) {
+      const float* tr = q.m_tris + (int64_t)i * kTriFloats;
+      const float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
+      float tu, tv;
+      MJPBR_COUNT(kOpTri);
+      if (woop_hit(q.m_w, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{c.x, c.y, c.z}, q.max_dist, &tu, &tv) >= 0.0f) return kAnyHit;
+    }
+    return kAnyRunning;
+  }
+  if (q.leaf < q.leaf_end) {  // the next geom of the scene leaf
+    const float* g = blk + L.geom_off + (q.leaf++) * kGeomFloats;
+    if (__float_as_int(g[19]) & kGeomFlagSkip) return kAnyRunning;
+    const int32_t bvh = kMesh ? geom_bvh(g) : -1;
+    if (bvh >= 0) {  // trace the mesh from the next steps, its entries above the scene's
+      V3 lo, ld;
+      map_local(geom_frame(g), q.r, &lo, &ld);
+      q.m_nodes = sc.blas_nodes + (int64_t)sc.blas_root[bvh] * kNodeFloats;
+      q.m_tris = sc.blas_tris + (int64_t)sc.blas_tri_base[bvh] * kTriFloats;
+      q.m_w = woop_setup(lo, ld);
+      q.m_ri = make_inv(Ray{lo, ld});
+      q.m_base = q.sp;
+      push(st, q.sp, 0, 0.0f, err);
+      return kAnyRunning;
+    }
+    V3 n = v3(0.0f);
+    float d = intersect_primitive(g, q.r, &n);
+    if (cull && d >= 0.0f && dot(q.r.d, n) > 0.0f) d = -1.0f;
+    return (d >= 0.0f && d < q.max_dist) ? kAnyHit : kAnyRunning;
+  }
+  if (q.sp == 0) return kAnyClear;
+  --q.sp;
+  if (st.t[q.sp * st.stride] >= q.cut) return kAnyRunning;
+  const int32_t code = st.code[q.sp * st.stride];
+  const int32_t ref = code >> 3, cnt = code & 7;
+  if (cnt == 0) {
+    const float4* nd = reinterpret_cast<const float4*>(blk + L.node_off + ref * kNodeFloats);
+    expand(st, q.sp, q.ri, nd[0], nd[1], nd[2], nd[3], q.cut, err);
+  } else {
+    q.leaf = ref;
+    q.leaf_end = ref + cnt;
+  }
+  return kAnyRunning;
+}
+
 }  // namespace mjpbr
