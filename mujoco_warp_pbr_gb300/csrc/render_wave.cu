@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "abi_internal.h"
+#include "refill.cuh"
 #include "rt_shade.cuh"
 
 namespace mjpbr {
@@ -42,6 +43,9 @@ constexpr int kTile = 16;  // pixel tiles of 16 x 16, addressed in Z order withi
 // shadow: 64 KB of traversal stacks per CTA) and of the surface / shading stages targets.
 #ifndef MJPBR_WAVE_TRACE_CTAS
 #define MJPBR_WAVE_TRACE_CTAS 3
+#endif
+#ifndef MJPBR_WAVE_MIRROR_CTAS
+#define MJPBR_WAVE_MIRROR_CTAS 3
 #endif
 #ifndef MJPBR_WAVE_SHADE_CTAS
 #define MJPBR_WAVE_SHADE_CTAS 3
@@ -91,7 +95,7 @@ struct WaveMap {
   int32_t* vis;          // (sample, segment, light) unoccluded shadow rays
   MirrorEntry* mirror;
   ShadowEntry* shadow;
-  int32_t* counters;     // [0] mirror entries, [1] shadow entries, [2..3] the shadow stage's fetch counter (64-bit)
+  int32_t* counters;     // [0] mirror entries, [1] shadow entries; 64-bit fetch counters of the shadow [2..3] and mirror [4..5] stages
   int64_t mirror_cap, shadow_cap;
 };
 
@@ -366,23 +370,35 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_surface_
 }
 
 // ---------------------------------------------------------------- 3. mirror rays (persistent)
+// Steps a lane runs between refills of the warp's idle lanes (mirror and shadow stages).
+#ifndef MJPBR_WAVE_REFILL_STEPS
+#define MJPBR_WAVE_REFILL_STEPS 32
+#endif
+
+// Closest hit of every queued mirror ray, lanes refilled from the queue (refill.cuh).
 template <bool kMesh>
-__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_mirror_kernel(const __grid_constant__ MjpbrScene s,
+__global__ void __launch_bounds__(kThreads, MJPBR_WAVE_MIRROR_CTAS) wave_mirror_kernel(const __grid_constant__ MjpbrScene s,
                                                                const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const Stack st = wave_stack(s, smem);
   const bool cull = s.settings.cull_backfaces != 0;
-  const int32_t count = (int32_t)min((int64_t)*wm.counters, wm.mirror_cap);
+  const int64_t items = min((int64_t)wm.counters[0], wm.mirror_cap);
   int32_t err = 0;
-  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
-    const MirrorEntry e = wm.mirror[i];
-    const int32_t sample = e.index.x;
-    const float* blk = s.world_blocks + (int64_t)(wm.w0 + sample / wm.per_world) * s.world_block_floats;
-    const Ray ray{V3{e.o.x, e.o.y, e.o.z}, V3{e.d.x, e.d.y, e.d.z}};
-    const Hit hit = trace_ray<kMesh>(s, st, blk, L, ray, kMaxVal, cull, false, &err);
-    wm.hit[1][sample] = pack_hit(hit);
-  }
+  ClosestQuery q;
+  const float* blk = nullptr;
+  int32_t sample = -1;
+  refill_loop<MJPBR_WAVE_REFILL_STEPS>(
+      items, reinterpret_cast<unsigned long long*>(wm.counters + 4), q,
+      [&](int64_t item, ClosestQuery& qq) {
+        const MirrorEntry e = wm.mirror[item];
+        sample = e.index.x;
+        blk = s.world_blocks + (int64_t)(wm.w0 + sample / wm.per_world) * s.world_block_floats;
+        closest_begin(qq, st, Ray{V3{e.o.x, e.o.y, e.o.z}, V3{e.d.x, e.d.y, e.d.z}}, kMaxVal, &err);
+        return true;
+      },
+      [&](ClosestQuery& qq) { return closest_step<kMesh>(qq, s, st, blk, L, cull, &err); },
+      [&](ClosestQuery& qq, int32_t) { wm.hit[1][sample] = pack_hit(qq.h); }, &err);
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
@@ -427,23 +443,9 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_mirror_s
 }
 
 // ---------------------------------------------------------------- 5. shadow rays (persistent)
-// Steps a lane runs between refills of the warp's idle lanes.
-#ifndef MJPBR_WAVE_SHADOW_STEPS
-#define MJPBR_WAVE_SHADOW_STEPS 32
-#endif
-constexpr int32_t kMaxRaySteps = 1 << 20;        // steps of one shadow ray: far above any traversal of the scene
-constexpr uint64_t kShadowTimeLimitNs = 4000000000ull;
-
-MJ_DEV uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Work items: (entry, ray k < shadow_samples); the lanes of a warp take items from a counter as
-// soon as their last ray is done (one atomic per warp per refill), trace them as resumable any-hit
-// queries and add each unoccluded ray to its entry's count (an integer sum, so the counts do not
-// depend on the order).
+// Work items: (entry, ray k < shadow_samples), traced as any-hit queries with lanes refilled from
+// the queue (refill.cuh); each unoccluded ray adds one to its entry's count (an integer sum, so
+// the counts do not depend on the order).
 template <bool kMesh>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_shadow_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                const __grid_constant__ WaveMap wm) {
@@ -453,79 +455,38 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_shadow_k
   const bool cull = s.settings.cull_backfaces != 0;
   const int32_t ns = max(s.settings.shadow_samples, 1);
   const int64_t items = min((int64_t)wm.counters[1], wm.shadow_cap) * ns;
-  unsigned long long* fetch = reinterpret_cast<unsigned long long*>(wm.counters + 2);
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
   int32_t err = 0;
   AnyQuery q;
   const float* blk = nullptr;
-  int32_t steps = 0;
-  int32_t target = -1;  // the count the lane's ray adds to; -1: no ray
-  bool exhausted = false;
-  // every trip takes new items or advances a ray, so the loop ends; a launch still running after
-  // kShadowTimeLimitNs (three orders of magnitude above the largest chunk's) reports a broken queue
-  // and returns instead of spinning
-  const uint64_t t_start = global_ns();
-  for (;;) {
-    if (__any_sync(full, global_ns() - t_start > kShadowTimeLimitNs)) {
-      err |= kErrWorkQueue;
-      break;
-    }
-    const bool need = target < 0 && !exhausted;
-    const unsigned m = __ballot_sync(full, need);
-    if (m) {
-      const int leader = __ffs(m) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(fetch, (unsigned long long)__popc(m));
-      base = __shfl_sync(full, base, leader);
-      if (need) {
-        const int64_t item = (int64_t)base + __popc(m & ((1u << lane) - 1u));
-        if (item >= items) {
-          exhausted = true;
-        } else {
-          const int32_t ei = (int32_t)(item / ns), k = (int32_t)(item - (int64_t)ei * ns);
-          const ShadowEntry e = wm.shadow[ei];
-          const int32_t tgt = __float_as_int(e.l.w);
-          const int32_t li = tgt % wm.nl;
-          const int32_t sample = tgt / (2 * wm.nl);
-          const int32_t seg = (tgt / wm.nl) & 1;
-          int32_t w, cam, pixelid, smp;
-          sample_pixel(s, wm, sample, &w, &cam, &pixelid, &smp);
-          blk = s.world_blocks + (int64_t)w * s.world_block_floats;
-          const Light light = load_light(blk + L.light_off + li * kLightFloats);
-          if (k < shadow_ray_count(light, ns)) {
-            steps = 0;
-            Ray r;
-            float max_dist;
-            r.o = V3{e.o.x, e.o.y, e.o.z};
-            shadow_ray(light, ns, r.o, V3{e.l.x, e.l.y, e.l.z}, e.o.w, pixel_seed_of(s, seed, w, cam, pixelid), 2 * smp + seg, L.nlight, li,
-                       k, &r.d, &max_dist);
-            any_begin(q, st, r, max_dist, &err);
-            target = tgt;
-          }
-        }
-      }
-    }
-    if (__ballot_sync(full, target >= 0) == 0) {
-      if (__all_sync(full, exhausted)) break;
-      continue;
-    }
-    if (target >= 0) {
-#pragma unroll 1
-      for (int32_t step = 0; step < MJPBR_WAVE_SHADOW_STEPS; ++step) {
-        int32_t res = any_step<kMesh>(q, s, st, blk, L, cull, &err);
-        if (++steps > kMaxRaySteps) {  // more steps than any tree of the scene can take
-          err |= kErrWorkQueue;
-          res = kAnyHit;
-        }
-        if (res != kAnyRunning) {
-          if (res == kAnyClear) atomicAdd(&wm.vis[target], 1);
-          target = -1;
-          break;
-        }
-      }
-    }
-  }
+  int32_t target = -1;
+  refill_loop<MJPBR_WAVE_REFILL_STEPS>(
+      items, reinterpret_cast<unsigned long long*>(wm.counters + 2), q,
+      [&](int64_t item, AnyQuery& qq) {
+        const int32_t ei = (int32_t)(item / ns), k = (int32_t)(item - (int64_t)ei * ns);
+        const ShadowEntry e = wm.shadow[ei];
+        const int32_t tgt = __float_as_int(e.l.w);
+        const int32_t li = tgt % wm.nl;
+        const int32_t sample = tgt / (2 * wm.nl);
+        const int32_t seg = (tgt / wm.nl) & 1;
+        int32_t w, cam, pixelid, smp;
+        sample_pixel(s, wm, sample, &w, &cam, &pixelid, &smp);
+        blk = s.world_blocks + (int64_t)w * s.world_block_floats;
+        const Light light = load_light(blk + L.light_off + li * kLightFloats);
+        if (k >= shadow_ray_count(light, ns)) return false;
+        Ray r;
+        float max_dist;
+        r.o = V3{e.o.x, e.o.y, e.o.z};
+        shadow_ray(light, ns, r.o, V3{e.l.x, e.l.y, e.l.z}, e.o.w, pixel_seed_of(s, seed, w, cam, pixelid), 2 * smp + seg, L.nlight, li, k,
+                   &r.d, &max_dist);
+        any_begin(qq, st, r, max_dist, &err);
+        target = tgt;
+        return true;
+      },
+      [&](AnyQuery& qq) { return any_step<kMesh>(qq, s, st, blk, L, cull, &err); },
+      [&](AnyQuery&, int32_t res) {
+        if (res == kAnyClear) atomicAdd(&wm.vis[target], 1);
+      },
+      &err);
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
@@ -781,7 +742,7 @@ int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t
     }
     stage_mark(stream);
     if (rgb_tiles > 0) {
-      cudaError_t e = cudaMemsetAsync(wm.counters, 0, 4 * sizeof(int32_t), stream);  // queue lengths, shadow fetch counter
+      cudaError_t e = cudaMemsetAsync(wm.counters, 0, 6 * sizeof(int32_t), stream);  // queue lengths, fetch counters
       if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "wavefront queue counters: %s", cudaGetErrorString(e));
       k_surface<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, wm);
       if ((rc = check_launch("wave_surface_kernel"))) return rc;

@@ -382,4 +382,143 @@ MJ_DEV int32_t any_step(AnyQuery& q, const MjpbrScene& sc, const Stack& st, cons
   return kAnyRunning;
 }
 
+// Closest-hit query as a resumable state machine (the persistent refill kernels' counterpart of
+// trace_ray with any = false): closest_begin sets up the ray, closest_step advances it by one step
+// and returns kAnyRunning until the query is done (kAnyClear), the best hit in q.h. The tests, their
+// order and the hit selection (tolerance, tie-break to the higher geom id, culling) are
+// trace_ray's, step for step.
+struct ClosestQuery {
+  Ray r;
+  RayInv ri;
+  Hit h;
+  int32_t sp, leaf, leaf_end;
+  int32_t m_slot, m_bvh, m_base, m_face;  // the mesh geom being traced (m_slot -1: none)
+  const float* m_nodes;
+  const float* m_tris;
+  WoopRay m_w;
+  RayInv m_ri;
+  V3 m_ld, m_n;
+  float m_best, m_u, m_v;
+};
+
+MJ_DEV void closest_begin(ClosestQuery& q, const Stack& st, const Ray& r, float max_dist, int32_t* err) {
+  MJPBR_COUNT(kOpRayClosest);
+  q.r = r;
+  q.ri = make_inv(r);
+  q.h.geom = -1;
+  q.h.slot = -1;
+  q.h.dist = max_dist;
+  q.h.normal = v3(0.0f);
+  q.h.u = q.h.v = 0.0f;
+  q.h.face = -1;
+  q.h.mesh = -1;
+  q.sp = 0;
+  q.leaf = q.leaf_end = 0;
+  q.m_slot = -1;
+  push(st, q.sp, 0, 0.0f, err);
+}
+
+// A geom's hit (d >= 0) against the best so far (trace_ray's selection).
+MJ_DEV void closest_offer(ClosestQuery& q, const float* g, int32_t slot, float d, V3 n, float u, float v, int32_t face, int32_t mesh,
+                          bool cull) {
+  if (cull && d >= 0.0f && dot(q.r.d, n) > 0.0f) d = -1.0f;
+  const int32_t gi = __float_as_int(g[16]);
+  const float tol = kRayTolRel * fmaxf(q.h.dist, 1.0f);
+  const bool closer = (d < q.h.dist - tol) || (fabsf(d - q.h.dist) <= tol && (q.h.geom < 0 || gi > q.h.geom));
+  if (d >= 0.0f && closer) {
+    q.h.dist = d;
+    q.h.normal = n;
+    q.h.geom = gi;
+    q.h.slot = slot;
+    q.h.u = u;
+    q.h.v = v;
+    q.h.face = face;
+    q.h.mesh = mesh;
+  }
+}
+
+template <bool kMesh>
+MJ_DEV int32_t closest_step(ClosestQuery& q, const MjpbrScene& sc, const Stack& st, const float* blk, const BlockLayout& L, bool cull,
+                            int32_t* err) {
+  if (kMesh && q.m_slot >= 0) {
+    if (q.sp > q.m_base) {  // one step of the mesh traversal
+      --q.sp;
+      if (st.t[q.sp * st.stride] >= q.m_best) return kAnyRunning;
+      const int32_t code = st.code[q.sp * st.stride];
+      const int32_t ref = code >> 3, cnt = code & 7;
+      if (cnt == 0) {
+        const float* nd = q.m_nodes + (int64_t)ref * kNodeFloats;
+        expand(st, q.sp, q.m_ri, ldg4(nd), ldg4(nd + 4), ldg4(nd + 8), ldg4(nd + 12), q.m_best, err);
+        return kAnyRunning;
+      }
+      for (int32_t i = ref; i < ref + cnt; ++i) {
+        const float* tr = q.m_tris + (int64_t)i * kTriFloats;
+        const float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
+        const V3 v0{a.x, a.y, a.z}, v1{b.x, b.y, b.z}, v2{c.x, c.y, c.z};
+        float tu, tv;
+        MJPBR_COUNT(kOpTri);
+        const float t = woop_hit(q.m_w, v0, v1, v2, q.m_best, &tu, &tv);
+        if (t < 0.0f) continue;
+        const V3 ng = cross(v1 - v0, v2 - v0);
+        if (cull && dot(q.m_ld, ng) > 0.0f) continue;
+        q.m_best = t;
+        q.m_face = __float_as_int(a.w);
+        q.m_n = ng;
+        q.m_u = tu;
+        q.m_v = tv;
+      }
+      return kAnyRunning;
+    }
+    // the mesh is done: its hit goes through the same selection as a primitive's
+    const int32_t slot = q.m_slot;
+    q.m_slot = -1;
+    const float* g = blk + L.geom_off + slot * kGeomFloats;
+    if (q.m_face >= 0) {
+      closest_offer(q, g, slot, q.m_best, mul(geom_frame(g).mat, normalize(q.m_n)), q.m_u, q.m_v, q.m_face, q.m_bvh, cull);
+    }
+    return kAnyRunning;
+  }
+  if (q.leaf < q.leaf_end) {  // the next geom of the scene leaf
+    const int32_t slot = q.leaf++;
+    const float* g = blk + L.geom_off + slot * kGeomFloats;
+    if (__float_as_int(g[19]) & kGeomFlagSkip) return kAnyRunning;
+    const int32_t bvh = kMesh ? geom_bvh(g) : -1;
+    if (bvh >= 0) {  // trace the mesh from the next steps, its entries above the scene's
+      V3 lo;
+      map_local(geom_frame(g), q.r, &lo, &q.m_ld);
+      q.m_nodes = sc.blas_nodes + (int64_t)sc.blas_root[bvh] * kNodeFloats;
+      q.m_tris = sc.blas_tris + (int64_t)sc.blas_tri_base[bvh] * kTriFloats;
+      q.m_w = woop_setup(lo, q.m_ld);
+      q.m_ri = make_inv(Ray{lo, q.m_ld});
+      q.m_best = q.h.dist * (1.0f + kRayTolRel) + kRayTolAbs;
+      q.m_face = -1;
+      q.m_n = v3(0.0f);
+      q.m_u = q.m_v = 0.0f;
+      q.m_slot = slot;
+      q.m_bvh = bvh;
+      q.m_base = q.sp;
+      push(st, q.sp, 0, 0.0f, err);
+      return kAnyRunning;
+    }
+    V3 n = v3(0.0f);
+    const float d = intersect_primitive(g, q.r, &n);
+    closest_offer(q, g, slot, d, n, 0.0f, 0.0f, -1, -1, cull);
+    return kAnyRunning;
+  }
+  if (q.sp == 0) return kAnyClear;
+  --q.sp;
+  const float cut = q.h.dist * (1.0f + kRayTolRel) + kRayTolAbs;
+  if (st.t[q.sp * st.stride] >= cut) return kAnyRunning;
+  const int32_t code = st.code[q.sp * st.stride];
+  const int32_t ref = code >> 3, cnt = code & 7;
+  if (cnt == 0) {
+    const float4* nd = reinterpret_cast<const float4*>(blk + L.node_off + ref * kNodeFloats);
+    expand(st, q.sp, q.ri, nd[0], nd[1], nd[2], nd[3], cut, err);
+  } else {
+    q.leaf = ref;
+    q.leaf_end = ref + cnt;
+  }
+  return kAnyRunning;
+}
+
 }  // namespace mjpbr
