@@ -28,6 +28,7 @@
 
 #include "abi_internal.h"
 #include "pt_bounce.cuh"
+#include "refill.cuh"
 
 namespace mjpbr {
 namespace {
@@ -84,7 +85,7 @@ struct PtWaveMap {
   uint8_t* vis;            // (npath, nslot)
   int32_t* queue[2];
   ShadowEntry* shadow;
-  int32_t* counters;       // [0], [1] queue lengths, [2] shadow entries
+  int32_t* counters;       // [0], [1] queue lengths, [2] shadow entries; 64-bit fetch counters of extend [4..5], shadow [6..7]
   int64_t path_cap, shadow_cap;
 };
 
@@ -278,6 +279,7 @@ __global__ void __launch_bounds__(kThreads) ptw_start_kernel(const __grid_consta
   if (path == 0) {
     wm.counters[0] = wm.npath;
     wm.counters[1] = 0;
+    for (int k = 4; k < 8; ++k) wm.counters[k] = 0;  // the extend and shadow stages' fetch counters
   }
   if (path >= wm.npath) return;
   int32_t w, sample;
@@ -329,6 +331,13 @@ __global__ void __launch_bounds__(kThreads) ptw_geometry_kernel(const __grid_con
 }
 
 // ---------------------------------------------------------------- extend
+// Steps a lane of the traversal stages runs between refills of the warp's idle lanes.
+#ifndef MJPBR_PTW_REFILL_STEPS
+#define MJPBR_PTW_REFILL_STEPS 32
+#endif
+
+// Closest hit of every live path, lanes refilled from the queue (refill.cuh); the pending
+// next-event terms of the path's last bounce are added first.
 template <bool kMesh>
 __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_constant__ MjpbrScene s,
                                                                  const __grid_constant__ PtWaveMap wm, int32_t cur, bool pending_nee) {
@@ -336,30 +345,40 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_co
   const Stack st = wave_stack(s, smem);
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const bool cull = s.settings.cull_backfaces != 0;
-  const int32_t count = (int32_t)min((int64_t)wm.counters[cur], wm.path_cap);
+  const int64_t items = min((int64_t)wm.counters[cur], wm.path_cap);
   int32_t err = 0;
-  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
-    const int32_t path = wm.queue[cur][i];
-    PathRec& r = wm.path[path];
-    if (pending_nee) apply_nee(wm, path, r);
-    const float4 o = r.o, d = r.d;
-    const int32_t sample = __float_as_int(r.emis.w);
-    const int32_t passes = __float_as_int(r.normal.w);
-    const bool camera_ray = (__float_as_int(r.base.w) & 1) != 0;
-    const int32_t pix_all = path / wm.nsample;
-    const int32_t w = wm.w0 + pix_all / wm.pixels;
-    const float* blk = world_block(s, w);
-    const Hit hit = trace_ray<kMesh>(s, st, blk, L, Ray{V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}}, o.w, cull, false, &err);
-    wm.hit[path] = pack_hit(hit);
-    if (camera_ray && passes == 0 && sample == 0) {
-      int32_t ww, smp;
-      Pixel p;
-      path_pixel(s, wm, path, &ww, &p, &smp);
-      const float dcam_z = r.beta.w;
-      write_geometry(s, w, p, hit, dcam_z);
-      if (hit.geom != -1) r.rad.w = hit.dist * -dcam_z;
-    }
-  }
+  ClosestQuery q;
+  const float* blk = nullptr;
+  int32_t path = -1;
+  refill_loop<MJPBR_PTW_REFILL_STEPS>(
+      items, reinterpret_cast<unsigned long long*>(wm.counters + 4), q,
+      [&](int64_t item, ClosestQuery& qq) {
+        path = wm.queue[cur][item];
+        PathRec& r = wm.path[path];
+        if (pending_nee) apply_nee(wm, path, r);
+        const float4 o = r.o, d = r.d;
+        blk = world_block(s, wm.w0 + (path / wm.nsample) / wm.pixels);
+        closest_begin(qq, st, Ray{V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}}, o.w, &err);
+        return true;
+      },
+      [&](ClosestQuery& qq) { return closest_step<kMesh>(qq, s, st, blk, L, cull, &err); },
+      [&](ClosestQuery& qq, int32_t) {
+        const Hit& hit = qq.h;
+        wm.hit[path] = pack_hit(hit);
+        PathRec& r = wm.path[path];
+        const int32_t sample = __float_as_int(r.emis.w);
+        const int32_t passes = __float_as_int(r.normal.w);
+        const bool camera_ray = (__float_as_int(r.base.w) & 1) != 0;
+        if (camera_ray && passes == 0 && sample == 0) {
+          int32_t ww, smp;
+          Pixel p;
+          path_pixel(s, wm, path, &ww, &p, &smp);
+          const float dcam_z = r.beta.w;
+          write_geometry(s, ww, p, hit, dcam_z);
+          if (hit.geom != -1) r.rad.w = hit.dist * -dcam_z;
+        }
+      },
+      &err);
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
@@ -420,6 +439,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_PTW_SHADE_CTAS) ptw_shade_kern
 }
 
 // ---------------------------------------------------------------- shadow rays
+// Any hit of every recorded shadow ray, lanes refilled from the queue (refill.cuh).
 template <bool kMesh>
 __global__ void __launch_bounds__(kThreads, 3) ptw_shadow_kernel(const __grid_constant__ MjpbrScene s,
                                                                  const __grid_constant__ PtWaveMap wm) {
@@ -427,17 +447,23 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_shadow_kernel(const __grid_co
   const Stack st = wave_stack(s, smem);
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const bool cull = s.settings.cull_backfaces != 0;
-  const int32_t count = (int32_t)min((int64_t)wm.counters[2], wm.shadow_cap);
+  const int64_t items = min((int64_t)wm.counters[2], wm.shadow_cap);
   int32_t err = 0;
-  for (int32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
-    const ShadowEntry e = wm.shadow[i];
-    const int32_t target = __float_as_int(e.d.w);
-    const int32_t path = target / wm.nslot;
-    const int32_t w = wm.w0 + (path / wm.nsample) / wm.pixels;
-    const Hit hit = trace_ray<kMesh>(s, st, world_block(s, w), L, Ray{V3{e.o.x, e.o.y, e.o.z}, V3{e.d.x, e.d.y, e.d.z}}, e.o.w, cull,
-                                     true, &err);
-    wm.vis[target] = hit.geom == -1 ? 1 : 0;
-  }
+  AnyQuery q;
+  const float* blk = nullptr;
+  int32_t target = -1;
+  refill_loop<MJPBR_PTW_REFILL_STEPS>(
+      items, reinterpret_cast<unsigned long long*>(wm.counters + 6), q,
+      [&](int64_t item, AnyQuery& qq) {
+        const ShadowEntry e = wm.shadow[item];
+        target = __float_as_int(e.d.w);
+        const int32_t path = target / wm.nslot;
+        blk = world_block(s, wm.w0 + (path / wm.nsample) / wm.pixels);
+        any_begin(qq, st, Ray{V3{e.o.x, e.o.y, e.o.z}, V3{e.d.x, e.d.y, e.d.z}}, e.o.w, &err);
+        return true;
+      },
+      [&](AnyQuery& qq) { return any_step<kMesh>(qq, s, st, blk, L, cull, &err); },
+      [&](AnyQuery&, int32_t res) { wm.vis[target] = res == kAnyClear ? 1 : 0; }, &err);
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
@@ -572,7 +598,8 @@ int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int3
       k_extend<<<g_extend, kThreads, stack, stream>>>(s, wm, cur, it > 0);
       if ((rc = check_launch("ptw_extend_kernel"))) return rc;
       cudaError_t e = cudaMemsetAsync(wm.counters + next, 0, sizeof(int32_t), stream);
-      if (e == cudaSuccess) e = cudaMemsetAsync(wm.counters + 2, 0, sizeof(int32_t), stream);
+      // shadow entries [2], the fetch counters of the next extend [4..5] and of the shadow stage [6..7]
+      if (e == cudaSuccess) e = cudaMemsetAsync(wm.counters + 2, 0, 6 * sizeof(int32_t), stream);
       if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path wavefront queue counters: %s", cudaGetErrorString(e));
       k_shade<<<g_shade, kThreads, 0, stream>>>(s, seed, wm, cur);
       if ((rc = check_launch("ptw_shade_kernel"))) return rc;
