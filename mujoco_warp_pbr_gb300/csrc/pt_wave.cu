@@ -27,11 +27,15 @@
 #include <climits>
 
 #include "abi_internal.h"
+#include <cooperative_groups.h>
+
 #include "pt_bounce.cuh"
 #include "refill.cuh"
 
 namespace mjpbr {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr int kThreads = 256;
 // Resident CTAs per SM the shade stage's register allocation targets.
@@ -39,15 +43,17 @@ constexpr int kThreads = 256;
 #define MJPBR_PTW_SHADE_CTAS 3
 #endif
 
+// A path between stages: 80 bytes every bounce reads and writes, then the first surface's denoiser
+// features (48 bytes), read and written only by the bounce that can set them (a camera ray's).
 struct __align__(16) PathRec {
-  float4 o;       // origin, max_dist
-  float4 d;       // direction, pdf_prev
-  float4 beta;    // throughput, dcam_z
-  float4 rad;     // radiance, first-hit depth (sample 0)
-  float4 albedo;  // first-surface albedo, depth (int bits)
-  float4 normal;  // first-surface normal, passes (int bits)
-  float4 emis;    // first-surface emission, sample (int bits)
-  float4 base;    // first-surface base colour, flags (int bits: 1 camera ray, 2 delta)
+  float4 o;     // origin, max_dist
+  float4 d;     // direction, pdf_prev
+  float4 beta;  // throughput, dcam_z
+  float4 rad;   // radiance, first-hit depth (sample 0)
+  int4 meta;    // depth, passes, sample, flags (1 camera ray, 2 delta)
+  float4 f0;    // first surface: albedo xyz, normal x
+  float4 f1;    // normal yz, emission xy
+  float4 f2;    // emission z, base colour xyz
 };
 
 struct __align__(16) HitRec {
@@ -81,7 +87,7 @@ struct PtWaveMap {
   int32_t geo_base[MJPBR_MAX_RENDER + 1];  // pixels of the cameras without RGB (prefix sums)
   PathRec* path;
   HitRec* hit;
-  float4* nee;             // (npath, 2 + 2 * nslot)
+  float4* nee;             // (npath, 1 + nslot): the bounce's throughput, then each slot's term and flag
   uint8_t* vis;            // (npath, nslot)
   int32_t* queue[2];
   ShadowEntry* shadow;
@@ -119,38 +125,56 @@ MJ_DEV uint32_t pixel_seed_of(const MjpbrScene& s, uint32_t seed, int32_t w, con
   return seed + (uint32_t)w * (uint32_t)s.total_rays + (uint32_t)(s.ray_adr[p.cam] + p.pixelid);
 }
 
-MJ_DEV void store_path(PathRec& r, const PathState& ps, float first_depth) {
+MJ_DEV void store_path_hot(PathRec& r, const PathState& ps, float first_depth) {
   r.o = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.max_dist);
   r.d = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.pdf_prev);
   r.beta = make_float4(ps.beta.x, ps.beta.y, ps.beta.z, ps.dcam_z);
   r.rad = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, first_depth);
-  r.albedo = make_float4(ps.albedo.x, ps.albedo.y, ps.albedo.z, __int_as_float(ps.depth));
-  r.normal = make_float4(ps.normal.x, ps.normal.y, ps.normal.z, __int_as_float(ps.passes));
-  r.emis = make_float4(ps.emission.x, ps.emission.y, ps.emission.z, __int_as_float(ps.sample));
-  r.base = make_float4(ps.base_color.x, ps.base_color.y, ps.base_color.z,
-                       __int_as_float((ps.camera_ray ? 1 : 0) | (ps.delta ? 2 : 0)));
+  r.meta = make_int4(ps.depth, ps.passes, ps.sample, (ps.camera_ray ? 1 : 0) | (ps.delta ? 2 : 0));
+}
+
+MJ_DEV void store_path_features(PathRec& r, const PathState& ps) {
+  r.f0 = make_float4(ps.albedo.x, ps.albedo.y, ps.albedo.z, ps.normal.x);
+  r.f1 = make_float4(ps.normal.y, ps.normal.z, ps.emission.x, ps.emission.y);
+  r.f2 = make_float4(ps.emission.z, ps.base_color.x, ps.base_color.y, ps.base_color.z);
+}
+
+MJ_DEV void store_path(PathRec& r, const PathState& ps, float first_depth) {
+  store_path_hot(r, ps, first_depth);
+  store_path_features(r, ps);
+}
+
+MJ_DEV PathState load_path_hot(const PathRec& r, float* first_depth) {
+  PathState ps;
+  const float4 o = r.o, d = r.d, beta = r.beta, rad = r.rad;
+  const int4 meta = r.meta;
+  ps.o = V3{o.x, o.y, o.z};
+  ps.max_dist = o.w;
+  ps.d = V3{d.x, d.y, d.z};
+  ps.pdf_prev = d.w;
+  ps.beta = V3{beta.x, beta.y, beta.z};
+  ps.dcam_z = beta.w;
+  ps.radiance = V3{rad.x, rad.y, rad.z};
+  *first_depth = rad.w;
+  ps.depth = meta.x;
+  ps.passes = meta.y;
+  ps.sample = meta.z;
+  ps.camera_ray = (meta.w & 1) != 0;
+  ps.delta = (meta.w & 2) != 0;
+  return ps;
+}
+
+MJ_DEV void load_path_features(const PathRec& r, PathState& ps) {
+  const float4 f0 = r.f0, f1 = r.f1, f2 = r.f2;
+  ps.albedo = V3{f0.x, f0.y, f0.z};
+  ps.normal = V3{f0.w, f1.x, f1.y};
+  ps.emission = V3{f1.z, f1.w, f2.x};
+  ps.base_color = V3{f2.y, f2.z, f2.w};
 }
 
 MJ_DEV PathState load_path(const PathRec& r, float* first_depth) {
-  PathState ps;
-  ps.o = V3{r.o.x, r.o.y, r.o.z};
-  ps.max_dist = r.o.w;
-  ps.d = V3{r.d.x, r.d.y, r.d.z};
-  ps.pdf_prev = r.d.w;
-  ps.beta = V3{r.beta.x, r.beta.y, r.beta.z};
-  ps.dcam_z = r.beta.w;
-  ps.radiance = V3{r.rad.x, r.rad.y, r.rad.z};
-  *first_depth = r.rad.w;
-  ps.albedo = V3{r.albedo.x, r.albedo.y, r.albedo.z};
-  ps.depth = __float_as_int(r.albedo.w);
-  ps.normal = V3{r.normal.x, r.normal.y, r.normal.z};
-  ps.passes = __float_as_int(r.normal.w);
-  ps.emission = V3{r.emis.x, r.emis.y, r.emis.z};
-  ps.sample = __float_as_int(r.emis.w);
-  ps.base_color = V3{r.base.x, r.base.y, r.base.z};
-  const int32_t flags = __float_as_int(r.base.w);
-  ps.camera_ray = (flags & 1) != 0;
-  ps.delta = (flags & 2) != 0;
+  PathState ps = load_path_hot(r, first_depth);
+  load_path_features(r, ps);
   return ps;
 }
 
@@ -217,30 +241,48 @@ MJ_DEV int64_t cta_append(bool want, int32_t* counter, int64_t cap, int32_t* sca
   return pos;
 }
 
-// Next-event estimation of the wavefront: the terms are recorded in the path's record; the
-// shadow rays are traced by the shadow stage and the terms added by the nee stage.
+// Next-event estimation of the wavefront: each slot's term is recorded in the path's record and
+// its shadow ray appended to the shadow queue at once (one atomic per group of converged lanes);
+// the shadow stage traces the rays and the next extend (or resolve) adds the terms.
 struct RecordedNee {
-  float4* rec;  // [0] beta, active; [1] origin; per slot [2 + 2k] contribution, flag; [3 + 2k] ray direction, length
-  int32_t nslot;
-  MJ_DEV void begin(const PathState& ps, V3 origin) {
+  float4* rec;  // [0] beta, active; [1 + k] slot k's contribution, flag
+  int32_t nslot, path;
+  V3 origin;
+  const PtWaveMap* wm;
+  int32_t* err;
+  MJ_DEV void begin(const PathState& ps, V3 o) {
     rec[0] = make_float4(ps.beta.x, ps.beta.y, ps.beta.z, __int_as_float(0));
-    rec[1] = make_float4(origin.x, origin.y, origin.z, 0.0f);
-    for (int32_t k = 0; k < nslot; ++k) rec[2 + 2 * k].w = __int_as_float(kNeeSkip);
+    origin = o;
+    for (int32_t k = 0; k < nslot; ++k) rec[1 + k].w = __int_as_float(kNeeSkip);
   }
-  MJ_DEV void none(int32_t slot) { rec[2 + 2 * slot].w = __int_as_float(kNeeZero); }
+  MJ_DEV void shadow_ray(int32_t slot, V3 dir, float len) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(wm->counters + 2, (int32_t)g.size());
+    const int64_t pos = (int64_t)g.shfl(base, 0) + g.thread_rank();
+    if (pos >= wm->shadow_cap) {
+      *err |= kErrWorkQueue;
+      return;
+    }
+    ShadowEntry e;
+    e.o = make_float4(origin.x, origin.y, origin.z, len);
+    e.d = make_float4(dir.x, dir.y, dir.z, __int_as_float(path * nslot + slot));
+    wm->shadow[pos] = e;
+  }
+  MJ_DEV void none(int32_t slot) { rec[1 + slot].w = __int_as_float(kNeeZero); }
   template <class F>
   MJ_DEV void light(RtCtx&, int32_t slot, bool shadowed, V3, V3 dir, float max_t, F contribution) {
     const V3 c = contribution();
-    rec[2 + 2 * slot] = make_float4(c.x, c.y, c.z, __int_as_float(shadowed ? kNeeIfVisible : kNeeAdd));
-    rec[3 + 2 * slot] = make_float4(dir.x, dir.y, dir.z, max_t);
+    rec[1 + slot] = make_float4(c.x, c.y, c.z, __int_as_float(shadowed ? kNeeIfVisible : kNeeAdd));
+    if (shadowed) shadow_ray(slot, dir, max_t);
   }
   MJ_DEV void lights_done(PathState&) { rec[0].w = __int_as_float(1); }
   template <class F>
   MJ_DEV void env(RtCtx&, PathState&, V3, V3 dir, F term) {
     const int32_t slot = nslot - 1;
     const V3 t = term();
-    rec[2 + 2 * slot] = make_float4(t.x, t.y, t.z, __int_as_float(kNeeIfVisible));
-    rec[3 + 2 * slot] = make_float4(dir.x, dir.y, dir.z, kUnboundedShadow);
+    rec[1 + slot] = make_float4(t.x, t.y, t.z, __int_as_float(kNeeIfVisible));
+    shadow_ray(slot, dir, kUnboundedShadow);
   }
 };
 
@@ -251,14 +293,14 @@ struct RecordedNee {
 // stage before the path's next hit, and by the resolve stage for the paths that ended: the same
 // additions in the same order as the persistent kernel.
 MJ_DEV void apply_nee(const PtWaveMap& wm, int32_t path, PathRec& r) {
-  float4* rec = wm.nee + (int64_t)path * (2 + 2 * wm.nslot);
+  float4* rec = wm.nee + (int64_t)path * (1 + wm.nslot);
   const float4 head = rec[0];
   if (__float_as_int(head.w) == 0) return;
   const int32_t nlights = wm.nslot - 1;  // the model's lights and the headlight
   const uint8_t* vis = wm.vis + (int64_t)path * wm.nslot;
   V3 direct = v3(0.0f);
   for (int32_t k = 0; k < nlights; ++k) {
-    const float4 c = rec[2 + 2 * k];
+    const float4 c = rec[1 + k];
     const int32_t flag = __float_as_int(c.w);
     if (flag == kNeeSkip) continue;
     const bool add = flag == kNeeAdd || (flag == kNeeIfVisible && vis[k]);
@@ -266,7 +308,7 @@ MJ_DEV void apply_nee(const PtWaveMap& wm, int32_t path, PathRec& r) {
   }
   V3 radiance{r.rad.x, r.rad.y, r.rad.z};
   radiance += cmul(V3{head.x, head.y, head.z}, direct);
-  const float4 e = rec[2 + 2 * nlights];
+  const float4 e = rec[1 + nlights];
   if (__float_as_int(e.w) == kNeeIfVisible && vis[nlights]) radiance += V3{e.x, e.y, e.z};
   r.rad = make_float4(radiance.x, radiance.y, radiance.z, r.rad.w);
   rec[0].w = __int_as_float(0);
@@ -366,9 +408,10 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_co
         const Hit& hit = qq.h;
         wm.hit[path] = pack_hit(hit);
         PathRec& r = wm.path[path];
-        const int32_t sample = __float_as_int(r.emis.w);
-        const int32_t passes = __float_as_int(r.normal.w);
-        const bool camera_ray = (__float_as_int(r.base.w) & 1) != 0;
+        const int4 meta = r.meta;
+        const int32_t sample = meta.z;
+        const int32_t passes = meta.y;
+        const bool camera_ray = (meta.w & 1) != 0;
         if (camera_ray && passes == 0 && sample == 0) {
           int32_t ww, smp;
           Pixel p;
@@ -397,7 +440,6 @@ __global__ void __launch_bounds__(kThreads, MJPBR_PTW_SHADE_CTAS) ptw_shade_kern
     const int32_t i = round * stride + blockIdx.x * kThreads + threadIdx.x;
     int32_t path = -1;
     bool live = false;
-    float4* rec = nullptr;
     if (i < count) {
       path = wm.queue[cur][i];
       int32_t w, sample;
@@ -409,29 +451,22 @@ __global__ void __launch_bounds__(kThreads, MJPBR_PTW_SHADE_CTAS) ptw_shade_kern
       p.rec = blk + L.cam_off + p.cam * kCamFloats;
       const M3 R = cam_mat(p.rec);
       const V3 head_dir = -V3{R.m[2], R.m[5], R.m[8]};
+      PathRec& r = wm.path[path];
       float first_depth;
-      PathState ps = load_path(wm.path[path], &first_depth);
+      PathState ps = load_path_hot(r, &first_depth);
+      // only a camera ray's bounce can set the first surface's features
+      const bool features = ps.camera_ray;
+      if (features) load_path_features(r, ps);
       const Hit hit = unpack_hit(wm.hit[path], blk, L);
-      rec = wm.nee + (int64_t)path * (2 + 2 * wm.nslot);
+      float4* rec = wm.nee + (int64_t)path * (1 + wm.nslot);
       rec[0].w = __int_as_float(0);
-      RecordedNee nee{rec, wm.nslot};
+      RecordedNee nee{rec, wm.nslot, path, v3(0.0f), &wm, &err};
       live = !PtCore<kMesh, kTex>::surface(c, nee, ps, hit, pixel_seed_of(s, seed, w, p), head_dir);
-      store_path(wm.path[path], ps, first_depth);
+      store_path_hot(r, ps, first_depth);
+      if (features) store_path_features(r, ps);
       err |= c.err;
     }
-    // the shadow rays of the recorded next-event terms, then the paths that continue
-    const bool active = rec && __float_as_int(rec[0].w) != 0;
-    for (int32_t k = 0; k < wm.nslot; ++k) {
-      const bool want = active && __float_as_int(rec[2 + 2 * k].w) == kNeeIfVisible;
-      const int64_t pos = cta_append(want, wm.counters + 2, wm.shadow_cap, scan, &err);
-      if (pos >= 0) {
-        const float4 o = rec[1], d = rec[3 + 2 * k];
-        ShadowEntry e;
-        e.o = make_float4(o.x, o.y, o.z, d.w);
-        e.d = make_float4(d.x, d.y, d.z, __int_as_float(path * wm.nslot + k));
-        wm.shadow[pos] = e;
-      }
-    }
+    // the paths that continue
     const int64_t pos = cta_append(live, wm.counters + next, wm.path_cap, scan, &err);
     if (pos >= 0) wm.queue[next][pos] = path;
   }
@@ -521,7 +556,7 @@ int64_t layout(PtWaveMap* wm, char* base, int64_t npath, int32_t nslot) {
   char* counters = take(256);
   char* path = take(npath * (int64_t)sizeof(PathRec));
   char* hit = take(npath * (int64_t)sizeof(HitRec));
-  char* nee = take(npath * (2 + 2 * (int64_t)nslot) * 16);
+  char* nee = take(npath * (1 + (int64_t)nslot) * 16);
   char* vis = take(npath * nslot);
   char* q0 = take(npath * 4);
   char* q1 = take(npath * 4);
