@@ -38,7 +38,7 @@ class LaunchShape:
   schedule: int  # GRID, QUEUE or WAVEFRONT
   render_order: int  # grid tile shape: ROW (32 x 8) or TILED (16 x 16)
   queue_item: int  # queue work item, pixels
-  wave_chunk_worlds: int = 0  # wavefront: worlds per chunk (0: about 16 M samples)
+  wave_chunk_worlds: int = 0  # wavefront: worlds per chunk (0: about 64 M camera samples / 32 M paths)
 
   def describe(self) -> str:
     if self.schedule == GRID:

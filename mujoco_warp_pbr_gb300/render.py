@@ -274,9 +274,10 @@ def scene(m: Any, d: Any, rc: PbrRenderContext) -> _lib.Scene:
 
 
 # camera samples (real-time tier) or paths (path tier) per chunk of the wavefront schedules when
-# wave_chunk_worlds is 0
-WAVE_CHUNK_SAMPLES = 1 << 24
-WAVE_CHUNK_PATHS = 1 << 23
+# wave_chunk_worlds is 0: queues of about 21 GB (mesh / IBL scene, two lights) and 13 GB (path
+# scene), a few per cent faster than chunks of a quarter of that (fewer launches and launch tails)
+WAVE_CHUNK_SAMPLES = 1 << 26
+WAVE_CHUNK_PATHS = 1 << 25
 
 
 def _ensure_wave_scratch(rc: PbrRenderContext, struct: _lib.Scene) -> bool:
