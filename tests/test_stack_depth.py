@@ -98,3 +98,32 @@ def test_stack_depth_reaches_the_settings():
   want = context.traversal_stack_depth(levels, hc.meshes["mesh_levels"])
   assert hc.settings["stack_depth"] == want
   assert hc.meshes["mesh_levels"] >= 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", ["grid", "wavefront"])
+def test_a_stack_too_shallow_for_the_scene_is_reported(schedule):
+  """Rendering the mesh scene with fewer stack entries than its BVHs need: every push past the
+  stack's end is dropped (never written) and reported in the error word; with the computed depth
+  the same frame reports nothing."""
+  import ctypes
+
+  torch = pytest.importorskip("torch")
+  if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU")
+  import mujoco_warp_pbr_gb300 as mjpbr
+  from mujoco_warp_pbr_gb300 import synthetic
+  from tests import helpers
+
+  sc = synthetic.mesh_ibl_scene(seed=2, nworld=2, res=48, tex_size=64, env_width=128)
+  m, d, rc = helpers.gpu_scene(sc, schedule=schedule)
+  mjpbr.refit_bvh(m, d, rc)
+  mjpbr.render(m, d, rc, seed=1)
+  assert mjpbr.check_errors(rc) == 0
+  s = _lib.Scene.from_buffer_copy(mjpbr.scene_descriptor(m, d, rc))
+  assert s.settings.stack_depth > 8
+  s.settings.stack_depth = 8
+  stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+  lib = _lib.load()
+  assert lib.mjpbr_render(ctypes.byref(s), 1, stream) == 0, lib.mjpbr_last_error().decode()
+  assert mjpbr.check_errors(rc) & 1, "no stack overflow reported"
