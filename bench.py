@@ -360,6 +360,53 @@ def _config(args, sc) -> dict:
   return cfg
 
 
+class ImageCopier:
+  """get_rgb's float images (nworld, H, W, 3) of the given cameras copied to pinned host memory
+  after each step. Frames above 64 MB of images are double-buffered: step i's copy runs on a second
+  stream while step i + 1 renders (the render stream waits for a buffer's previous copy before
+  get_rgb rewrites it); smaller frames copy on the render stream."""
+
+  def __init__(self, torch, mjpbr, rc, cams, shapes, dev, stream):
+    self.torch, self.mjpbr, self.rc, self.cams, self.stream = torch, mjpbr, rc, cams, stream
+    self.d2h = sum(4 * n * h * w * 3 for n, h, w, _ in shapes)
+    self.overlap = self.d2h > (64 << 20)
+    nbuf = 2 if self.overlap else 1
+    self.dev = [[torch.empty(sh, dtype=torch.float32, device=dev) for sh in shapes] for _ in range(nbuf)]
+    self.host = [[torch.empty(sh, dtype=torch.float32).pin_memory() for sh in shapes] for _ in range(nbuf)]
+    self.copy_stream = torch.cuda.Stream(dev) if self.overlap else stream
+    self.copied = [torch.cuda.Event() for _ in range(nbuf)]
+    for ev in self.copied:
+      ev.record(self.copy_stream)
+    self.i = 0
+
+  def after_step(self) -> None:
+    torch, slot = self.torch, self.i % len(self.dev)
+    self.i += 1
+    if self.overlap:
+      self.stream.wait_event(self.copied[slot])
+    for cam, td in zip(self.cams, self.dev[slot], strict=True):
+      self.mjpbr.get_rgb(self.rc, cam, td)
+    if not self.overlap:
+      for td, th in zip(self.dev[slot], self.host[slot], strict=True):
+        th.copy_(td, non_blocking=True)
+      return
+    ready = torch.cuda.Event()
+    ready.record(self.stream)
+    self.copy_stream.wait_event(ready)
+    with torch.cuda.stream(self.copy_stream):
+      for td, th in zip(self.dev[slot], self.host[slot], strict=True):
+        th.copy_(td, non_blocking=True)
+      self.copied[slot].record(self.copy_stream)
+
+  def finish(self) -> None:
+    """The render stream waits for the last copy (call before recording the end event)."""
+    if self.overlap:
+      self.stream.wait_stream(self.copy_stream)
+
+  def describe(self) -> str:
+    return "get_rgb float32 (nworld, H, W, 3) per RGB camera" + (", double-buffered: step i's copy overlaps step i + 1" if self.overlap else "")
+
+
 def run(args) -> None:
   import torch
   import torch.distributed as dist
@@ -455,43 +502,18 @@ def run(args) -> None:
   assert mjpbr.check_errors(rc) == 0
 
   # ---- end to end through the public API with host buffers: poses in from pinned memory,
-  # refit + render, get_rgb's float image (the reference's output format) back to pinned memory.
-  # Frames with more than 64 MB of images are double-buffered: step i's copy to the host runs on a
-  # second stream while step i + 1 renders; the timed region ends when the last copy has landed.
-  # Smaller frames copy on the render stream (the second stream's events cost more than they hide).
+  # refit + render, get_rgb's float image (the reference's output format) back to pinned memory
   host = {name: getattr(d, name).cpu().pin_memory() for name in ("geom_xpos", "geom_xmat", "cam_xpos", "cam_xmat", "light_xpos", "light_xdir")}
   shapes = [(sc.nworld, h, w, 3) for (w, h), on in zip(rc.base.cam_res, rc.base.render_rgb) if on]
-  rgb_dev = [[torch.empty(sh, dtype=torch.float32, device=dev) for sh in shapes] for _ in range(2)]
-  rgb_host = [[torch.empty(sh, dtype=torch.float32).pin_memory() for sh in shapes] for _ in range(2)]
-  rgb_cams = [c for c, on in enumerate(rc.base.render_rgb) if on]
+  copier = ImageCopier(torch, mjpbr, rc, [c for c, on in enumerate(rc.base.render_rgb) if on], shapes, dev, stream)
   h2d = sum(t.numel() * t.element_size() for t in host.values())
-  d2h = sum(t.numel() * t.element_size() for t in rgb_host[0])
-  overlap = d2h > (64 << 20)
-  copy_stream = torch.cuda.Stream(dev) if overlap else stream
-  copied = [torch.cuda.Event() for _ in range(2)]
-  for ev in copied:
-    ev.record(copy_stream)
+  d2h = copier.d2h
 
   def e2e_step(i: int, seed: int) -> None:
-    slot = i % 2
     for name, t in host.items():
       getattr(d, name).copy_(t, non_blocking=True)
     step(seed)
-    if overlap:
-      stream.wait_event(copied[slot])  # the previous copy out of this slot's buffers has finished
-    for cam, td in zip(rgb_cams, rgb_dev[slot], strict=True):
-      mjpbr.get_rgb(rc, cam, td)
-    if not overlap:
-      for td, th in zip(rgb_dev[slot], rgb_host[slot], strict=True):
-        th.copy_(td, non_blocking=True)
-      return
-    ready = torch.cuda.Event()
-    ready.record(stream)
-    copy_stream.wait_event(ready)
-    with torch.cuda.stream(copy_stream):
-      for td, th in zip(rgb_dev[slot], rgb_host[slot], strict=True):
-        th.copy_(td, non_blocking=True)
-      copied[slot].record(copy_stream)
+    copier.after_step()
 
   e2e_steps = max(3, args.steps // 2)
   for i in range(2):
@@ -504,8 +526,7 @@ def run(args) -> None:
   e0.record(stream)
   for i in range(e2e_steps):
     e2e_step(i, 2000 + i)
-  if overlap:
-    stream.wait_stream(copy_stream)
+  copier.finish()
   e1.record(stream)
   torch.cuda.synchronize()
   e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
@@ -540,7 +561,7 @@ def run(args) -> None:
       "data": "synthetic (seeded scenes; no dataset)",
       "config": _config(args, sc),
       "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-              "output": "get_rgb float32 (nworld, H, W, 3) per RGB camera" + (", double-buffered: step i's copy overlaps step i + 1" if overlap else "")},
+              "output": copier.describe()},
       "roofline": {
         "bound": "hbm",
         "kernel": kernel,
@@ -692,15 +713,19 @@ def measure_large(args, dev, nworld: int, steps: int, warmup: int, cpu_budget: f
   ms = e0.elapsed_time(e1) / steps
   # end to end: poses from pinned host memory, the graph, get_rgb's float image back to the host
   host_poses = poses.cpu().pin_memory()
-  rgb_dev = [torch.empty((sc.nworld, h, w, 3), dtype=torch.float32, device=dev) for w, h in rc.base.cam_res]
-  rgb_host = [torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in rgb_dev]
+  copier = ImageCopier(torch, mjpbr, rc, list(range(len(rc.base.cam_res))), [(sc.nworld, h, w, 3) for w, h in rc.base.cam_res], dev, stream)
+  for _ in range(2):
+    poses.copy_(host_poses, non_blocking=True)
+    graph.replay()
+    copier.after_step()
+  copier.finish()
+  torch.cuda.synchronize()
   e0.record(stream)
   for _ in range(steps):
     poses.copy_(host_poses, non_blocking=True)
     graph.replay()
-    for cam, (td, th) in enumerate(zip(rgb_dev, rgb_host, strict=True)):
-      mjpbr.get_rgb(rc, cam, td)
-      th.copy_(td, non_blocking=True)
+    copier.after_step()
+  copier.finish()
   e1.record(stream)
   torch.cuda.synchronize()
   e2e_ms = e0.elapsed_time(e1) / steps
@@ -718,7 +743,7 @@ def measure_large(args, dev, nworld: int, steps: int, warmup: int, cpu_budget: f
                "rr_depth": 2, "envs": 4, "denoiser": "learned (KPCN, BF16)", "chunk_worlds": args.chunk, "graph": "one CUDA graph per frame",
                "l2": "frame working set far above L2"},
     "e2e": {"value": npix / e2e_ms / 1e3, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4),
-            "d2h_bytes_per_step": int(sum(t.numel() * 4 for t in rgb_host)), "output": "get_rgb float32 (nworld, H, W, 3) per camera"},
+            "d2h_bytes_per_step": int(copier.d2h), "output": copier.describe()},
     "roofline": {
       "bound": "hbm",
       "kernel": "whole frame graph (path tracer, network, finish pass)",
@@ -797,17 +822,21 @@ def measure_batched(args, dev, nworld: int, steps: int, warmup: int, cpu_budget:
   value = aggregate_rate(npix * steps, total_ms, world_size)
   # end to end: next poses from pinned host memory, the graph, get_rgb's float images back
   host_poses = poses.cpu().pin_memory()
-  rgb_dev = [torch.empty((sc.nworld, h, w, 3), dtype=torch.float32, device=dev) for w, h in rc.base.cam_res]
-  rgb_host = [torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in rgb_dev]
+  copier = ImageCopier(torch, mjpbr, rc, list(range(len(rc.base.cam_res))), [(sc.nworld, h, w, 3) for w, h in rc.base.cam_res], dev, stream)
+  for _ in range(2):
+    poses.copy_(host_poses, non_blocking=True)
+    graph.replay()
+    copier.after_step()
+  copier.finish()
+  torch.cuda.synchronize()
   e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
   e2e_steps = max(3, steps // 2)
   e0.record(stream)
   for _ in range(e2e_steps):
     poses.copy_(host_poses, non_blocking=True)
     graph.replay()
-    for cam, (td, th) in enumerate(zip(rgb_dev, rgb_host, strict=True)):
-      mjpbr.get_rgb(rc, cam, td)
-      th.copy_(td, non_blocking=True)
+    copier.after_step()
+  copier.finish()
   e1.record(stream)
   torch.cuda.synchronize()
   e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
@@ -829,7 +858,7 @@ def measure_batched(args, dev, nworld: int, steps: int, warmup: int, cpu_budget:
     "ms_per_step": avg,
     "config": cfg,
     "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_poses.numel() * 4),
-            "d2h_bytes_per_step": int(sum(t.numel() * 4 for t in rgb_host)), "output": "get_rgb float32 (nworld, H, W, 3) per camera"},
+            "d2h_bytes_per_step": int(copier.d2h), "output": copier.describe()},
     "roofline": {
       "bound": "hbm",
       "kernel": f"render ({tuned['best']}), whole graph timed",
