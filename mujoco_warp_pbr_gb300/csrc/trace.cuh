@@ -440,45 +440,8 @@ MJ_DEV void closest_offer(ClosestQuery& q, const float* g, int32_t slot, float d
 template <bool kMesh>
 MJ_DEV int32_t closest_step(ClosestQuery& q, const MjpbrScene& sc, const Stack& st, const float* blk, const BlockLayout& L, bool cull,
                             int32_t* err) {
-  if (kMesh && q.m_slot >= 0) {
-    if (q.sp > q.m_base) {  // one step of the mesh traversal
-      --q.sp;
-      if (st.t[q.sp * st.stride] >= q.m_best) return kAnyRunning;
-      const int32_t code = st.code[q.sp * st.stride];
-      const int32_t ref = code >> 3, cnt = code & 7;
-      if (cnt == 0) {
-        const float* nd = q.m_nodes + (int64_t)ref * kNodeFloats;
-        expand(st, q.sp, q.m_ri, ldg4(nd), ldg4(nd + 4), ldg4(nd + 8), ldg4(nd + 12), q.m_best, err);
-        return kAnyRunning;
-      }
-      for (int32_t i = ref; i < ref + cnt; ++i) {
-        const float* tr = q.m_tris + (int64_t)i * kTriFloats;
-        const float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
-        const V3 v0{a.x, a.y, a.z}, v1{b.x, b.y, b.z}, v2{c.x, c.y, c.z};
-        float tu, tv;
-        MJPBR_COUNT(kOpTri);
-        const float t = woop_hit(q.m_w, v0, v1, v2, q.m_best, &tu, &tv);
-        if (t < 0.0f) continue;
-        const V3 ng = cross(v1 - v0, v2 - v0);
-        if (cull && dot(q.m_ld, ng) > 0.0f) continue;
-        q.m_best = t;
-        q.m_face = __float_as_int(a.w);
-        q.m_n = ng;
-        q.m_u = tu;
-        q.m_v = tv;
-      }
-      return kAnyRunning;
-    }
-    // the mesh is done: its hit goes through the same selection as a primitive's
-    const int32_t slot = q.m_slot;
-    q.m_slot = -1;
-    const float* g = blk + L.geom_off + slot * kGeomFloats;
-    if (q.m_face >= 0) {
-      closest_offer(q, g, slot, q.m_best, mul(geom_frame(g).mat, normalize(q.m_n)), q.m_u, q.m_v, q.m_face, q.m_bvh, cull);
-    }
-    return kAnyRunning;
-  }
-  if (q.leaf < q.leaf_end) {  // the next geom of the scene leaf
+  const bool in_mesh = kMesh && q.m_slot >= 0;
+  if (!in_mesh && q.leaf < q.leaf_end) {  // the next geom of the scene leaf
     const int32_t slot = q.leaf++;
     const float* g = blk + L.geom_off + slot * kGeomFloats;
     if (__float_as_int(g[19]) & kGeomFlagSkip) return kAnyRunning;
@@ -505,19 +468,52 @@ MJ_DEV int32_t closest_step(ClosestQuery& q, const MjpbrScene& sc, const Stack& 
     closest_offer(q, g, slot, d, n, 0.0f, 0.0f, -1, -1, cull);
     return kAnyRunning;
   }
-  if (q.sp == 0) return kAnyClear;
+  if (in_mesh && q.sp == q.m_base) {  // the mesh is done: its hit goes through the primitives' selection
+    const int32_t slot = q.m_slot;
+    q.m_slot = -1;
+    const float* g = blk + L.geom_off + slot * kGeomFloats;
+    if (q.m_face >= 0) {
+      closest_offer(q, g, slot, q.m_best, mul(geom_frame(g).mat, normalize(q.m_n)), q.m_u, q.m_v, q.m_face, q.m_bvh, cull);
+    }
+    return kAnyRunning;
+  }
+  if (!in_mesh && q.sp == 0) return kAnyClear;
+  // one entry of the current level's stack; scene and mesh nodes share the child-bounds layout,
+  // so lanes at either level expand their node with the same instructions
   --q.sp;
-  const float cut = q.h.dist * (1.0f + kRayTolRel) + kRayTolAbs;
+  const float cut = in_mesh ? q.m_best : q.h.dist * (1.0f + kRayTolRel) + kRayTolAbs;
   if (st.t[q.sp * st.stride] >= cut) return kAnyRunning;
   const int32_t code = st.code[q.sp * st.stride];
   const int32_t ref = code >> 3, cnt = code & 7;
   if (cnt == 0) {
-    const float4* nd = reinterpret_cast<const float4*>(blk + L.node_off + ref * kNodeFloats);
-    expand(st, q.sp, q.ri, nd[0], nd[1], nd[2], nd[3], cut, err);
-  } else {
-    q.leaf = ref;
-    q.leaf_end = ref + cnt;
+    const float4* nd = reinterpret_cast<const float4*>(in_mesh ? q.m_nodes + (int64_t)ref * kNodeFloats : blk + L.node_off + ref * kNodeFloats);
+    RayInv ri;  // component copies: a selected reference would put the query in local memory
+    ri.inv = in_mesh ? q.m_ri.inv : q.ri.inv;
+    ri.oinv = in_mesh ? q.m_ri.oinv : q.ri.oinv;
+    expand(st, q.sp, ri, nd[0], nd[1], nd[2], nd[3], cut, err);
+    return kAnyRunning;
   }
+  if (in_mesh) {
+    for (int32_t i = ref; i < ref + cnt; ++i) {
+      const float* tr = q.m_tris + (int64_t)i * kTriFloats;
+      const float4 a = ldg4(tr), b = ldg4(tr + 4), c = ldg4(tr + 8);
+      const V3 v0{a.x, a.y, a.z}, v1{b.x, b.y, b.z}, v2{c.x, c.y, c.z};
+      float tu, tv;
+      MJPBR_COUNT(kOpTri);
+      const float t = woop_hit(q.m_w, v0, v1, v2, q.m_best, &tu, &tv);
+      if (t < 0.0f) continue;
+      const V3 ng = cross(v1 - v0, v2 - v0);
+      if (cull && dot(q.m_ld, ng) > 0.0f) continue;
+      q.m_best = t;
+      q.m_face = __float_as_int(a.w);
+      q.m_n = ng;
+      q.m_u = tu;
+      q.m_v = tv;
+    }
+    return kAnyRunning;
+  }
+  q.leaf = ref;
+  q.leaf_end = ref + cnt;
   return kAnyRunning;
 }
 
