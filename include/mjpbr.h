@@ -26,9 +26,6 @@
  *   mjpbr_build_mips       mip chains of texture.upload_textures / EnvironmentMap
  *                                                                         (mujoco_warp_pbr/_src/texture.py:63-101,
  *                                                                          mujoco_warp_pbr/_src/envmap.py:330-340)
- *   mjpbr_tiled_texture, mjpbr_tile_texture
- *                          none: the tiled copy of the uploaded textures the kernels sample
- *                          (mujoco_warp_pbr/_src/texture.py:63-101 uploads row-major Warp textures)
  *   mjpbr_prefilter_env    envmap._prefilter                              (mujoco_warp_pbr/_src/envmap.py:171-221)
  *   mjpbr_env_sh9          envmap._sh9_irradiance                         (mujoco_warp_pbr/_src/envmap.py:224-249)
  *   mjpbr_env_sampling_tables  envmap.sampling_distribution               (mujoco_warp_pbr/_src/envmap.py:409-430)
@@ -93,10 +90,6 @@ enum MjpbrRenderOrder { MJPBR_ORDER_ROW = 0, MJPBR_ORDER_TILED = 1, MJPBR_ORDER_
 enum MjpbrSchedule { MJPBR_SCHEDULE_GRID = 0, MJPBR_SCHEDULE_QUEUE = 1, MJPBR_SCHEDULE_WAVEFRONT = 2 };
 /* Texel formats of MjpbrTexture. */
 enum MjpbrTexFormat { MJPBR_TEX_RGBA8 = 0, MJPBR_TEX_RGBA16F = 1 };
-/* Texel order of a texture's levels: rows, or 4 x 4-texel tiles (tiles row by row, texels of a tile
- * row by row; levels padded to whole tiles), so that a bilinear 2 x 2 footprint mostly lies in one
- * 64- or 128-byte tile. */
-enum MjpbrTexLayout { MJPBR_TEX_ROWS = 0, MJPBR_TEX_TILED = 1 };
 
 /* A batched table: nbatch rows (1 or nworld), row r used by worlds with worldid % nbatch == r. */
 typedef struct mjpbr_f32b { const float* ptr; int32_t nbatch; int32_t pad_; } mjpbr_f32b;
@@ -140,15 +133,14 @@ typedef struct MjpbrConvGrad {
   int32_t in2_full;      /* 1: in2 has the output resolution; 0: half of it, upsampled x2 */
 } MjpbrConvGrad;
 
-/* One mipmapped 2D texture inside MjpbrScene.tex_data (RGBA). */
+/* One mipmapped 2D texture inside MjpbrScene.tex_data (RGBA, row-major levels). */
 typedef struct MjpbrTexture {
   int32_t format;   /* MjpbrTexFormat */
   int32_t width;    /* level 0 */
   int32_t height;
   int32_t nlevel;
   int64_t level_offset[MJPBR_MAX_MIPS]; /* byte offset of each level in tex_data */
-  int32_t layout;   /* MjpbrTexLayout */
-  int32_t pad_;
+  int32_t pad_[2];
 } MjpbrTexture;
 
 /* Render settings (mujoco_warp_pbr/_src/kernel_inputs.py:47-116 plus the path-tier and denoiser
@@ -493,15 +485,6 @@ int mjpbr_dfg_lut(float* lut, int32_t size, int32_t nsample, void* stream);
  * (2x2 average per level, odd sizes truncate). The mip chains of texture uploads and environment
  * maps, mujoco_warp_pbr/_src/texture.py:91-99 and mujoco_warp_pbr/_src/envmap.py:330-337. */
 int mjpbr_build_mips(const MjpbrTexture* tex, uint8_t* data, void* stream);
-
-/* Host: the description of the tiled copy (MJPBR_TEX_TILED) of a row-major texture, its levels
- * placed from byte `offset` on (128-byte aligned); returns the byte offset past its last level, or
- * -1 for a bad description. No counterpart in the reference (a GB300 memory layout). */
-int64_t mjpbr_tiled_texture(const MjpbrTexture* rows, int64_t offset, MjpbrTexture* tiled);
-
-/* Copies every level of a row-major texture (rows, src) into its tiled layout (tiled, dst, from
- * mjpbr_tiled_texture), on the stream; tile texels outside the level are zero. */
-int mjpbr_tile_texture(const MjpbrTexture* rows, const uint8_t* src, const MjpbrTexture* tiled, uint8_t* dst, void* stream);
 
 /* GGX-prefiltered stack (levels, height, width, 4) float16 of one environment map (radiance: host
  * description of a RGBA16F mipmapped texture in device bytes data), nsample importance samples per texel with filtered importance

@@ -49,8 +49,7 @@ class Texture(ctypes.Structure):
     ("height", c_i32),
     ("nlevel", c_i32),
     ("level_offset", ctypes.c_int64 * MAX_MIPS),
-    ("layout", c_i32),
-    ("pad_", c_i32),
+    ("pad_", c_i32 * 2),
   ]
 
 
@@ -334,8 +333,6 @@ _SIGNATURES = {
   "mjpbr_get_image": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_i32, c_vp, c_i32, c_vp]),
   "mjpbr_dfg_lut": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp]),
   "mjpbr_build_mips": (ctypes.c_int, [ctypes.POINTER(Texture), c_vp, c_vp]),
-  "mjpbr_tiled_texture": (ctypes.c_int64, [ctypes.POINTER(Texture), ctypes.c_int64, ctypes.POINTER(Texture)]),
-  "mjpbr_tile_texture": (ctypes.c_int, [ctypes.POINTER(Texture), c_vp, ctypes.POINTER(Texture), c_vp, c_vp]),
   "mjpbr_prefilter_env": (ctypes.c_int, [ctypes.POINTER(Texture), c_vp, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp]),
   "mjpbr_denoise_atrous": (ctypes.c_int, [ctypes.POINTER(Scene), c_vp]),
   "mjpbr_bvh_node_count": (c_i32, [c_i32]),

@@ -1001,7 +1001,7 @@ def dfg_lut(device: torch.device, size: int = DFG_LUT_SIZE, nsample: int = DFG_L
 
 
 def upload_textures(ts: TextureSet, device: torch.device) -> tuple[torch.Tensor, torch.Tensor]:
-  """Texture descriptions and bytes (row-major levels) on the device, with the mip chains built there."""
+  """Texture descriptions and bytes on the device, with the mip chains built there."""
   data = torch.from_numpy(ts.data).to(device)
   stream = torch.cuda.current_stream(device).cuda_stream
   for d in ts.desc:
@@ -1009,26 +1009,6 @@ def upload_textures(ts: TextureSet, device: torch.device) -> tuple[torch.Tensor,
       _lib.call("mjpbr_build_mips", ctypes.byref(d), data.data_ptr(), stream)
   desc = torch.from_numpy(ts.desc_bytes()).to(device)
   return desc, data
-
-
-def tile_textures(desc: list[Any], data: torch.Tensor, device: torch.device) -> tuple[torch.Tensor, torch.Tensor]:
-  """The copy the render kernels sample: every level in 4 x 4-texel tiles (MJPBR_TEX_TILED), so
-  that a bilinear footprint mostly lies in one 64- or 128-byte tile instead of two rows. Returns
-  the tiled descriptions and bytes on the device; the row-major copy is kept by the caller."""
-  lib = _lib.load()
-  tiled, offset = [], 0
-  for d in desc:
-    t = _lib.Texture()
-    offset = int(lib.mjpbr_tiled_texture(ctypes.byref(d), offset, ctypes.byref(t)))
-    if offset < 0:
-      raise ValueError("texture description rejected by the tiled layout")
-    tiled.append(t)
-  out = torch.empty(max(offset, 16), dtype=torch.uint8, device=device)
-  stream = torch.cuda.current_stream(device).cuda_stream
-  for d, t in zip(desc, tiled, strict=True):
-    _lib.call("mjpbr_tile_texture", ctypes.byref(d), data.data_ptr(), ctypes.byref(t), out.data_ptr(), stream)
-  tiled_bytes = np.frombuffer(b"".join(bytes(t) for t in tiled), dtype=np.uint8).copy() if tiled else np.zeros(0, np.uint8)
-  return torch.from_numpy(tiled_bytes).to(device), out
 
 
 def _dev(a: np.ndarray | None, device: torch.device) -> torch.Tensor | None:
@@ -1088,11 +1068,10 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
   aov_pix = rgb_stride if op["denoise"] else 1
   t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(device) for k, v in hc.tables.items()}
   m = hc.meshes
-  textures = tex_data = tex_tiled = None
+  textures = tex_data = None
   tex_desc: list[Any] = []
   if hc.textures is not None:
-    _, tex_data = upload_textures(hc.textures, device)
-    textures, tex_tiled = tile_textures(hc.textures.desc, tex_data, device)
+    textures, tex_data = upload_textures(hc.textures, device)
     tex_desc = hc.textures.desc
   env = envmap_lib.upload_environments(hc.environments, device) if hc.environments is not None else None
   st = hc.settings
@@ -1161,7 +1140,6 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     textures=textures,
     tex_data=tex_data,
     tex_desc=tex_desc,
-    tex_tiled=tex_tiled,
     dfg_lut=dfg_lut(device),
     dfg_size=DFG_LUT_SIZE,
     env=env,

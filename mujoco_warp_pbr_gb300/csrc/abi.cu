@@ -224,14 +224,6 @@ int mjpbr_build_mips(const MjpbrTexture* tex, uint8_t* data, void* stream) {
   return build_mips_launch(tex, data, static_cast<cudaStream_t>(stream));
 }
 
-int64_t mjpbr_tiled_texture(const MjpbrTexture* rows, int64_t offset, MjpbrTexture* tiled) {
-  return tiled_texture_layout(rows, offset, tiled);
-}
-
-int mjpbr_tile_texture(const MjpbrTexture* rows, const uint8_t* src, const MjpbrTexture* tiled, uint8_t* dst, void* stream) {
-  return tile_texture_launch(rows, src, tiled, dst, static_cast<cudaStream_t>(stream));
-}
-
 int mjpbr_prefilter_env(const MjpbrTexture* radiance, const uint8_t* data, int32_t levels, int32_t height,
                         int32_t width, int32_t nsample, uint16_t* stack, void* stream) {
   return prefilter_launch(radiance, data, levels, height, width, nsample, stack, static_cast<cudaStream_t>(stream));

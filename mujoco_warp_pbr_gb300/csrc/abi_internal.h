@@ -29,8 +29,6 @@ int outputs_launch(const MjpbrScene& s, int which, int32_t cam, float depth_scal
                    cudaStream_t stream);
 int dfg_lut_launch(float* lut, int32_t size, int32_t nsample, cudaStream_t stream);
 int build_mips_launch(const MjpbrTexture* tex, uint8_t* data, cudaStream_t stream);
-int64_t tiled_texture_layout(const MjpbrTexture* rows, int64_t offset, MjpbrTexture* tiled);
-int tile_texture_launch(const MjpbrTexture* rows, const uint8_t* src, const MjpbrTexture* tiled, uint8_t* dst, cudaStream_t stream);
 int prefilter_launch(const MjpbrTexture* radiance, const uint8_t* data, int32_t levels, int32_t height, int32_t width,
                      int32_t nsample, uint16_t* stack, cudaStream_t stream);
 int env_sh9_launch(const float* image, int32_t h, int32_t w, double* rows, float* sh, cudaStream_t stream);

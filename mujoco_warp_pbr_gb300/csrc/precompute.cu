@@ -4,8 +4,6 @@
 // (envmap.py:171-221; Karis 2013, Krivanek & Colbert 2008), the environment's 9 spherical-harmonic
 // coefficients of Lambertian radiance (envmap.py:224-249; Ramamoorthi & Hanrahan 2001) and its
 // importance-sampling distribution (envmap.py:409-430).
-#include <algorithm>
-
 #include "abi_internal.h"
 #include "shading.cuh"
 
@@ -311,63 +309,6 @@ int build_mips_launch(const MjpbrTexture* tex, uint8_t* data, cudaStream_t strea
     dim3 grid((dw + 127) / 128, dh);
     mip_kernel<<<grid, 128, 0, stream>>>(t, data, level);
     int rc = check_launch("mip_kernel");
-    if (rc) return rc;
-  }
-  return MJPBR_OK;
-}
-
-// One texel of a level of the tiled copy: tiles of 4 x 4 texels, tiles row by row.
-__global__ void tile_kernel(const __grid_constant__ MjpbrTexture rows, const uint8_t* src, const __grid_constant__ MjpbrTexture tiled,
-                            uint8_t* dst, int32_t level) {
-  const int32_t w = max(rows.width >> level, 1), h = max(rows.height >> level, 1);
-  const int32_t tw = (w + 3) >> 2, th = (h + 3) >> 2;
-  const int32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= tw * 4 || y >= th * 4) return;
-  const int64_t t = ((int64_t)(y >> 2) * tw + (x >> 2)) * 16 + (y & 3) * 4 + (x & 3);
-  const bool inside = x < w && y < h;
-  if (rows.format == MJPBR_TEX_RGBA8) {
-    const uint32_t v = inside ? reinterpret_cast<const uint32_t*>(src + rows.level_offset[level])[(int64_t)y * w + x] : 0u;
-    reinterpret_cast<uint32_t*>(dst + tiled.level_offset[level])[t] = v;
-  } else {
-    const uint2 v = inside ? reinterpret_cast<const uint2*>(src + rows.level_offset[level])[(int64_t)y * w + x] : make_uint2(0u, 0u);
-    reinterpret_cast<uint2*>(dst + tiled.level_offset[level])[t] = v;
-  }
-}
-
-int64_t tiled_texture_layout(const MjpbrTexture* rows, int64_t offset, MjpbrTexture* tiled) {
-  if (!rows || !tiled || rows->nlevel < 1 || rows->nlevel > MJPBR_MAX_MIPS || rows->width < 1 || rows->height < 1 || offset < 0) return -1;
-  const int64_t texel = rows->format == MJPBR_TEX_RGBA8 ? 4 : 8;
-  MjpbrTexture t = *rows;
-  t.layout = MJPBR_TEX_TILED;
-  t.pad_ = 0;
-  int64_t off = (offset + 127) / 128 * 128;
-  for (int32_t level = 0; level < MJPBR_MAX_MIPS; ++level) {
-    if (level >= t.nlevel) {
-      t.level_offset[level] = 0;
-      continue;
-    }
-    const int64_t w = std::max(rows->width >> level, 1), h = std::max(rows->height >> level, 1);
-    t.level_offset[level] = off;
-    off += ((w + 3) / 4) * ((h + 3) / 4) * 16 * texel;
-    off = (off + 127) / 128 * 128;
-  }
-  *tiled = t;
-  return off;
-}
-
-int tile_texture_launch(const MjpbrTexture* rows, const uint8_t* src, const MjpbrTexture* tiled, uint8_t* dst, cudaStream_t stream) {
-  if (!rows || !src || !tiled || !dst) return set_error(MJPBR_ERR_ARG, "tile_texture: NULL argument");
-  MjpbrTexture check;
-  if (rows->layout != MJPBR_TEX_ROWS || tiled->layout != MJPBR_TEX_TILED || tiled_texture_layout(rows, tiled->level_offset[0], &check) < 0 ||
-      check.level_offset[0] != tiled->level_offset[0] || check.nlevel != tiled->nlevel || check.width != tiled->width ||
-      check.height != tiled->height || check.format != tiled->format) {
-    return set_error(MJPBR_ERR_ARG, "tile_texture: the tiled description does not match the row-major one");
-  }
-  for (int32_t level = 0; level < rows->nlevel; ++level) {
-    const int32_t w = max(rows->width >> level, 1), h = max(rows->height >> level, 1);
-    dim3 grid((((w + 3) >> 2) * 4 + 127) / 128, ((h + 3) >> 2) * 4);
-    tile_kernel<<<grid, 128, 0, stream>>>(*rows, src, *tiled, dst, level);
-    int rc = check_launch("tile_kernel");
     if (rc) return rc;
   }
   return MJPBR_OK;

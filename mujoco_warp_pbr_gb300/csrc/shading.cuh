@@ -230,9 +230,7 @@ MJ_DEV uint32_t encode_display(V3 c) {
 // ---------------------------------------------------------------- textures
 
 MJ_DEV float4 fetch_texel(const MjpbrTexture& t, const uint8_t* data, int level, int w, int x, int y) {
-  // tiled levels: 4 x 4-texel tiles row by row (MJPBR_TEX_TILED), else rows
-  const int64_t idx = t.layout == MJPBR_TEX_TILED ? ((int64_t)(y >> 2) * ((w + 3) >> 2) + (x >> 2)) * 16 + (y & 3) * 4 + (x & 3)
-                                                  : (int64_t)y * w + x;
+  int64_t idx = (int64_t)y * w + x;
   if (t.format == MJPBR_TEX_RGBA8) {
     uchar4 c = __ldg(reinterpret_cast<const uchar4*>(data + t.level_offset[level]) + idx);
     return make_float4(c.x * (1.0f / 255.0f), c.y * (1.0f / 255.0f), c.z * (1.0f / 255.0f), c.w * (1.0f / 255.0f));

@@ -209,15 +209,14 @@ def prepare_environments(images: list[np.ndarray]) -> HostEnvironments:
 class DeviceEnvironments:
   """Device resources: radiance textures (descriptions + bytes), prefiltered stacks, SH, tables."""
 
-  radiance_desc: torch.Tensor  # tiled descriptions (MJPBR_TEX_TILED), what the kernels read
-  radiance_data: torch.Tensor  # row-major levels (the prefilter's input)
-  desc: list[Any]              # row-major descriptions
+  radiance_desc: torch.Tensor
+  radiance_data: torch.Tensor
+  desc: list[Any]
   prefiltered: torch.Tensor  # (nenv, levels, h, w, 4) float16 stored as int16
   sh: torch.Tensor
   prob: torch.Tensor
   marginal: torch.Tensor
   conditional: torch.Tensor
-  radiance_tiled: torch.Tensor  # the tiled copy of radiance_data the render kernels sample
   levels: int
   height: int
   width: int
@@ -227,12 +226,10 @@ class DeviceEnvironments:
 def upload_environments(env: HostEnvironments, device: torch.device) -> DeviceEnvironments:
   from mujoco_warp_pbr_gb300.context import TEX_RGBA16F
   from mujoco_warp_pbr_gb300.context import pack_textures
-  from mujoco_warp_pbr_gb300.context import tile_textures
   from mujoco_warp_pbr_gb300.context import upload_textures
 
   ts = pack_textures([(TEX_RGBA16F, im) for im in env.radiance])
-  _, data = upload_textures(ts, device)
-  desc, tiled = tile_textures(ts.desc, data, device)
+  desc, data = upload_textures(ts, device)
   L, H, W = env.prefilter_levels, env.prefilter_height, env.prefilter_width
   stack = torch.zeros((env.nenv, L, H, W, 4), dtype=torch.int16, device=device)
   stream = torch.cuda.current_stream(device).cuda_stream
@@ -257,7 +254,6 @@ def upload_environments(env: HostEnvironments, device: torch.device) -> DeviceEn
   return DeviceEnvironments(
     radiance_desc=desc,
     radiance_data=data,
-    radiance_tiled=tiled,
     desc=ts.desc,
     prefiltered=stack,
     sh=sh,

@@ -161,8 +161,8 @@ class PbrRenderContext:
   blas_tri_base: torch.Tensor | None
   mesh_nface: list[int]
   # textures, tables and environment maps
-  textures: torch.Tensor | None  # tiled descriptions (MJPBR_TEX_TILED), what the kernels read
-  tex_data: torch.Tensor | None  # row-major levels (as uploaded, mip chains built)
+  textures: torch.Tensor | None
+  tex_data: torch.Tensor | None
   tex_desc: list[Any]
   dfg_lut: torch.Tensor
   dfg_size: int
@@ -190,7 +190,6 @@ class PbrRenderContext:
   # the wavefront schedule's ray queues and records (uint8, allocated at the first render that
   # needs them, sized by mjpbr_wave_scratch_bytes)
   wave_scratch: torch.Tensor | None = None
-  tex_tiled: torch.Tensor | None = None  # the tiled copy of tex_data the kernels sample
   # accepted for compatibility with the reference's signature; the GB300 kernels choose their own
   block_dim: int | None = None
   max_registers: int | None = None

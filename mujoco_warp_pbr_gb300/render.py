@@ -209,7 +209,7 @@ def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
       "blas_root": rc.blas_root,
       "blas_tri_base": rc.blas_tri_base,
       "textures": rc.textures,
-      "tex_data": rc.tex_tiled if rc.tex_tiled is not None else rc.tex_data,
+      "tex_data": rc.tex_data,
       "dfg_lut": rc.dfg_lut,
       "dfg_size": rc.dfg_size,
       "aov_guide": rc.aov_guide,
@@ -231,7 +231,7 @@ def scene_fields(m: Any, d: Any, rc: PbrRenderContext) -> dict[str, Any]:
         "prefilter_width": env.width,
         "env_prefiltered": env.prefiltered,
         "env_radiance": env.radiance_desc,
-        "env_data": env.radiance_tiled,
+        "env_data": env.radiance_data,
         "env_sh": env.sh,
         "cdf_height": int(env.prob.shape[1]),
         "cdf_width": int(env.prob.shape[2]),
