@@ -118,6 +118,15 @@ typedef struct MjpbrConv {
   int32_t in2_full; /* 1: in2 has the output resolution; 0: half of it, upsampled x2 */
 } MjpbrConv;
 
+/* Weights of the learned denoiser's U-Net (mujoco_warp_pbr_gb300.kpcn), layers in the order e0a
+ * e0b e1a e1b e2a e2b e3a e3b d2a d2b d1a d1b d0a d0b head: BF16 weight (c_out, 9, c_in + c_in2)
+ * as raw 16-bit values and FP32 bias (c_out), device pointers. */
+#define MJPBR_KPCN_LAYERS 15
+typedef struct MjpbrKpcnWeights {
+  const uint16_t* weight[MJPBR_KPCN_LAYERS];
+  const float* bias[MJPBR_KPCN_LAYERS];
+} MjpbrKpcnWeights;
+
 /* Weight and bias gradients of a 3x3 convolution layer (same tensors and constraints as
  * MjpbrConv): grad_weight (c_out, 9, c_in + c_in2) += sum over pixels of grad_out (x) the shifted
  * input, grad_bias (c_out) += sum of grad_out; FP32, accumulated into the existing values. */
@@ -399,6 +408,18 @@ int mjpbr_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m, i
 /* Forward 3x3 convolution (see MjpbrConv); also the input-gradient pass with the flipped,
  * transposed weights. No counterpart in the reference (its denoiser is the a-trous filter). */
 int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream);
+
+/* Bytes of the workspace mjpbr_denoise_learned needs for chunks of nimg worlds of a camera of
+ * width x height (-1: a size the network's tiles do not cover). */
+int64_t mjpbr_kpcn_workspace_bytes(int32_t nimg, int32_t height, int32_t width);
+
+/* The learned denoiser on a path-traced frame rendered with denoising (settings.denoise, the
+ * render's denoise_buffers[0] and aov_guide): per RGB camera, chunk worlds at a time, the network
+ * input, the U-Net, the per-pixel 5 x 5 kernels into denoise_buffers[1], then the a-trous filter's
+ * finish pass without filtering into the outputs. The same launches as kpcn.KPCN.denoise; no
+ * counterpart in the reference (its denoiser is the a-trous filter, mjpbr_denoise_atrous). */
+int mjpbr_denoise_learned(const MjpbrScene* scene, const MjpbrKpcnWeights* weights, void* workspace, int64_t workspace_bytes,
+                          int32_t chunk, void* stream);
 
 /* Weight / bias gradients of a 3x3 convolution (see MjpbrConvGrad), on the tensor cores. */
 int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream);

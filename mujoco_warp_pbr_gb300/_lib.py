@@ -40,6 +40,15 @@ class I32B(ctypes.Structure):
   _fields_ = [("ptr", c_vp), ("nbatch", c_i32), ("pad_", c_i32)]
 
 
+KPCN_LAYERS = 15
+
+
+class KpcnWeights(ctypes.Structure):
+  """MjpbrKpcnWeights."""
+
+  _fields_ = [("weight", c_vp * KPCN_LAYERS), ("bias", c_vp * KPCN_LAYERS)]
+
+
 class Texture(ctypes.Structure):
   """MjpbrTexture."""
 
@@ -333,6 +342,8 @@ _SIGNATURES = {
   "mjpbr_get_image": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_i32, c_vp, c_i32, c_vp]),
   "mjpbr_dfg_lut": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp]),
   "mjpbr_build_mips": (ctypes.c_int, [ctypes.POINTER(Texture), c_vp, c_vp]),
+  "mjpbr_kpcn_workspace_bytes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+  "mjpbr_denoise_learned": (ctypes.c_int, [ctypes.POINTER(Scene), ctypes.POINTER(KpcnWeights), c_vp, ctypes.c_int64, ctypes.c_int32, c_vp]),
   "mjpbr_prefilter_env": (ctypes.c_int, [ctypes.POINTER(Texture), c_vp, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp]),
   "mjpbr_denoise_atrous": (ctypes.c_int, [ctypes.POINTER(Scene), c_vp]),
   "mjpbr_bvh_node_count": (c_i32, [c_i32]),

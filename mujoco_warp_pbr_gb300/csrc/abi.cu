@@ -247,6 +247,16 @@ int mjpbr_conv3x3_bf16(const MjpbrConv* conv, void* stream) {
   return conv3x3_launch(*conv, static_cast<cudaStream_t>(stream));
 }
 
+int64_t mjpbr_kpcn_workspace_bytes(int32_t nimg, int32_t height, int32_t width) { return kpcn_workspace_bytes(nimg, height, width); }
+
+int mjpbr_denoise_learned(const MjpbrScene* scene, const MjpbrKpcnWeights* weights, void* workspace, int64_t workspace_bytes,
+                          int32_t chunk, void* stream) {
+  if (!scene || !weights) return set_error(MJPBR_ERR_ARG, "scene or weights is NULL");
+  int rc = validate_scene(scene, true);
+  if (rc) return rc;
+  return denoise_learned_launch(*scene, *weights, workspace, workspace_bytes, chunk, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_conv3x3_wgrad_bf16(const MjpbrConvGrad* grad, void* stream) {
   if (!grad) return set_error(MJPBR_ERR_ARG, "grad is NULL");
   return conv3x3_wgrad_launch(*grad, static_cast<cudaStream_t>(stream));

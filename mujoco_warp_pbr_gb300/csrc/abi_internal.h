@@ -36,6 +36,9 @@ int env_tables_launch(const double* image, int32_t h, int32_t w, float* prob, fl
                       cudaStream_t stream);
 int denoise_launch(const MjpbrScene& s, cudaStream_t stream);
 int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream);
+int64_t kpcn_workspace_bytes(int32_t nimg, int32_t height, int32_t width);
+int denoise_learned_launch(const MjpbrScene& s, const MjpbrKpcnWeights& wts, void* workspace, int64_t workspace_bytes, int32_t chunk,
+                           cudaStream_t st);
 int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream);
 int wait_probe_launch(uint32_t polls, int32_t* error_word, int32_t* roles_done, cudaStream_t stream);
 int kpcn_features_launch(const MjpbrScene& s, int32_t cam, int32_t w0, int32_t nw, uint16_t* x0, cudaStream_t st);

@@ -345,6 +345,16 @@ class KPCN:
       l.gb.zero_()
 
   # ---------------------------------------------------------------- rendering
+  def c_weights(self) -> _lib.KpcnWeights:
+    """The network's BF16 weights and FP32 biases as the C ABI's MjpbrKpcnWeights (device pointers,
+    valid while the network lives), for mjpbr_denoise_learned."""
+    wts = _lib.KpcnWeights()
+    for k, spec in enumerate(layer_specs()):
+      layer = self.layers[spec.name]
+      wts.weight[k] = layer.w16.data_ptr()
+      wts.bias[k] = layer.b.data_ptr()
+    return wts
+
   def denoise(self, m: Any, d: Any, rc: Any, chunk: int = 512) -> None:
     """Filters a denoising path-traced frame (rendered with render(..., denoise=False)) into the
     context's RGB (and HDR) outputs with the network, every RGB camera in turn, `chunk` worlds at a
