@@ -114,6 +114,8 @@ class KPCN:
     self.step_count = 0
     self.error = torch.zeros(1, dtype=torch.int32, device=self.device)
     self._ws: dict[tuple[int, int, int], dict[str, torch.Tensor]] = {}
+    self._c_ws: torch.Tensor | None = None  # mjpbr_denoise_learned's workspace
+    self._c_weights: _lib.KpcnWeights | None = None
 
   # ---------------------------------------------------------------- parameters
   def state_dict(self) -> dict[str, np.ndarray]:
@@ -355,15 +357,32 @@ class KPCN:
       wts.bias[k] = layer.b.data_ptr()
     return wts
 
-  def denoise(self, m: Any, d: Any, rc: Any, chunk: int = 512) -> None:
+  def denoise(self, m: Any, d: Any, rc: Any, chunk: int = 512, driver: str = "c") -> None:
     """Filters a denoising path-traced frame (rendered with render(..., denoise=False)) into the
     context's RGB (and HDR) outputs with the network, every RGB camera in turn, `chunk` worlds at a
     time (the activations of a chunk are the only network memory). Raises ValueError for camera
     sizes the convolution tiles do not cover (the a-trous filter, render(..., denoise=True),
-    handles those). Capturable in a CUDA graph after one call outside the capture."""
+    handles those). Capturable in a CUDA graph after one call outside the capture.
+
+    driver "c" makes the whole pass one library call (mjpbr_denoise_learned); "python" issues the
+    same launches from here, one call each (the reference the C driver is tested against)."""
     from mujoco_warp_pbr_gb300.render import scene
 
     s = scene(m, d, rc)
+    for (width, height), on in zip(rc.base.cam_res, rc.base.render_rgb):
+      if on and not supported(width, height):
+        raise ValueError(f"the learned denoiser needs images whose 4 levels tile into 128 pixels, got {width}x{height}")
+    if driver == "c":
+      lib = _lib.load()
+      nw = min(chunk, rc.nworld)
+      need = max(int(lib.mjpbr_kpcn_workspace_bytes(nw, h, w)) for (w, h), on in zip(rc.base.cam_res, rc.base.render_rgb) if on)
+      if self._c_ws is None or self._c_ws.numel() < need:
+        self._c_ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+      if self._c_weights is None:
+        self._c_weights = self.c_weights()
+      _lib.call("mjpbr_denoise_learned", ctypes.byref(s), ctypes.byref(self._c_weights), self._c_ws.data_ptr(), self._c_ws.numel(), chunk,
+                self._stream())
+      return
     n = rc.nworld
     st = self._stream()
     src = rc.denoise_buffers[0].view(n, -1, 4)

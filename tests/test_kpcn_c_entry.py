@@ -28,7 +28,7 @@ def test_c_entry_matches_the_python_denoiser():
   from mujoco_warp_pbr_gb300 import kpcn, synthetic
   from tests import helpers
 
-  sc = synthetic.path_scene(seed=4, nworld=6, res=64)
+  sc = synthetic.path_scene(seed=4, nworld=6, res=128)
   m, d, rc = helpers.gpu_scene(sc, denoise=True)
   net = kpcn.KPCN.load(Path(kpcn.__file__).resolve().parent / "weights" / "kpcn_path.npz")
 
@@ -42,10 +42,10 @@ def test_c_entry_matches_the_python_denoiser():
     assert mjpbr.check_errors(rc) == 0
     return rc.base.rgb_data.cpu().numpy().copy(), rc.hdr_data.cpu().numpy().copy()
 
-  ref = frame(lambda: net.denoise(m, d, rc, chunk=4))
+  ref = frame(lambda: net.denoise(m, d, rc, chunk=4, driver="python"))
   lib = _lib.load()
   scene = mjpbr.scene_descriptor(m, d, rc)
-  nbytes = lib.mjpbr_kpcn_workspace_bytes(4, 64, 64)
+  nbytes = lib.mjpbr_kpcn_workspace_bytes(4, 128, 128)
   ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
   wts = net.c_weights()
   stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -56,6 +56,10 @@ def test_c_entry_matches_the_python_denoiser():
 
   got = frame(c_call)
   for a, b in zip(got, ref):
+    np.testing.assert_array_equal(a, b)
+  # the default driver of KPCN.denoise is this call
+  got2 = frame(lambda: net.denoise(m, d, rc, chunk=4))
+  for a, b in zip(got2, ref):
     np.testing.assert_array_equal(a, b)
   # a workspace one byte short and a chunk of zero are rejected before any launch
   assert lib.mjpbr_denoise_learned(ctypes.byref(scene), ctypes.byref(wts), ctypes.c_void_p(ws.data_ptr()), nbytes - 1, 4, stream) == _lib.ERR_ARG
