@@ -5,12 +5,14 @@
 //   start    one path per (pixel, sample) of the RGB cameras: the camera ray (pt_bounce.cuh
 //            start_sample); depth / segmentation of cameras without RGB (one ray per pixel)
 //   per bounce, over the queue of live paths:
-//     extend   closest hit of every path; depth / segmentation from sample 0's first hit
+//     extend   closest hit of every path (persistent, lanes refilled from the queue: refill.cuh);
+//              depth / segmentation from sample 0's first hit
 //     shade    the bounce after the hit (PtCore::surface): emission, mirror lobe, next-event
-//              estimation recorded per path (each light's unshadowed contribution and shadow ray,
-//              the environment sample's term and ray), the BSDF sample and Russian roulette;
-//              shadow rays and the paths that continue are appended to queues (one atomic per CTA)
-//     shadow   any hit of every recorded shadow ray
+//              estimation recorded per path (each light's unshadowed contribution, the environment
+//              sample's term) with each shadow ray appended to the shadow queue as it is recorded
+//              (one atomic per group of converged lanes), the BSDF sample and Russian roulette;
+//              the paths that continue are appended to the next queue (one atomic per CTA)
+//     shadow   any hit of every queued shadow ray (persistent, lanes refilled)
 //   (the recorded terms of the unoccluded rays are added to the path's radiance, in light order,
 //   by the next bounce's extend stage, or by the resolve stage for a path that ended: the
 //   persistent kernel's exact additions in its order)
@@ -20,9 +22,10 @@
 // image is the persistent kernel's, bit for bit (the random numbers are counter-based per sample
 // and bounce, so the order in which paths run does not matter).
 //
-// Scratch (MjpbrScene.wave_scratch), per path of a chunk: the path state (128 B), its hit (32 B),
-// its next-event record (32 B + 32 B per slot: each light, the headlight, the environment), one
-// visibility byte per slot, two queue entries and up to one shadow entry (32 B) per slot.
+// Scratch (MjpbrScene.wave_scratch), per path of a chunk: the path record (80 B every bounce moves,
+// 48 B of first-surface features), its hit (32 B), its next-event record (16 B + 16 B per slot: each
+// light, the headlight, the environment), one visibility byte per slot, two queue entries and up to
+// one shadow entry (32 B) per slot.
 #include <algorithm>
 #include <climits>
 
