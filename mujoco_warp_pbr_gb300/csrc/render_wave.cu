@@ -510,34 +510,38 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_resolve_
   stage_world_block(s, w, blk, kThreads);
   __syncthreads();
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  // a CTA shades `ppc` pixels of a tile with one thread per camera sample (nn consecutive threads
+  // per pixel); the pixel's first thread sums the samples in sample order through shared memory
+  __shared__ float sums[kThreads * 6];
+  const int32_t nn = wm.nn;
+  const int32_t ppc = kThreads / nn, parts = (kTile * kTile + ppc - 1) / ppc;
   int32_t cam, tx, ty;
-  tile_of(wm.rgb, blockIdx.x, &cam, &tx, &ty);
+  tile_of(wm.rgb, blockIdx.x / parts, &cam, &tx, &ty);
+  const int32_t lp = threadIdx.x / nn, smp = threadIdx.x - lp * nn;
+  const int32_t q = (blockIdx.x % parts) * ppc + lp;
   Pixel p;
   p.cam = cam;
   p.width = s.cam_res[cam][0];
   p.height = s.cam_res[cam][1];
   p.rec = blk + L.cam_off + cam * kCamFloats;
-  const int32_t q = threadIdx.x;
   p.px = tx * kTile + z_x(q);
   p.py = ty * kTile + z_y(q);
-  if (p.px >= p.width || p.py >= p.height) return;
+  const bool active = lp < ppc && q < kTile * kTile && p.px < p.width && p.py < p.height;
   p.pixelid = p.py * p.width + p.px;
   const MjpbrSettings& st = s.settings;
   RtCtx c;
   init_ctx(c, s, blk, L, w, kTex);
   const M3 R = cam_mat(p.rec);
   const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
-  const int32_t n = st.samples_per_axis, nn = wm.nn;
+  const int32_t n = st.samples_per_axis;
   const float inv_n = 1.0f / (float)n;
-  float pixel_spread, pixel_width;
-  pixel_cone(s, p, &pixel_spread, &pixel_width);
-  const float spread = pixel_spread * inv_n;
   const V3 head_dir = -V3{R.m[2], R.m[5], R.m[8]};
   const uint32_t pseed = pixel_seed_of(s, seed, w, cam, p.pixelid);
   const int32_t first = blockIdx.y * wm.per_world + wm.sample_base[cam] + p.pixelid * nn;
-  V3 display = v3(0.0f), hdr = v3(0.0f);
-#pragma unroll 1
-  for (int32_t smp = 0; smp < nn; ++smp) {
+  if (active) {
+    float pixel_spread, pixel_width;
+    pixel_cone(s, p, &pixel_spread, &pixel_width);  // reads the camera's rays: active pixels only
+    const float spread = pixel_spread * inv_n;
     V3 dcam, ocam;
     float max_dist, depth_z;
     primary_ray(s, p, n, smp % n, smp / n, &dcam, &ocam, &max_dist, &depth_z);
@@ -587,8 +591,18 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_resolve_
       s.guide_normal[a + 1] = gnormal.y;
       s.guide_normal[a + 2] = gnormal.z;
     }
-    display += display_transform(radiance * c.exposure, st.tone_mapper);
-    hdr += radiance;
+    const V3 display = display_transform(radiance * c.exposure, st.tone_mapper);
+    float* slot_sum = sums + threadIdx.x * 6;
+    slot_sum[0] = display.x, slot_sum[1] = display.y, slot_sum[2] = display.z;
+    slot_sum[3] = radiance.x, slot_sum[4] = radiance.y, slot_sum[5] = radiance.z;
+  }
+  __syncthreads();
+  if (!active || smp != 0) return;
+  V3 display = v3(0.0f), hdr = v3(0.0f);
+  for (int32_t k = 0; k < nn; ++k) {  // the samples in sample order, as one thread's loop would add them
+    const float* v = sums + (threadIdx.x + k) * 6;
+    display += V3{v[0], v[1], v[2]};
+    hdr += V3{v[3], v[4], v[5]};
   }
   const int64_t adr = (int64_t)w * s.rgb_stride + s.rgb_adr[cam] + p.pixelid;
   const float inv_nn = inv_n * inv_n;
@@ -765,7 +779,8 @@ int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t
     }
     stage_mark(stream);
     if (rgb_tiles > 0) {
-      k_resolve<<<dim3(rgb_tiles, wm.nw), kThreads, blk_bytes, stream>>>(s, seed, wm);
+      const int32_t ppc = kThreads / wm.nn, parts = (kTile * kTile + ppc - 1) / ppc;
+      k_resolve<<<dim3(rgb_tiles * parts, wm.nw), kThreads, blk_bytes, stream>>>(s, seed, wm);
       if ((rc = check_launch("wave_resolve_kernel"))) return rc;
     }
     stage_mark(stream);
