@@ -237,7 +237,7 @@ def path_tier(dev, steps: int, nworld: int = 1024, res: int = 128, spp: int = 2)
   synthetic.apply_per_world(small, ms_, rcs)
   counts = roofline.count_frame(mjpbr.scene_descriptor(ms_, ds_, rcs), 100, stream.cuda_stream)
   fp32 = roofline.fp32_roofline(counts, small.nworld * res * res, npix, avg,
-                               kernel="path wavefront: ptw_start, ptw_extend, ptw_shade, ptw_shadow, ptw_resolve per chunk")
+                               kernel="path wavefront: ptw_first_extend, ptw_extend, ptw_shade, ptw_shadow, ptw_resolve per chunk")
   return {
     "workload": sc.name,
     "value": npix / (avg / 1000.0) / 1e6,
@@ -541,7 +541,7 @@ def run(args) -> None:
     traffic = _traffic(sc.name)
     launches = render_launches(rc, int(chunks.value), int(scene.nlight))
     if args.workload == "path":
-      kernel = "path wavefront: ptw_start, ptw_extend, ptw_shade, ptw_shadow, ptw_resolve per chunk, one frame"
+      kernel = "path wavefront: ptw_first_extend, ptw_extend, ptw_shade, ptw_shadow, ptw_resolve per chunk, one frame"
     elif wave:
       kernel = "wavefront render: wave_primary, wave_surface, wave_mirror, wave_mirror_surface, wave_shadow, wave_resolve per chunk, one frame"
     else:

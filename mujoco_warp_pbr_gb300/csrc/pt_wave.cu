@@ -2,11 +2,12 @@
 // the bounce loop of mujoco_warp_pbr/_src/pathtrace.py:200-421 over every path of a chunk of
 // worlds at once, one kernel per stage and compacted path queues between the bounces:
 //
-//   start    one path per (pixel, sample) of the RGB cameras: the camera ray (pt_bounce.cuh
-//            start_sample); depth / segmentation of cameras without RGB (one ray per pixel)
+//   geometry depth / segmentation of cameras without RGB (one ray per pixel)
 //   per bounce, over the queue of live paths:
 //     extend   closest hit of every path (persistent, lanes refilled from the queue: refill.cuh);
-//              depth / segmentation from sample 0's first hit
+//              depth / segmentation from sample 0's first hit; the first bounce's extend starts
+//              the paths itself, one per (pixel, sample) of the RGB cameras (pt_bounce.cuh
+//              start_sample), and writes each path record once, after its hit
 //     shade    the bounce after the hit (PtCore::surface): emission, mirror lobe, next-event
 //              estimation recorded per path (each light's unshadowed contribution, the environment
 //              sample's term) with each shadow ray appended to the shadow queue as it is recorded
@@ -317,29 +318,6 @@ MJ_DEV void apply_nee(const PtWaveMap& wm, int32_t path, PathRec& r) {
   rec[0].w = __int_as_float(0);
 }
 
-// ---------------------------------------------------------------- start
-__global__ void __launch_bounds__(kThreads) ptw_start_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
-                                                             const __grid_constant__ PtWaveMap wm) {
-  const int32_t path = blockIdx.x * kThreads + threadIdx.x;
-  if (path == 0) {
-    wm.counters[0] = wm.npath;
-    wm.counters[1] = 0;
-    for (int k = 4; k < 8; ++k) wm.counters[k] = 0;  // the extend and shadow stages' fetch counters
-  }
-  if (path >= wm.npath) return;
-  int32_t w, sample;
-  Pixel p;
-  path_pixel(s, wm, path, &w, &p, &sample);
-  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-  p.rec = world_block(s, w) + L.cam_off + p.cam * kCamFloats;
-  const M3 R = cam_mat(p.rec);
-  const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
-  PathState ps;
-  start_sample(ps, s, p, pixel_seed_of(s, seed, w, p), R, cpos, sample);
-  store_path(wm.path[path], ps, 0.0f);
-  wm.queue[0][path] = path;
-}
-
 // ---------------------------------------------------------------- cameras without RGB
 template <bool kMesh>
 __global__ void __launch_bounds__(kThreads) ptw_geometry_kernel(const __grid_constant__ MjpbrScene s,
@@ -423,6 +401,61 @@ __global__ void __launch_bounds__(kThreads, 3) ptw_extend_kernel(const __grid_co
           write_geometry(s, ww, p, hit, dcam_z);
           if (hit.geom != -1) r.rad.w = hit.dist * -dcam_z;
         }
+      },
+      &err);
+  if (err && s.error_word) atomicOr(s.error_word, err);
+}
+
+// The first bounce's extend, with the start folded in: each path's camera ray is generated where
+// it is traced (start_sample, pt_bounce.cuh) and the path record written once, after the hit; the
+// path queue of the shade stage is the identity.
+template <bool kMesh>
+__global__ void __launch_bounds__(kThreads, 3) ptw_first_extend_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
+                                                                       const __grid_constant__ PtWaveMap wm) {
+  extern __shared__ __align__(16) float smem[];
+  const Stack st = wave_stack(s, smem);
+  const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
+  const bool cull = s.settings.cull_backfaces != 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) wm.counters[0] = wm.npath;  // the shade stage's queue
+  int32_t err = 0;
+  ClosestQuery q;
+  const float* blk = nullptr;
+  int32_t path = -1;
+  // the path's start state (the same for the ray and for the record stored after the hit)
+  auto start = [&](int32_t i, PathState& ps, Pixel& p, int32_t& w, int32_t& sample) {
+    path_pixel(s, wm, i, &w, &p, &sample);
+    p.rec = world_block(s, w) + L.cam_off + p.cam * kCamFloats;
+    const M3 R = cam_mat(p.rec);
+    const V3 cpos{p.rec[0], p.rec[1], p.rec[2]};
+    start_sample(ps, s, p, pixel_seed_of(s, seed, w, p), R, cpos, sample);
+  };
+  refill_loop<MJPBR_PTW_REFILL_STEPS>(
+      wm.npath, reinterpret_cast<unsigned long long*>(wm.counters + 4), q,
+      [&](int64_t item, ClosestQuery& qq) {
+        path = (int32_t)item;
+        wm.queue[0][path] = path;
+        PathState ps;
+        Pixel p;
+        int32_t w, sample;
+        start(path, ps, p, w, sample);
+        blk = world_block(s, w);
+        closest_begin(qq, st, Ray{ps.o, ps.d}, ps.max_dist, &err);
+        return true;
+      },
+      [&](ClosestQuery& qq) { return closest_step<kMesh>(qq, s, st, blk, L, cull, &err); },
+      [&](ClosestQuery& qq, int32_t) {
+        const Hit& hit = qq.h;
+        wm.hit[path] = pack_hit(hit);
+        PathState ps;
+        Pixel p;
+        int32_t w, sample;
+        start(path, ps, p, w, sample);
+        float first_depth = 0.0f;
+        if (sample == 0) {
+          write_geometry(s, w, p, hit, ps.dcam_z);
+          if (hit.geom != -1) first_depth = hit.dist * -ps.dcam_z;
+        }
+        store_path(wm.path[path], ps, first_depth);
       },
       &err);
   if (err && s.error_word) atomicOr(s.error_word, err);
@@ -599,15 +632,18 @@ int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int3
   const size_t stack = (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
   auto k_geometry = ptw_geometry_kernel<kMesh>;
   auto k_extend = ptw_extend_kernel<kMesh>;
+  auto k_first = ptw_first_extend_kernel<kMesh>;
   auto k_shade = ptw_shade_kernel<kMesh, kTex>;
   auto k_shadow = ptw_shadow_kernel<kMesh>;
   auto k_resolve = ptw_resolve_kernel<kTex>;
   int rc = set_smem(k_geometry, stack, "path wavefront geometry");
   if (!rc) rc = set_smem(k_extend, stack, "path wavefront extend");
+  if (!rc) rc = set_smem(k_first, stack, "path wavefront first extend");
   if (!rc) rc = set_smem(k_shadow, stack, "path wavefront shadow");
   if (rc) return rc;
   const int sms = device_sm_count();
   const int g_extend = sms * resident_ctas(k_extend, stack);
+  const int g_first = sms * resident_ctas(k_first, stack);
   const int g_shade = sms * resident_ctas(k_shade, 0);
   const int g_shadow = sms * resident_ctas(k_shadow, stack);
   PtWaveMap wm;
@@ -629,12 +665,18 @@ int launch_pt_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int3
       if ((rc = check_launch("ptw_geometry_kernel"))) return rc;
     }
     if (wm.npath == 0) continue;
-    ptw_start_kernel<<<(unsigned)((wm.npath + kThreads - 1) / kThreads), kThreads, 0, stream>>>(s, seed, wm);
-    if ((rc = check_launch("ptw_start_kernel"))) return rc;
+    // queue lengths and the fetch counters; the first extend sets the shade stage's queue length
+    cudaError_t ez = cudaMemsetAsync(wm.counters, 0, 8 * sizeof(int32_t), stream);
+    if (ez != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path wavefront counters: %s", cudaGetErrorString(ez));
     for (int32_t it = 0; it < iterations; ++it) {
       const int32_t cur = it & 1, next = cur ^ 1;
-      k_extend<<<g_extend, kThreads, stack, stream>>>(s, wm, cur, it > 0);
-      if ((rc = check_launch("ptw_extend_kernel"))) return rc;
+      if (it == 0) {
+        k_first<<<g_first, kThreads, stack, stream>>>(s, seed, wm);
+        if ((rc = check_launch("ptw_first_extend_kernel"))) return rc;
+      } else {
+        k_extend<<<g_extend, kThreads, stack, stream>>>(s, wm, cur, true);
+        if ((rc = check_launch("ptw_extend_kernel"))) return rc;
+      }
       cudaError_t e = cudaMemsetAsync(wm.counters + next, 0, sizeof(int32_t), stream);
       // shadow entries [2], the fetch counters of the next extend [4..5] and of the shadow stage [6..7]
       if (e == cudaSuccess) e = cudaMemsetAsync(wm.counters + 2, 0, 6 * sizeof(int32_t), stream);
