@@ -8,12 +8,18 @@ environment rotation). A step is refit_bvh + render of one frame of every world.
   value      Mpix/s from CUDA events around each step (inputs resident on the device); L2 is
              flushed (a 256 MB write) before every timed step, outside the events.
   e2e        the same metric through the public API with host buffers: every step copies the
-             geom / camera / light poses from pinned host memory to the device, refits, renders
-             and copies the packed RGB images back to pinned host memory.
-  roofline   the render kernel's algorithmic HBM bytes (outputs written once, world blocks and
-             tables read once) per launch over its event-timed duration, against the measured
-             copy bandwidth; the kernel is bound by FP32 issue and traversal latency, not HBM,
-             so this fraction is small by construction.
+             geom / camera / light poses from pinned host memory to the device, refits, renders,
+             converts with get_rgb and copies the float images (the reference's output format) to
+             pinned host memory; frames above 64 MB of images copy on a second stream while the
+             next step renders (double-buffered), and the timed region ends when the last copy
+             has landed.
+  roofline   the frame's algorithmic HBM bytes (outputs written once, world blocks and tables
+             read once) over its event-timed duration, against the measured copy bandwidth, with
+             the DRAM traffic of the frame's stage kernels from an ncu launch list; the render is
+             bound by traversal latency and divergence, not HBM, so this fraction is small by
+             construction.
+  stages_ms  the wavefront's stage split from CUDA events the library records at every stage
+             boundary in the timed steps.
   roofline_fp32, rays_per_s  the real-time kernel's algorithmic FP32 work: a 256-world frame of the
              same scene rendered by the counting build (libmjpbr_count.so) counts ray queries,
              box / triangle / primitive tests and shading work; FLOPS_PER_OP of
@@ -22,12 +28,14 @@ environment rotation). A step is refit_bvh + render of one frame of every world.
   cpu_baseline  the CPU oracle (scalar C restatement of the reference's real-time tier, OpenMP
              over all host cores) on a bounded sample of the same workload.
 
-Other workloads (--workload): primitives (16 worlds x 64², plane + 8 primitives, soft shadows),
+Other workloads (--workload): primitives (16 worlds x 64², plane + 8 primitives, soft shadows;
+a tens-of-microseconds frame, timed as a CUDA graph replay of refit + render),
 batched (2048 worlds x 3 cameras of 64², 128² and 256², one a fisheye bundle, enable masks,
 autotuned launch shape, one CUDA graph per step), path (the path-traced tier as the headline),
 large_path (8192 worlds x 2 cameras x 256², 2 spp, four environments, learned denoiser, one CUDA
 graph per frame). The default line also carries path_tier (1024 worlds x 128² with emissive quads
-at 2 spp) and learned_denoiser (learned 2 spp vs a-trous 16 spp: relative MSE and Mpix/s).
+at 2 spp), learned_denoiser (learned 2 spp vs a-trous 16 spp: relative MSE and Mpix/s), batched
+and large_path (at 1024 worlds).
 
 --impl reference times the reference's own CPU implementation of the path: the reference is
 Python on Warp / MuJoCo Warp (not installable here), so its CPU path is timed through the C

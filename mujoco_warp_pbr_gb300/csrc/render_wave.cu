@@ -6,11 +6,14 @@
 //                 depth / segmentation of the pixel from its first sample
 //   2. surface 0  eval_surface at the primary hit -> surface record; every light the shading will
 //                 ask about appends one shadow entry, a reflective surface one mirror ray
-//   3. mirror     closest hit of every queued mirror ray -> hit record
+//   3. mirror     closest hit of every queued mirror ray -> hit record (persistent; lanes take a
+//                 new ray as soon as theirs is done: refill.cuh)
 //   4. surface 1  eval_surface at the mirror hit -> surface record, shadow entries
-//   5. shadow     every shadow entry's rays (any hit) -> count of unoccluded rays
-//   6. resolve    one thread per pixel: the shading of both segments with the stored counts,
-//                 tone map per sample, average, encode; guides
+//   5. shadow     every shadow entry's rays (any hit, persistent with lane refill) -> count of
+//                 unoccluded rays
+//   6. resolve    one thread per camera sample: the shading of both segments with the stored
+//                 counts, tone map; the pixel's first thread averages its samples in sample
+//                 order and encodes; guides
 //
 // Each stage has its own small register budget and instruction footprint, and its warps run one
 // kind of work (the megakernel interleaves traversal, texturing and shading in every warp and is
