@@ -47,6 +47,6 @@ def test_bench_reads_committed_traffic():
   """The bench's roofline.traffic comes from the committed ncu figures, per workload."""
   import bench
 
-  assert bench._traffic("mesh_ibl_4096x128") == 139461989376
-  assert bench._traffic("path_1024x128_spp2") == 62562225664
+  assert bench._traffic("mesh_ibl_4096x128") == 138889244928
+  assert bench._traffic("path_1024x128_spp2") == 57841523456
   assert bench._traffic("mesh_ibl_1024x128") is None
