@@ -631,6 +631,14 @@ namespace {
 #define MJPBR_CONV_SMEM_BUDGET (110 * 1024)
 #endif
 constexpr size_t kPipeSmemBudget = MJPBR_CONV_SMEM_BUDGET;
+// One CTA per SM with most of the shared memory: measured faster for the layers of 16-pixel rows and
+// the 64-pixel-row layers of 96 or more input channels (their staged pipeline then holds bigger
+// stages), slower for every other layer shape of the denoiser.
+constexpr size_t kPipeSmemWide = 200 * 1024;
+
+size_t pipe_budget(int32_t width, int32_t cin) {
+  return (width <= 16 || (width == 64 && cin >= 96)) ? kPipeSmemWide : kPipeSmemBudget;
+}
 constexpr size_t kPipeSmemMax = 220 * 1024;
 int conv_sm_count() { return device_sm_count(); }
 
@@ -754,13 +762,14 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     };
     // resident weights when they fit beside two one-chunk stages; then the largest stage (in
     // chunks) of which two fit, then as many stages as fit (at most kMaxStages)
-    const bool resident = wbytes + 2 * stage_bytes(1, true) <= kPipeSmemBudget;
+    const size_t budget = pipe_budget(w, g.cin);
+    const bool resident = wbytes + 2 * stage_bytes(1, true) <= budget;
     const size_t fixed = resident ? wbytes : 0;
     const int32_t gmax = std::max(nci, nchunk - nci);
     int32_t G = 1;
-    while (G < gmax && fixed + 2 * stage_bytes(G + 1, resident) <= kPipeSmemBudget) ++G;
+    while (G < gmax && fixed + 2 * stage_bytes(G + 1, resident) <= budget) ++G;
     int32_t nst = 2;
-    while (nst < kMaxStages && fixed + (nst + 1) * stage_bytes(G, resident) <= kPipeSmemBudget) ++nst;
+    while (nst < kMaxStages && fixed + (nst + 1) * stage_bytes(G, resident) <= budget) ++nst;
     wg.group = G;
     wg.nstage = nst;
     wg.resident = resident;
@@ -769,7 +778,7 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     wg.rowplane = wg.spitch * 16;
     wg.in2_off = (int32_t)round128((size_t)2 * nci * wg.rowplane);
     wg.slot_bytes = (int32_t)round128((size_t)wg.in2_off + (size_t)2 * (nchunk - nci) * wg.rowplane);
-    wg.nslot = (int32_t)std::min<size_t>(kMaxSlots, kPipeSmemBudget > wbytes ? (kPipeSmemBudget - wbytes) / wg.slot_bytes : 0);
+    wg.nslot = (int32_t)std::min<size_t>(kMaxSlots, budget > wbytes ? (budget - wbytes) / wg.slot_bytes : 0);
     wg.ring = conv_ring_enabled() && wg.single && (c.c_in2 == 0 || c.in2_full) && wg.nslot >= 4;
     wg.abuf = (int32_t)round128((size_t)copies * 2 * G * wg.plane);
     wg.s2buf = half_in2 ? (int32_t)round128((size_t)2 * G * wg.s2plane) : 0;
