@@ -33,6 +33,8 @@
  *   mjpbr_build_scene_bvh  scene BVH build of mujoco_warp.create_render_context (third party; called at
  *                                                                          mujoco_warp_pbr/_src/io.py:511-528)
  *   mjpbr_build_mesh_bvh   per-mesh BVH build (warp.Mesh, mujoco_warp_pbr/_src/io.py:164-179,198-203)
+ *   mjpbr_newton_sync_poses   newton_pbr ScenePoses.sync                  (newton-pbr/newton_pbr/_render.py:31-131)
+ *   mjpbr_newton_images       newton_pbr SensorPbrCamera output copy      (newton-pbr/newton_pbr/sensor.py:45-86,247-265)
  */
 #ifndef MJPBR_H_
 #define MJPBR_H_
@@ -496,6 +498,31 @@ int mjpbr_get_segmentation(const MjpbrScene* scene, int32_t cam, int32_t* out, i
  * 2 guide_normal, into out (nworld_out, H, W, 3). mujoco_warp_pbr/_src/output.py:55-152. */
 int mjpbr_get_image(const MjpbrScene* scene, int32_t which, int32_t cam, float* out, int32_t nworld_out,
                     void* stream);
+
+/* Newton sensor adapter, pose step: the geom poses (geom_xpos (nworld, ngeom, 3), geom_xmat
+ * (nworld, ngeom, 9)) and camera `cam`'s pose (cam_xpos (nworld, ncam, 3), cam_xmat (nworld, ncam, 9))
+ * of every render world from a Newton model's transforms. Transforms are Newton's transformf:
+ * position, then a unit quaternion (x, y, z, w), 7 floats. Geom g of world w shows shape
+ * s = geom_shape[w or 0][g] (geom_shape_rows 1 or nworld): pose = body_q[shape_body[s]] (if >= 0)
+ * * shape_transform[s] * geom_offset[g]; world w's camera takes camera_transforms[w] (both look
+ * along local -Z with +Y up). A shape index outside [0, nshape) or a body index >= nbody is
+ * skipped and ORs 8 into *error_word (device int32). All arrays device memory.
+ * newton-pbr/newton_pbr/_render.py:31-77 (the pose kernel) and :96-131 (ScenePoses.sync). */
+int mjpbr_newton_sync_poses(const float* body_q, int32_t nbody, const int32_t* shape_body, const float* shape_transform,
+                            int32_t nshape, const int32_t* geom_shape, int32_t geom_shape_rows, const float* geom_offset,
+                            const float* camera_transforms, int32_t nworld, int32_t ngeom, int32_t ncam, int32_t cam,
+                            float* geom_xpos, float* geom_xmat, float* cam_xpos, float* cam_xmat, int32_t* error_word,
+                            void* stream);
+
+/* Newton sensor adapter, output step: rendering camera `cam`'s outputs, every world, in Newton's
+ * formats, each (nworld, H, W[, 3]) device memory or NULL when not wanted: color packed
+ * 0xAABBGGRR; depth the ray distance (planar depth * ray_scale[pixel], ray_scale (H, W)) and
+ * forward_depth the planar depth, both -1 where nothing is hit; shape_index the Newton shape
+ * geom_shape[w or 0][geom] of a geom hit, else 0xFFFFFFFF; hdr linear radiance before exposure.
+ * newton-pbr/newton_pbr/sensor.py:45-86 (_copy_outputs) called at :247-265. */
+int mjpbr_newton_images(const MjpbrScene* scene, int32_t cam, const int32_t* geom_shape, int32_t geom_shape_rows,
+                        const float* ray_scale, uint32_t* color, float* depth, float* forward_depth, uint32_t* shape_index,
+                        float* hdr, void* stream);
 
 /* Split-sum DFG table (size, size, 2) float32 into lut (device), nsample Hammersley samples per
  * texel. mujoco_warp_pbr/_src/ibl.py:62-101. */

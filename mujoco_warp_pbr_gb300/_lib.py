@@ -340,6 +340,11 @@ _SIGNATURES = {
   "mjpbr_get_depth": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_f32, c_vp, c_i32, c_vp]),
   "mjpbr_get_segmentation": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp]),
   "mjpbr_get_image": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_i32, c_vp, c_i32, c_vp]),
+  "mjpbr_newton_sync_poses": (
+    ctypes.c_int,
+    [c_vp, c_i32, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+  ),
+  "mjpbr_newton_images": (ctypes.c_int, [ctypes.POINTER(Scene), c_i32, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
   "mjpbr_dfg_lut": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp]),
   "mjpbr_build_mips": (ctypes.c_int, [ctypes.POINTER(Texture), c_vp, c_vp]),
   "mjpbr_kpcn_workspace_bytes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),

@@ -216,6 +216,26 @@ int mjpbr_get_image(const MjpbrScene* scene, int32_t which, int32_t cam, float* 
   return outputs_launch(*scene, 3 + which, cam, 1.0f, out, nworld_out, static_cast<cudaStream_t>(stream));
 }
 
+int mjpbr_newton_sync_poses(const float* body_q, int32_t nbody, const int32_t* shape_body, const float* shape_transform,
+                            int32_t nshape, const int32_t* geom_shape, int32_t geom_shape_rows, const float* geom_offset,
+                            const float* camera_transforms, int32_t nworld, int32_t ngeom, int32_t ncam, int32_t cam,
+                            float* geom_xpos, float* geom_xmat, float* cam_xpos, float* cam_xmat, int32_t* error_word,
+                            void* stream) {
+  return newton_sync_poses_launch(body_q, nbody, shape_body, shape_transform, nshape, geom_shape, geom_shape_rows, geom_offset,
+                                  camera_transforms, nworld, ngeom, ncam, cam, geom_xpos, geom_xmat, cam_xpos, cam_xmat,
+                                  error_word, static_cast<cudaStream_t>(stream));
+}
+
+int mjpbr_newton_images(const MjpbrScene* scene, int32_t cam, const int32_t* geom_shape, int32_t geom_shape_rows,
+                        const float* ray_scale, uint32_t* color, float* depth, float* forward_depth, uint32_t* shape_index,
+                        float* hdr, void* stream) {
+  if (!scene) return set_error(MJPBR_ERR_ARG, "scene is NULL");
+  int rc = validate_scene(scene, true);
+  if (rc) return rc;
+  return newton_images_launch(*scene, cam, geom_shape, geom_shape_rows, ray_scale, color, depth, forward_depth, shape_index,
+                              hdr, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_dfg_lut(float* lut, int32_t size, int32_t nsample, void* stream) {
   return dfg_lut_launch(lut, size, nsample, static_cast<cudaStream_t>(stream));
 }

@@ -59,6 +59,14 @@ int unpool_add_grad_launch(const float* dskip, const float* dpool, const uint16_
                            int32_t w, int32_t c, cudaStream_t st);
 int adam_launch(float* param, float* grad, float* m, float* v, uint16_t* copy, uint16_t* flip, int64_t n, int32_t cout, int32_t cin,
                 float lr, float beta1, float beta2, float eps, int32_t step, cudaStream_t st);
+int newton_sync_poses_launch(const float* body_q, int32_t nbody, const int32_t* shape_body, const float* shape_transform,
+                             int32_t nshape, const int32_t* geom_shape, int32_t geom_shape_rows, const float* geom_offset,
+                             const float* camera_transforms, int32_t nworld, int32_t ngeom, int32_t ncam, int32_t cam,
+                             float* geom_xpos, float* geom_xmat, float* cam_xpos, float* cam_xmat, int32_t* error_word,
+                             cudaStream_t stream);
+int newton_images_launch(const MjpbrScene& s, int32_t cam, const int32_t* geom_shape, int32_t geom_shape_rows,
+                         const float* ray_scale, uint32_t* color, float* depth, float* forward_depth, uint32_t* shape_index,
+                         float* hdr, cudaStream_t stream);
 int gemm_bf16_launch(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                      cudaStream_t stream);
 

@@ -36,6 +36,7 @@ constexpr float kPi = 3.14159265358979323846f;
 constexpr int32_t kErrStackOverflow = 1;
 constexpr int32_t kErrWorkQueue = 2;
 constexpr int32_t kErrWaitTimeout = 4;
+constexpr int32_t kErrPoseIndex = 8;  // a pose input named a body or shape out of range (skipped)
 // Most traversal stack entries per ray (settings.stack_depth sizes a launch's stacks, at most this).
 constexpr int32_t kStackDepth = 32;
 

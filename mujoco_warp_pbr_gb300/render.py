@@ -388,7 +388,7 @@ def check_errors(rc: PbrRenderContext) -> int:
   """Synchronises and returns (then clears) the error bits kernels reported (0: none).
 
   Bit 1: a traversal stack overflowed. Bit 2: the work queue was inconsistent. Bit 4: a bounded
-  wait gave up."""
+  wait gave up. Bit 8: the Newton adapter's pose step met a shape or body index out of range."""
   value = int(rc.error_word.item())
   rc.error_word.zero_()
   return value

@@ -154,8 +154,10 @@ class Builder:
     self.cams.append({"pos": pos, "mat": mat, "fovy": fovy, "res": resolution, "proj": int(orthographic)})
     return len(self.cams) - 1
 
-  def mesh(self, vert: np.ndarray, face: np.ndarray, normal: np.ndarray | None = None, texcoord: np.ndarray | None = None) -> int:
-    self.meshes.append({"vert": np.asarray(vert, np.float32), "face": np.asarray(face, np.int32), "normal": normal, "texcoord": texcoord})
+  def mesh(self, vert: np.ndarray, face: np.ndarray, normal: np.ndarray | None = None, texcoord: np.ndarray | None = None, facenormal: np.ndarray | None = None) -> int:
+    """A triangle mesh; normal: per-vertex normals (None: area-weighted vertex normals), or with
+    facenormal (nface, 3) the normal index of each face corner."""
+    self.meshes.append({"vert": np.asarray(vert, np.float32), "face": np.asarray(face, np.int32), "normal": normal, "texcoord": texcoord, "facenormal": facenormal})
     return len(self.meshes) - 1
 
   def hfield(self, elevation: np.ndarray, size: Any) -> int:
@@ -187,7 +189,7 @@ class Builder:
       verts.append(v)
       faces.append(f)
       normals.append(n.astype(np.float32))
-      facenormals.append(f)
+      facenormals.append(f if m.get("facenormal") is None else np.asarray(m["facenormal"], np.int32))
       if m["texcoord"] is not None:
         tadr.append(nt)
         tcs.append(np.asarray(m["texcoord"], np.float32))
