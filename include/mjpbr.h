@@ -33,6 +33,7 @@
  *   mjpbr_build_scene_bvh  scene BVH build of mujoco_warp.create_render_context (third party; called at
  *                                                                          mujoco_warp_pbr/_src/io.py:511-528)
  *   mjpbr_build_mesh_bvh   per-mesh BVH build (warp.Mesh, mujoco_warp_pbr/_src/io.py:164-179,198-203)
+ *   mjpbr_build_mesh_bvh_device  GPU mesh BVH builds of warp.Mesh (mujoco_warp_pbr/_src/io.py:164-179)
  *   mjpbr_newton_sync_poses   newton_pbr ScenePoses.sync                  (newton-pbr/newton_pbr/_render.py:31-131)
  *   mjpbr_newton_images       newton_pbr SensorPbrCamera output copy      (newton-pbr/newton_pbr/sensor.py:45-86,247-265)
  */
@@ -581,6 +582,26 @@ int mjpbr_build_scene_bvh(const float* lower, const float* upper, int32_t nprim,
  * Returns the number of nodes written in *nnode_out. */
 int mjpbr_build_mesh_bvh(const float* vert, int32_t nvert, const int32_t* face, int32_t nface, int32_t leaf_size,
                          float* nodes_out, float* tris_out, float* bounds_out, int32_t* nnode_out);
+
+/* Device scratch bytes of mjpbr_build_mesh_bvh_device for nsrc sources of nface faces in all
+ * (-1 for nsrc < 1 or nface < nsrc). */
+int64_t mjpbr_mesh_bvh_device_scratch_bytes(int32_t nsrc, int32_t nface);
+
+/* Device: linear BVHs (Morton-ordered radix trees, subtrees of at most leaf_size triangles as
+ * leaves) of nsrc triangle meshes at once, in the records of mjpbr_build_mesh_bvh. Sources are
+ * concatenated: source s has faces [face_base[s], face_base[s + 1]) of face (nface, 3), whose
+ * vertex indices are local (< vert_num[s]) to the vertices from vert_base[s] of vert (*, 3);
+ * every source needs at least one face. Source s's nodes go to nodes from row node_base[s]
+ * (capacity mjpbr_bvh_node_count(its faces)), its triangles to tris rows [face_base[s],
+ * face_base[s + 1]) in leaf order (leaf refs are relative to face_base[s]), its AABB to
+ * bounds[s] (6), its node count to nnode[s]. All arrays (and scratch) device memory; a face
+ * naming a vertex out of range is clamped and ORs 16 into *error_word. Stands in for the GPU
+ * mesh BVH builds of Warp (wp.Mesh bvh_constructor "lbvh" / "cubql",
+ * mujoco_warp_pbr/_src/io.py:164-179). */
+int mjpbr_build_mesh_bvh_device(const float* vert, const int32_t* face, const int32_t* vert_base, const int32_t* vert_num,
+                                const int32_t* face_base, const int32_t* node_base, int32_t nsrc, int32_t nface, int32_t leaf_size,
+                                float* nodes, float* tris, float* bounds, int32_t* nnode, void* scratch, int64_t scratch_bytes,
+                                int32_t* error_word, void* stream);
 
 #ifdef __cplusplus
 }

@@ -467,12 +467,8 @@ def hfield_mesh(mjm: Any, h: int) -> tuple[np.ndarray, np.ndarray]:
   return vert, face
 
 
-def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
-  """Triangle BVHs concatenated, one per mesh, then one per height field (hfield_mesh): nodes
-  (nnode, 16), tris (ntri, 12), root / tri_base per BVH, local AABBs (nmesh + nhfield, 6)."""
-  lib = _lib.load()
-  nodes, tris, roots, bases, bounds, nfaces, levels = [], [], [], [], [], [], []
-  node_total = tri_total = 0
+def mesh_sources(mjm: Any) -> list[tuple[str, np.ndarray, np.ndarray]]:
+  """(name, vertices, faces) of every triangle BVH: one per mesh, then one per height field."""
   vert_all = np.asarray(mjm.mesh_vert, np.float32).reshape(-1, 3)
   face_all = np.asarray(mjm.mesh_face, np.int32).reshape(-1, 3)
   sources = []
@@ -482,6 +478,17 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
     sources.append((f"mesh {m}", vert_all[v0 : v0 + nv], face_all[f0 : f0 + nf]))
   for h in range(nhfield_of(mjm)):
     sources.append((f"height field {h}", *hfield_mesh(mjm, h)))
+  return sources
+
+
+def build_mesh_bvhs(mjm: Any, sources: list[tuple[str, np.ndarray, np.ndarray]] | None = None) -> dict[str, Any]:
+  """Triangle BVHs concatenated, one per mesh, then one per height field (hfield_mesh), built on
+  the host with binned SAH: nodes (nnode, 16), tris (ntri, 12), root / tri_base per BVH, local
+  AABBs (nmesh + nhfield, 6)."""
+  lib = _lib.load()
+  nodes, tris, roots, bases, bounds, nfaces, levels = [], [], [], [], [], [], []
+  node_total = tri_total = 0
+  sources = mesh_sources(mjm) if sources is None else sources
   for name, vert, face in sources:
     vert = np.ascontiguousarray(vert, np.float32)
     face = np.ascontiguousarray(face, np.int32)
@@ -511,9 +518,102 @@ def build_mesh_bvhs(mjm: Any) -> dict[str, Any]:
     "blas_root": np.array(roots, np.int32) if roots else None,
     "blas_tri_base": np.array(bases, np.int32) if bases else None,
     "mesh_bounds": np.stack(bounds).astype(np.float32) if bounds else None,
-    "mesh_nface": nfaces[: mjm.nmesh],
-    "nhfield": nhfield_of(mjm),
+    "mesh_nface": nfaces[: mjm.nmesh] if mjm is not None else nfaces,
+    "nhfield": nhfield_of(mjm) if mjm is not None else 0,
     "mesh_levels": max(levels) if levels else 0,
+  }
+
+
+def device_mesh_sources(mjm: Any) -> dict[str, Any]:
+  """The triangle BVH sources concatenated for the device builder (mjpbr_build_mesh_bvh_device):
+  vertices, faces with source-local vertex indices, per-source vertex base / count, face base
+  (nsrc + 1) and node base (node capacities mjpbr_bvh_node_count(nface) in order), plus what
+  the host needs before the build: the sources' AABBs (of the vertices their faces use) and
+  face counts.
+
+  Raises:
+    ValueError: for a source without faces or a face naming a vertex out of range.
+  """
+  sources = mesh_sources(mjm)
+  nface = np.array([len(f) for _, _, f in sources], np.int64)
+  nvert = np.array([len(v) for _, v, _ in sources], np.int64)
+  bounds = np.zeros((len(sources), 6), np.float32)
+  for i, (name, vert, face) in enumerate(sources):
+    if len(face) == 0 or np.any(face < 0) or np.any(face >= len(vert)):
+      raise ValueError(f"{name}: BVH build failed (a face names a vertex out of range, or there are no faces)")
+    used = vert[face.reshape(-1)]
+    bounds[i, :3], bounds[i, 3:] = used.min(axis=0), used.max(axis=0)
+  cap = np.maximum(nface - 1, 1)
+  return {
+    "device_sources": {
+      "vert": np.ascontiguousarray(np.concatenate([v for _, v, _ in sources]), np.float32),
+      "face": np.ascontiguousarray(np.concatenate([f for _, _, f in sources]), np.int32),
+      "vert_base": np.concatenate([[0], np.cumsum(nvert)[:-1]]).astype(np.int32),
+      "vert_num": nvert.astype(np.int32),
+      "face_base": np.concatenate([[0], np.cumsum(nface)]).astype(np.int32),
+      "node_base": np.concatenate([[0], np.cumsum(cap)[:-1]]).astype(np.int32),
+      "nodes": int(cap.sum()),
+      "names": [n for n, _, _ in sources],
+    },
+    "mesh_bounds": bounds,
+    "mesh_nface": [int(n) for n in nface[: mjm.nmesh]],
+    "nhfield": nhfield_of(mjm),
+    "mesh_levels": None,
+  }
+
+
+MESH_BVH_LEAF = 4  # triangles per leaf of the mesh BVHs
+
+
+def _source_arrays(src: dict[str, Any], i: int) -> tuple[np.ndarray, np.ndarray]:
+  v0, nv = int(src["vert_base"][i]), int(src["vert_num"][i])
+  f0, f1 = int(src["face_base"][i]), int(src["face_base"][i + 1])
+  return src["vert"][v0 : v0 + nv], src["face"][f0:f1]
+
+
+def build_mesh_bvhs_device(src: dict[str, Any], device: torch.device) -> dict[str, Any]:
+  """Runs the device BVH builder over device_mesh_sources' arrays: blas_nodes / blas_tris /
+  blas_root / blas_tri_base / mesh_bounds as device tensors and mesh_levels (the deepest tree's
+  inner levels, read back for the traversal stack size)."""
+  i32 = torch.int32
+
+  def dev(a: np.ndarray, dtype: torch.dtype) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device=device, dtype=dtype)
+
+  lib = _lib.load()
+  nsrc = len(src["vert_num"])
+  nface = int(src["face_base"][-1])
+  vert, face = dev(src["vert"], torch.float32), dev(src["face"], i32)
+  vert_base, vert_num = dev(src["vert_base"], i32), dev(src["vert_num"], i32)
+  face_base, node_base = dev(src["face_base"], i32), dev(src["node_base"], i32)
+  nodes = torch.zeros((src["nodes"], 16), dtype=torch.float32, device=device)
+  tris = torch.zeros((nface, 12), dtype=torch.float32, device=device)
+  bounds = torch.zeros((nsrc, 6), dtype=torch.float32, device=device)
+  nnode = torch.zeros(nsrc, dtype=i32, device=device)
+  err = torch.zeros(1, dtype=i32, device=device)
+  nbytes = int(lib.mjpbr_mesh_bvh_device_scratch_bytes(nsrc, nface))
+  scratch = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
+  stream = torch.cuda.current_stream(device).cuda_stream
+  _lib.call(
+    "mjpbr_build_mesh_bvh_device",
+    vert.data_ptr(), face.data_ptr(), vert_base.data_ptr(), vert_num.data_ptr(), face_base.data_ptr(), node_base.data_ptr(),
+    nsrc, nface, MESH_BVH_LEAF, nodes.data_ptr(), tris.data_ptr(), bounds.data_ptr(), nnode.data_ptr(), scratch.data_ptr(), nbytes,
+    err.data_ptr(), stream,
+  )
+  host_nodes = nodes.cpu().numpy()
+  counts = nnode.cpu().numpy()
+  if int(err.item()) != 0:
+    raise ValueError("device BVH build: a face names a vertex out of range")
+  base = src["node_base"]
+  levels = max(mesh_tree_levels(host_nodes[base[i] : base[i] + counts[i]]) for i in range(nsrc))
+  return {
+    "blas_nodes": nodes,
+    "blas_tris": tris,
+    "blas_root": node_base,
+    "blas_tri_base": face_base[:nsrc].contiguous(),
+    "mesh_bounds": bounds,
+    "mesh_levels": int(levels),
+    "node_count": counts,
   }
 
 
@@ -801,7 +901,12 @@ def prepare_context(
     return xpos, xmat.reshape(ngeom, 9)
 
   # ---- meshes, scene BVH topology
-  meshes = build_mesh_bvhs(mjm) if mjm.nmesh or nhfield_of(mjm) else {"mesh_nface": [], "mesh_bounds": None, "nhfield": 0}
+  if not (mjm.nmesh or nhfield_of(mjm)):
+    meshes = {"mesh_nface": [], "mesh_bounds": None, "nhfield": 0}
+  elif mesh_bvh_constructor == "lbvh":
+    meshes = device_mesh_sources(mjm)  # built on the GPU by upload_context
+  else:
+    meshes = build_mesh_bvhs(mjm)
   enabled = np.nonzero(rendered)[0].astype(np.int32)
   geom_types = np.asarray(mjm.geom_type).reshape(-1)
   supported = np.isin(geom_types[enabled], [GEOM_PLANE, GEOM_SPHERE, GEOM_CAPSULE, GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH, GEOM_SDF, GEOM_HFIELD])
@@ -824,6 +929,7 @@ def prepare_context(
     xmat_all = np.asarray(host_data.geom_xmat, np.float64).reshape(xpos_all.shape[0], ngeom, 9)
     lo_all, hi_all = geom_aabbs_all(mjm, xpos_all[:nworld], xmat_all[:nworld], meshes.get("mesh_bounds"))
     topo = np.stack([build_scene_topology(lo_all[w][enabled], hi_all[w][enabled]) for w in range(nworld)])
+  meshes["scene_levels"] = scene_tree_levels(topo)
   nbvh = len(enabled)
   nnode = topo.shape[1]
   lib = _lib.load()
@@ -889,7 +995,7 @@ def prepare_context(
     "max_depth": int(max_depth),
     "rr_depth": int(rr_depth),
     "denoise": int(bool(denoise)),
-    "stack_depth": traversal_stack_depth(scene_tree_levels(topo), int(meshes.get("mesh_levels", 0))),
+    "stack_depth": traversal_stack_depth(scene_tree_levels(topo), int(meshes.get("mesh_levels") or 0)),
     "znear": float(getattr(mjm, "znear", 0.01)),
     "zfar": float(getattr(mjm, "zfar", 0.0)),
     "shadow_light_fraction": float(shadow_light_fraction),
@@ -1075,6 +1181,19 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     tex_desc = hc.textures.desc
   env = envmap_lib.upload_environments(hc.environments, device) if hc.environments is not None else None
   st = hc.settings
+  blas = {k: _dev(m.get(k), device) for k in ("mesh_bounds", "blas_nodes", "blas_tris", "blas_root", "blas_tri_base")}
+  if "device_sources" in m:
+    built = build_mesh_bvhs_device(m["device_sources"], device)
+    try:
+      st["stack_depth"] = traversal_stack_depth(m["scene_levels"], built["mesh_levels"])
+      blas = {k: built[k] for k in blas}
+    except ValueError:
+      # linear BVHs of degenerate meshes can be deeper than the traversal stacks: binned SAH instead
+      warnings.warn("mesh_bvh_constructor='lbvh': a mesh BVH is too deep for the traversal stack; built with binned SAH on the host", stacklevel=3)
+      names = m["device_sources"]["names"]
+      sah = build_mesh_bvhs(None, [(n, *_source_arrays(m["device_sources"], i)) for i, n in enumerate(names)])
+      st["stack_depth"] = traversal_stack_depth(m["scene_levels"], int(sah["mesh_levels"]))
+      blas = {k: _dev(sah.get(k), device) for k in blas}
   rc = PbrRenderContext(
     nworld=nworld,
     base=out,
@@ -1130,11 +1249,11 @@ def upload_context(hc: HostContext, device: torch.device) -> PbrRenderContext:
     tlas_child=_dev(hc.tlas_child, device),
     world_blocks=torch.zeros((nworld, hc.world_block_floats), dtype=f32, device=device),
     world_block_floats=hc.world_block_floats,
-    mesh_bounds=_dev(m.get("mesh_bounds"), device),
-    blas_nodes=_dev(m.get("blas_nodes"), device),
-    blas_tris=_dev(m.get("blas_tris"), device),
-    blas_root=_dev(m.get("blas_root"), device),
-    blas_tri_base=_dev(m.get("blas_tri_base"), device),
+    mesh_bounds=blas["mesh_bounds"],
+    blas_nodes=blas["blas_nodes"],
+    blas_tris=blas["blas_tris"],
+    blas_root=blas["blas_root"],
+    blas_tri_base=blas["blas_tri_base"],
     mesh_nface=list(m.get("mesh_nface", [])),
     nhfield=int(m.get("nhfield", 0)),
     textures=textures,

@@ -236,6 +236,16 @@ int mjpbr_newton_images(const MjpbrScene* scene, int32_t cam, const int32_t* geo
                               hdr, static_cast<cudaStream_t>(stream));
 }
 
+int64_t mjpbr_mesh_bvh_device_scratch_bytes(int32_t nsrc, int32_t nface) { return lbvh_scratch_bytes(nsrc, nface); }
+
+int mjpbr_build_mesh_bvh_device(const float* vert, const int32_t* face, const int32_t* vert_base, const int32_t* vert_num,
+                                const int32_t* face_base, const int32_t* node_base, int32_t nsrc, int32_t nface, int32_t leaf_size,
+                                float* nodes, float* tris, float* bounds, int32_t* nnode, void* scratch, int64_t scratch_bytes,
+                                int32_t* error_word, void* stream) {
+  return build_mesh_bvh_device_launch(vert, face, vert_base, vert_num, face_base, node_base, nsrc, nface, leaf_size, nodes, tris,
+                                      bounds, nnode, scratch, scratch_bytes, error_word, static_cast<cudaStream_t>(stream));
+}
+
 int mjpbr_dfg_lut(float* lut, int32_t size, int32_t nsample, void* stream) {
   return dfg_lut_launch(lut, size, nsample, static_cast<cudaStream_t>(stream));
 }

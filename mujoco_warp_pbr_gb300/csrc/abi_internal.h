@@ -67,6 +67,11 @@ int newton_sync_poses_launch(const float* body_q, int32_t nbody, const int32_t* 
 int newton_images_launch(const MjpbrScene& s, int32_t cam, const int32_t* geom_shape, int32_t geom_shape_rows,
                          const float* ray_scale, uint32_t* color, float* depth, float* forward_depth, uint32_t* shape_index,
                          float* hdr, cudaStream_t stream);
+int64_t lbvh_scratch_bytes(int32_t nsrc, int32_t nface);
+int build_mesh_bvh_device_launch(const float* vert, const int32_t* face, const int32_t* vert_base, const int32_t* vert_num,
+                                 const int32_t* face_base, const int32_t* node_base, int32_t nsrc, int32_t nface,
+                                 int32_t leaf_size, float* nodes, float* tris, float* bounds, int32_t* nnode, void* scratch,
+                                 int64_t scratch_bytes, int32_t* error_word, cudaStream_t st);
 int gemm_bf16_launch(const uint16_t* a, const uint16_t* b, float* d, int32_t m, int32_t n, int32_t k, int32_t* error_word,
                      cudaStream_t stream);
 

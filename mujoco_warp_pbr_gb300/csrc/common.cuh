@@ -37,6 +37,7 @@ constexpr int32_t kErrStackOverflow = 1;
 constexpr int32_t kErrWorkQueue = 2;
 constexpr int32_t kErrWaitTimeout = 4;
 constexpr int32_t kErrPoseIndex = 8;  // a pose input named a body or shape out of range (skipped)
+constexpr int32_t kErrBvhInput = 16;  // a BVH build face named a vertex outside its mesh (clamped)
 // Most traversal stack entries per ray (settings.stack_depth sizes a launch's stacks, at most this).
 constexpr int32_t kStackDepth = 32;
 
