@@ -563,6 +563,21 @@ def device_mesh_sources(mjm: Any) -> dict[str, Any]:
 
 
 MESH_BVH_LEAF = 4  # triangles per leaf of the mesh BVHs
+# With the default constructor ("cubql", the reference's GPU builder), models with at least this many
+# mesh and height-field triangles build their BVHs on the GPU (linear BVHs, tens of ms for millions of
+# triangles); smaller ones use the host's binned SAH, whose trees render about 5 % faster and build in
+# well under 100 ms at this size. "sah" always builds on the host, "lbvh" always on the GPU.
+DEVICE_BVH_FACES = 1 << 17
+
+
+def total_bvh_faces(mjm: Any) -> int:
+  """Triangles of every mesh and height-field BVH (hfield_mesh of r x c samples: 2 (r - 1)(c - 1)
+  top triangles, and per border segment two side triangles and one of the base)."""
+  n = int(np.sum(np.asarray(mjm.mesh_facenum))) if mjm.nmesh else 0
+  for h in range(nhfield_of(mjm)):
+    r, c = int(mjm.hfield_nrow[h]), int(mjm.hfield_ncol[h])
+    n += 2 * (r - 1) * (c - 1) + 3 * (2 * (r - 1) + 2 * (c - 1))
+  return n
 
 
 def _source_arrays(src: dict[str, Any], i: int) -> tuple[np.ndarray, np.ndarray]:
@@ -903,7 +918,7 @@ def prepare_context(
   # ---- meshes, scene BVH topology
   if not (mjm.nmesh or nhfield_of(mjm)):
     meshes = {"mesh_nface": [], "mesh_bounds": None, "nhfield": 0}
-  elif mesh_bvh_constructor == "lbvh":
+  elif mesh_bvh_constructor == "lbvh" or (mesh_bvh_constructor == "cubql" and total_bvh_faces(mjm) >= DEVICE_BVH_FACES):
     meshes = device_mesh_sources(mjm)  # built on the GPU by upload_context
   else:
     meshes = build_mesh_bvhs(mjm)

@@ -200,3 +200,25 @@ def test_lbvh_context_renders_like_the_oracle():
   np.testing.assert_array_equal(gpu_img["seg"], sah["seg"])
   np.testing.assert_array_equal(gpu_img["depth"], sah["depth"])
   assert helpers.rgb_diff(gpu_img["rgb"], sah["rgb"]).max() <= 1
+
+
+def test_default_constructor_builds_large_models_on_the_device():
+  for grid in (2, 5, 33):
+    sc = synthetic.hfield_scene(seed=0, nworld=1, res=8, grid=grid)
+    faces = sum(len(f) for _, _, f in context.mesh_sources(sc.mjm))
+    assert context.total_bvh_faces(sc.mjm) == faces
+  small = synthetic.mesh_ibl_scene(seed=0, nworld=1, res=8, tex_size=16, env_width=32)
+  hc = context.prepare_context(small.mjm, 1, data=small.mjd, **{**small.options, "envmap": None})
+  assert "device_sources" not in hc.meshes and hc.meshes["blas_nodes"] is not None
+  v, f = synthetic.icosphere(7)
+  b = synthetic.Builder()
+  b.mesh(v, f, normal=v.astype(np.float32))
+  b.geom(synthetic.GEOM_MESH, (1, 1, 1), dataid=0)
+  b.light(synthetic.LIGHT_DIRECTIONAL)
+  b.camera((0, -3, 1), (0, 0, 0))
+  mjm, mjd = b.build()
+  assert context.total_bvh_faces(mjm) >= context.DEVICE_BVH_FACES
+  hc = context.prepare_context(mjm, 1, data=mjd)
+  assert "device_sources" in hc.meshes
+  hc = context.prepare_context(mjm, 1, data=mjd, mesh_bvh_constructor="sah")
+  assert "device_sources" not in hc.meshes
