@@ -398,3 +398,35 @@ def test_static_model_without_bodies():
   torch.cuda.synchronize()
   got = np.unique(index.cpu().numpy())
   assert set(got.tolist()) <= {0, 1, 0xFFFFFFFF} and 1 in got
+
+
+@pytest.mark.gpu
+@gpu
+def test_image_step_throughput():
+  """The image step is a stream over the render buffers: 28 bytes read and 28 written per pixel.
+  Timed alone with CUDA events (L2 flushed before each launch) at 1024 worlds x 128x128 (0.94 GB per
+  launch); the floor is loose (1 TB/s), the measured figure is printed."""
+  from mujoco_warp_pbr_gb300 import _lib
+  from mujoco_warp_pbr_gb300.render import scene as scene_descriptor
+
+  nworld, res = 1024, 128
+  model, state, cams = _scene(nworld=nworld)
+  camera = newton_pbr.SensorPbrCamera(model, width=res, height=res, fovy=_FOVY, newton=nf.newton)
+  out = [camera.allocate_image_color(), camera.allocate_image_depth(), camera.allocate_image_depth(), camera.allocate_image_shape_index(), camera.allocate_image_color_hdr()]
+  camera.update(state, cams, color_image=out[0], depth_image=out[1], forward_depth_image=out[2], shape_index_image=out[3], hdr_color_image=out[4])
+  sc = scene_descriptor(camera.m, camera.d, camera.rc)
+  stream = torch.cuda.current_stream().cuda_stream
+  flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+  times = []
+  for _ in range(10):
+    flush.zero_()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    _lib.call("mjpbr_newton_images", sc, 0, camera.geom_shape.data_ptr(), 1 if camera.geom_shape.shape[0] == 1 else nworld, camera.ray_scale.data_ptr(), *(o.data_ptr() for o in out), stream)
+    b.record()
+    torch.cuda.synchronize()
+    times.append(a.elapsed_time(b))
+  ms = float(np.median(times))
+  gbs = nworld * res * res * 56 / (ms * 1e-3) / 1e9
+  print(f"newton image step: {ms:.3f} ms for {nworld} x {res}^2, {gbs:.0f} GB/s")
+  assert gbs > 1000.0
