@@ -150,6 +150,24 @@ def test_mesh_ibl_scene_matches_oracle(seed):
 
 @pytest.mark.gpu
 @pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+def test_large_path_configuration_matches_oracle():
+  """The large path-traced configuration's features at a small size: two cameras per world, four
+  environments chosen per world (env_id) with per-world rotations, per-world materials and
+  emission, 2 spp, depth 4."""
+  from mujoco_warp_pbr_gb300 import synthetic
+  from tests import helpers
+
+  sc = synthetic.large_path_scene(seed=2, nworld=6, res=24, env_width=128)
+  assert len(sc.options["envmap"]) == 4 and len(set(sc.per_world["env_id"].tolist())) > 1
+  opts = dict(path_samples=2, **PATH)
+  m, d, rc = helpers.gpu_scene(sc, **opts)
+  gpu = helpers.render_gpu(m, d, rc, seed=6)
+  ref = helpers.oracle_render(sc, seed=6, tables=helpers.gpu_tables(rc), **opts)
+  _assert_path_parity(gpu, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
 def test_tiles_cover_ragged_cameras():
   """Two cameras whose sizes are not multiples of the 32-pixel tile, one without RGB."""
   from tests import helpers
