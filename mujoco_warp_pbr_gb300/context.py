@@ -1144,9 +1144,12 @@ def create_render_context(mjm: Any, nworld: int = 1, **kwargs: Any) -> PbrRender
   topology is built from (default: every geom at the origin, refit each frame); `schedule`, the
   real-time tier's launch: "grid", "queue" (with `queue_item` pixels per work item) or
   "wavefront" (staged kernels over ray queues; `wave_chunk_worlds` worlds per chunk of its
-  scratch, 0: about 64 M camera samples / 32 M paths per chunk); all render the same images. block_dim,
-  max_registers, ordered_traversal, use_fast_math, mesh_bvh_constructor and mesh_bvh_frame are
-  validated and recorded; the GB300 kernels choose their own launch shapes and traversal.
+  scratch, 0: about 64 M camera samples / 32 M paths per chunk); all render the same images.
+  mesh_bvh_constructor places the mesh BVH build: "lbvh" on the GPU (linear BVHs), "sah" on the
+  host (binned SAH), "cubql" (default) on the GPU for models of DEVICE_BVH_FACES triangles or more
+  and on the host below. block_dim, max_registers, ordered_traversal, use_fast_math and
+  mesh_bvh_frame are validated and recorded; the GB300 kernels choose their own launch shapes and
+  traversal.
 
   Raises:
     ValueError: for invalid arguments, or a model with nothing to render.
