@@ -208,7 +208,7 @@ typedef struct MjpbrSettings {
  * features the settings switch off may be NULL. */
 typedef struct MjpbrScene {
   int32_t abi_version;       /* MJPBR_ABI_VERSION */
-  int32_t nworld;
+  int32_t nworld;            /* 1 .. 2^24 */
   int32_t ngeom;
   int32_t nmat;
   int32_t nlight;

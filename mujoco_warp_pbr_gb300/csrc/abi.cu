@@ -66,7 +66,7 @@ int validate_scene(const MjpbrScene* s, bool need_outputs) {
   if (s->settings.schedule < MJPBR_SCHEDULE_GRID || s->settings.schedule > MJPBR_SCHEDULE_WAVEFRONT) {
     return set_error(MJPBR_ERR_ARG, "settings.schedule must be 0 (grid), 1 (queue) or 2 (wavefront), got %d", s->settings.schedule);
   }
-  if (s->nworld < 1 || s->nworld > 65535) return set_error(MJPBR_ERR_ARG, "nworld must be in [1, 65535], got %d", s->nworld);
+  if (s->nworld < 1 || s->nworld > kMaxWorlds) return set_error(MJPBR_ERR_ARG, "nworld must be in [1, %d], got %d", kMaxWorlds, s->nworld);
   if (s->nrender < 1 || s->nrender > MJPBR_MAX_RENDER) {
     return set_error(MJPBR_ERR_ARG, "nrender must be in [1, %d], got %d", MJPBR_MAX_RENDER, s->nrender);
   }

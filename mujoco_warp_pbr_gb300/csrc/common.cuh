@@ -38,6 +38,10 @@ constexpr int32_t kErrWorkQueue = 2;
 constexpr int32_t kErrWaitTimeout = 4;
 constexpr int32_t kErrPoseIndex = 8;  // a pose input named a body or shape out of range (skipped)
 constexpr int32_t kErrBvhInput = 16;  // a BVH build face named a vertex outside its mesh (clamped)
+// Most worlds of one scene (grids of more than kMaxGridWorlds worlds are split into launches).
+constexpr int32_t kMaxWorlds = 1 << 24;
+// Most worlds one launch puts in grid y (CUDA's limit on gridDim.y); more worlds take more launches.
+constexpr int32_t kMaxGridWorlds = 65535;
 // Most traversal stack entries per ray (settings.stack_depth sizes a launch's stacks, at most this).
 constexpr int32_t kStackDepth = 32;
 

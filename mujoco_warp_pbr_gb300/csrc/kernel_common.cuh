@@ -8,6 +8,7 @@ namespace mjpbr {
 
 // Tiles of every rendering camera of a world, in camera order.
 struct TileMap {
+  int32_t w0;  // first world of the launch (launches cover at most kMaxGridWorlds worlds in grid y)
   int32_t ncam;
   int32_t tile_w, tile_h;
   int32_t tiles_x[MJPBR_MAX_RENDER];

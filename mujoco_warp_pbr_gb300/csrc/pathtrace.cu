@@ -205,7 +205,9 @@ int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
     tm.tile_base[c + 1] = tm.tile_base[c] + (any ? tm.tiles_x[c] * ty : 0);
   }
   tm.tiles_per_world = tm.tile_base[s.nrender];
-  tm.total = tm.tiles_per_world * s.nworld;
+  const int64_t total = (int64_t)tm.tiles_per_world * s.nworld;
+  if (total > INT32_MAX) return set_error(MJPBR_ERR_ARG, "path tracer: %lld tiles exceed the work counter", (long long)total);
+  tm.total = (int32_t)total;
   if (tm.total == 0) return MJPBR_OK;
   bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;

@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
                                                                            const __grid_constant__ TileMap tm) {
   extern __shared__ __align__(16) float smem[];
   float* blk = smem;
-  const int32_t w = blockIdx.y;
+  const int32_t w = tm.w0 + blockIdx.y;
   stage_world_block(s, w, blk, kThreads);
   __syncthreads();
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
@@ -421,9 +421,15 @@ int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaSt
     if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render: world block of %zu bytes: %s", smem, cudaGetErrorString(e));
     smem_set = smem;
   }
-  dim3 grid(tm.tile_base[tm.ncam], s.nworld);
-  kern<<<grid, kThreads, smem, stream>>>(s, seed, tm);
-  return check_launch("rt_kernel");
+  TileMap part = tm;
+  for (int32_t w0 = 0; w0 < s.nworld; w0 += kMaxGridWorlds) {
+    part.w0 = w0;
+    const dim3 grid(tm.tile_base[tm.ncam], std::min(kMaxGridWorlds, s.nworld - w0));
+    kern<<<grid, kThreads, smem, stream>>>(s, seed, part);
+    const int rc = check_launch("rt_kernel");
+    if (rc) return rc;
+  }
+  return MJPBR_OK;
 }
 
 template <bool kMesh, bool kTex>
@@ -487,6 +493,7 @@ int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
     return render_rt_queue(s, seed, stream);
   }
   TileMap tm;
+  tm.w0 = 0;
   tm.ncam = s.nrender;
   if (s.settings.render_order == MJPBR_ORDER_ROW) {
     tm.tile_w = 32;

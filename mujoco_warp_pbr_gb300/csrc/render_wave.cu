@@ -687,6 +687,7 @@ int64_t layout(WaveMap* wm, char* base, int32_t worlds, int32_t per_world, int32
 
 TileMap tile_map(const MjpbrScene& s, bool rgb_only) {
   TileMap tm;
+  tm.w0 = 0;  // the stages take their chunk's first world from the WaveMap
   tm.ncam = s.nrender;
   tm.tile_w = kTile;
   tm.tile_h = kTile;
@@ -814,8 +815,9 @@ int render_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) 
   if (!s.wave_scratch || (reinterpret_cast<uintptr_t>(s.wave_scratch) & 255u)) {
     return set_error(MJPBR_ERR_ARG, "the wavefront schedule needs wave_scratch (256-byte aligned)");
   }
-  // worlds per chunk: as many as the scratch holds, and sample / target indices within int32
-  int32_t chunk = s.nworld;
+  // worlds per chunk: as many as the scratch holds, sample / target indices within int32, and at
+  // most kMaxGridWorlds (the stages put a chunk's worlds in grid y)
+  int32_t chunk = std::min(s.nworld, kMaxGridWorlds);
   if (per_world > 0) {
     const int64_t nl2 = 2 * (int64_t)std::max(s.nlight, 1);
     chunk = (int32_t)std::min<int64_t>(chunk, (INT32_MAX / nl2) / per_world);

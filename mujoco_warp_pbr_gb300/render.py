@@ -277,6 +277,8 @@ def scene(m: Any, d: Any, rc: PbrRenderContext) -> _lib.Scene:
 # wave_chunk_worlds is 0: queues of about 21 GB (mesh / IBL scene, two lights) and 13 GB (path
 # scene), a few per cent faster than chunks of a quarter of that (fewer launches and launch tails)
 WAVE_CHUNK_SAMPLES = 1 << 26
+# worlds one launch of the real-time kernels covers (CUDA's gridDim.y limit; more take more launches)
+MAX_GRID_WORLDS = 65535
 WAVE_CHUNK_PATHS = 1 << 25
 
 
@@ -295,6 +297,8 @@ def _ensure_wave_scratch(rc: PbrRenderContext, struct: _lib.Scene) -> bool:
     chunk_units, units = WAVE_CHUNK_PATHS, pixels * int(rc.path_samples)
   chunk = rc.wave_chunk_worlds or max(1, chunk_units // max(units, 1))
   chunk = min(chunk, int(rc.base.rgb_data.shape[0]))
+  if rc.tier == 0:
+    chunk = min(chunk, MAX_GRID_WORLDS)  # the real-time stages put a chunk's worlds in grid y
   need = int(lib.mjpbr_wave_scratch_bytes(struct, chunk))
   if need < 0 or per_world < 0:
     raise ValueError("the wavefront schedule cannot render this scene")

@@ -103,3 +103,28 @@ def test_path_traced_edge_case_matches_oracle(case):
   np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
   diff = helpers.rgb_diff(gpu["rgb"], ref["rgb"])
   assert float(np.mean(diff <= 1)) >= 0.995
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("schedule", ["grid", "wavefront"])
+@pytest.mark.parametrize("tier", [0, 1])
+def test_more_worlds_than_one_grid_dimension(schedule, tier):
+  """70,000 worlds of 8x8 pixels: more than CUDA's 65,535 blocks in grid y, where the real-time grid
+  and wavefront schedules put the worlds (the launches cover them in batches; the path tier's
+  launches are one-dimensional). The last worlds match the oracle at the real-time bars."""
+  from oracle import oracle
+
+  nworld = 70000
+  sc = synthetic.primitive_scene(seed=9, nworld=nworld, res=8, shadow_samples=1)
+  opts = {"tier": tier, "path_samples": 2, "max_depth": 2} if tier else {}
+  m, d, rc = helpers.gpu_scene(sc, schedule=schedule, **opts)
+  gpu = helpers.render_gpu(m, d, rc, seed=2)
+  o = oracle.OracleScene(sc.mjm, sc.mjd, nworld, {**sc.options, **opts}, sc.per_world, tables=helpers.gpu_tables(rc))
+  w0, w1 = nworld - 6, nworld
+  ref = o.render(seed=2, worlds=(w0, w1))
+  np.testing.assert_array_equal(gpu["seg"][w0:w1], ref["seg"][w0:w1])
+  np.testing.assert_allclose(gpu["depth"][w0:w1], ref["depth"][w0:w1], rtol=1e-5, atol=1e-6)
+  assert helpers.rgb_diff(gpu["rgb"][w0:w1], ref["rgb"][w0:w1]).max() <= 1
+  # every world was rendered (no world left at the cleared value)
+  assert np.all(gpu["seg"].reshape(nworld, -1, 2)[:, :, 0].max(axis=1) >= 0)
