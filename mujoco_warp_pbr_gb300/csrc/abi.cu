@@ -36,6 +36,7 @@ namespace {
 
 constexpr int kMaxSmDevices = 64;
 std::atomic<int> g_device_sms[kMaxSmDevices];
+std::atomic<int> g_device_smem[kMaxSmDevices];
 
 }  // namespace
 
@@ -50,6 +51,24 @@ int device_sm_count() {
   if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
   if (dev >= 0 && dev < kMaxSmDevices) g_device_sms[dev].store(n, std::memory_order_relaxed);
   return n;
+}
+
+size_t device_max_smem() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 48 * 1024;
+  if (dev >= 0 && dev < kMaxSmDevices) {
+    const int cached = g_device_smem[dev].load(std::memory_order_relaxed);
+    if (cached > 0) return (size_t)cached;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || n <= 0) n = 48 * 1024;
+  if (dev >= 0 && dev < kMaxSmDevices) g_device_smem[dev].store(n, std::memory_order_relaxed);
+  return (size_t)n;
+}
+
+bool world_block_staged(int32_t floats, size_t other) {
+  // 8 KB of headroom for the kernels' static shared arrays
+  return (size_t)floats * sizeof(float) + other + 8 * 1024 <= device_max_smem();
 }
 
 namespace {

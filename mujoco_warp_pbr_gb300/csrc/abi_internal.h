@@ -14,6 +14,11 @@ int check_launch(const char* what);
 
 // Streaming multiprocessors of the current device (looked up once per device, thread-safe).
 int device_sm_count();
+// Largest dynamic shared memory one CTA may opt in to on the current device (bytes).
+size_t device_max_smem();
+// Whether a world block of `floats` floats fits in a CTA's shared memory beside `other` bytes
+// (traversal stacks, static arrays); kernels read larger blocks in place from global memory.
+bool world_block_staged(int32_t floats, size_t other);
 
 // MJPBR_OK, or MJPBR_ERR_ARG with a message naming the first inconsistent field of the scene.
 int validate_scene(const MjpbrScene* s, bool need_outputs);

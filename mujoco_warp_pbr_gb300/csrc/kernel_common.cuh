@@ -242,6 +242,19 @@ MJ_DEV void stage_world_block(const MjpbrScene& s, int32_t w, float* blk, int32_
   for (int32_t i = threadIdx.x; i < n4; i += nthreads) dst[i] = __ldg(src + i);
 }
 
+// The world block a CTA reads: world w's block staged into shared memory at smem (kStaged; the
+// caller synchronises before reading), or the block in global memory itself when it does not fit
+// in shared memory beside the traversal stacks.
+template <bool kStaged>
+MJ_DEV const float* world_block_of(const MjpbrScene& s, int32_t w, float* smem, int32_t nthreads) {
+  if constexpr (kStaged) {
+    stage_world_block(s, w, smem, nthreads);
+    return smem;
+  } else {
+    return s.world_blocks + (int64_t)w * s.world_block_floats;
+  }
+}
+
 // Per-world shading constants of a context.
 MJ_DEV void init_ctx(RtCtx& c, const MjpbrScene& s, const float* blk, const BlockLayout& L, int32_t w, bool tex) {
   c.s = &s;

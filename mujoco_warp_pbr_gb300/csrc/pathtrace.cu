@@ -75,18 +75,17 @@ struct Pt {
   }
 };
 
-template <bool kMesh, bool kTex>
+template <bool kMesh, bool kTex, bool kStaged>
 __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                          const __grid_constant__ PtTiles tm) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int32_t s_tile, s_next;
-  float* blk = smem;
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const MjpbrSettings& st = s.settings;
   const int lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
   RtCtx c;
-  c.st = shared_stack(smem + s.world_block_floats, kThreads, stack_entries(st.stack_depth));
+  c.st = shared_stack(smem + (kStaged ? s.world_block_floats : 0), kThreads, stack_entries(st.stack_depth));
   int32_t err = 0;
   for (;;) {
     if (threadIdx.x == 0) s_tile = atomicAdd(s.work_counter, 1);
@@ -99,7 +98,7 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
     while (cam + 1 < tm.ncam && lt >= tm.tile_base[cam + 1]) ++cam;
     const int32_t t = lt - tm.tile_base[cam];
     const int32_t tx = t % tm.tiles_x[cam], ty = t / tm.tiles_x[cam];
-    stage_world_block(s, w, blk, kThreads);
+    const float* blk = world_block_of<kStaged>(s, w, smem, kThreads);
     if (threadIdx.x == 0) s_next = 0;
     __syncthreads();
     init_ctx(c, s, blk, L, w, kTex);
@@ -172,10 +171,10 @@ __global__ void __launch_bounds__(kThreads, 2) pt_kernel(const __grid_constant__
   if (err && s.error_word) atomicOr(s.error_word, err);
 }
 
-template <bool kMesh, bool kTex>
+template <bool kMesh, bool kTex, bool kStaged>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const PtTiles& tm, cudaStream_t stream) {
-  size_t smem = (size_t)s.world_block_floats * sizeof(float) + (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
-  auto kern = pt_kernel<kMesh, kTex>;
+  size_t smem = (kStaged ? (size_t)s.world_block_floats * sizeof(float) : 0) + (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
+  auto kern = pt_kernel<kMesh, kTex, kStaged>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "path tracer: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
   int grid = std::min(tm.total, device_sm_count() * 2);
@@ -211,10 +210,17 @@ int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
   if (tm.total == 0) return MJPBR_OK;
   bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
-  if (mesh && tex) return launch_variant<true, true>(s, seed, tm, stream);
-  if (mesh) return launch_variant<true, false>(s, seed, tm, stream);
-  if (tex) return launch_variant<false, true>(s, seed, tm, stream);
-  return launch_variant<false, false>(s, seed, tm, stream);
+  if (world_block_staged(s.world_block_floats, (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8)) {
+    if (mesh && tex) return launch_variant<true, true, true>(s, seed, tm, stream);
+    if (mesh) return launch_variant<true, false, true>(s, seed, tm, stream);
+    if (tex) return launch_variant<false, true, true>(s, seed, tm, stream);
+    return launch_variant<false, false, true>(s, seed, tm, stream);
+  }
+  // world blocks too large for shared memory are read in place
+  if (mesh && tex) return launch_variant<true, true, false>(s, seed, tm, stream);
+  if (mesh) return launch_variant<true, false, false>(s, seed, tm, stream);
+  if (tex) return launch_variant<false, true, false>(s, seed, tm, stream);
+  return launch_variant<false, false, false>(s, seed, tm, stream);
 }
 
 }  // namespace mjpbr

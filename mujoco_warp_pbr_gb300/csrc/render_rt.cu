@@ -295,14 +295,14 @@ MJ_DEV Stack thread_stack(const MjpbrScene& s, float* stacks) {
 }
 
 // Grid schedule: one CTA per (camera tile, world); the hardware scheduler balances the CTAs.
-template <bool kMesh, bool kTex>
+template <bool kMesh, bool kTex, bool kStaged>
 __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                            const __grid_constant__ TileMap tm) {
   extern __shared__ __align__(16) float smem[];
-  float* blk = smem;
   const int32_t w = tm.w0 + blockIdx.y;
-  stage_world_block(s, w, blk, kThreads);
+  const float* blk = world_block_of<kStaged>(s, w, smem, kThreads);
   __syncthreads();
+  float* const stack_base = smem + (kStaged ? s.world_block_floats : 0);
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   const int32_t tile = blockIdx.x;
   int32_t cam = 0;
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
   if (s.settings.samples_per_axis == 2 && s.render_rgb[cam] != 0) {
     // sample lanes: 4 passes of 64 pixels, each warp a 4 x 2 pixel block (ROW tiles of 32 x 8 in
     // passes of 2 rows, TILED tiles of 16 x 16 in 8 x 8 quadrants)
-    const Stack st = thread_stack(s, smem + s.world_block_floats);
+    const Stack st = thread_stack(s, stack_base);
     const bool row = s.settings.render_order == MJPBR_ORDER_ROW;
     const int32_t smp = lane & 3, pix = lane >> 2;
 #pragma unroll 1
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, MJPBR_RT_MIN_BLOCKS) rt_kernel(const
     p.py = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
   }
   if (p.px >= p.width || p.py >= p.height) return;
-  render_pixel<kMesh, kTex>(s, seed, blk, L, w, p, thread_stack(s, smem + s.world_block_floats));
+  render_pixel<kMesh, kTex>(s, seed, blk, L, w, p, thread_stack(s, stack_base));
 }
 
 // Work items of the queue schedule: runs of `per_item` warp tiles (8 x 4 pixels) of one camera
@@ -411,11 +411,11 @@ constexpr size_t kQueueSmemLimit = kSmemPerSm / MJPBR_RT_MIN_BLOCKS - 2048;
 
 size_t stack_bytes(const MjpbrScene& s) { return (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8; }
 
-template <bool kMesh, bool kTex>
+template <bool kMesh, bool kTex, bool kStaged>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaStream_t stream) {
   static size_t smem_set = 0;
-  const size_t smem = (size_t)s.world_block_floats * sizeof(float) + stack_bytes(s);
-  auto kern = rt_kernel<kMesh, kTex>;
+  const size_t smem = (kStaged ? (size_t)s.world_block_floats * sizeof(float) : 0) + stack_bytes(s);
+  auto kern = rt_kernel<kMesh, kTex, kStaged>;
   if (smem > smem_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render: world block of %zu bytes: %s", smem, cudaGetErrorString(e));
@@ -513,10 +513,17 @@ int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
   if (tm.tile_base[s.nrender] == 0 || s.nworld == 0) return MJPBR_OK;
   bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
-  if (mesh && tex) return launch_variant<true, true>(s, seed, tm, stream);
-  if (mesh) return launch_variant<true, false>(s, seed, tm, stream);
-  if (tex) return launch_variant<false, true>(s, seed, tm, stream);
-  return launch_variant<false, false>(s, seed, tm, stream);
+  if (world_block_staged(s.world_block_floats, stack_bytes(s))) {
+    if (mesh && tex) return launch_variant<true, true, true>(s, seed, tm, stream);
+    if (mesh) return launch_variant<true, false, true>(s, seed, tm, stream);
+    if (tex) return launch_variant<false, true, true>(s, seed, tm, stream);
+    return launch_variant<false, false, true>(s, seed, tm, stream);
+  }
+  // world blocks too large for shared memory are read in place
+  if (mesh && tex) return launch_variant<true, true, false>(s, seed, tm, stream);
+  if (mesh) return launch_variant<true, false, false>(s, seed, tm, stream);
+  if (tex) return launch_variant<false, true, false>(s, seed, tm, stream);
+  return launch_variant<false, false, false>(s, seed, tm, stream);
 }
 
 }  // namespace mjpbr

@@ -254,16 +254,15 @@ MJ_DEV void emit_shadows(const MjpbrScene& s, const WaveMap& wm, const float* bl
 }
 
 // ---------------------------------------------------------------- 1. primary rays
-template <bool kMesh>
+template <bool kMesh, bool kStaged>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_primary_kernel(const __grid_constant__ MjpbrScene s,
                                                                 const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
-  float* blk = smem;
   const int32_t w = wm.w0 + blockIdx.y;
-  stage_world_block(s, w, blk, kThreads);
+  const float* blk = world_block_of<kStaged>(s, w, smem, kThreads);
   __syncthreads();
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
-  const Stack st = wave_stack(s, smem + s.world_block_floats);
+  const Stack st = wave_stack(s, smem + (kStaged ? s.world_block_floats : 0));
   int32_t cam, tx, ty;
   tile_of(wm.geo, blockIdx.x, &cam, &tx, &ty);
   Pixel p;
@@ -298,14 +297,13 @@ __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_TRACE_CTAS) wave_primary_
 }
 
 // ---------------------------------------------------------------- 2. surfaces at primary hits
-template <bool kMesh, bool kTex>
+template <bool kMesh, bool kTex, bool kStaged>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_surface_kernel(const __grid_constant__ MjpbrScene s,
                                                                 const __grid_constant__ WaveMap wm) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int32_t scan[kThreads / 32 + 1];
-  float* blk = smem;
   const int32_t w = wm.w0 + blockIdx.y;
-  stage_world_block(s, w, blk, kThreads);
+  const float* blk = world_block_of<kStaged>(s, w, smem, kThreads);
   __syncthreads();
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   int32_t cam, tx, ty;
@@ -503,14 +501,13 @@ struct StoredVis {
 };
 
 // ---------------------------------------------------------------- 6. shading and pixel outputs
-template <bool kTex>
+template <bool kTex, bool kStaged>
 __global__ void __launch_bounds__(kThreads, MJPBR_WAVE_SHADE_CTAS) wave_resolve_kernel(const __grid_constant__ MjpbrScene s, uint32_t seed,
                                                                 const __grid_constant__ WaveMap wm) {
   using Shade = RtShade<kTex, StoredVis>;
   extern __shared__ __align__(16) float smem[];
-  float* blk = smem;
   const int32_t w = wm.w0 + blockIdx.y;
-  stage_world_block(s, w, blk, kThreads);
+  const float* blk = world_block_of<kStaged>(s, w, smem, kThreads);
   __syncthreads();
   const BlockLayout L = block_layout(s.nbvh_geom, s.nnode, s.nlight, s.nrender);
   // a CTA shades `ppc` pixels of a tile with one thread per camera sample (nn consecutive threads
@@ -717,16 +714,17 @@ int set_smem(K kern, size_t smem, const char* what) {
   return MJPBR_OK;
 }
 
-template <bool kMesh, bool kTex>
+template <bool kMesh, bool kTex, bool kStaged>
 int launch_wave(const MjpbrScene& s, uint32_t seed, cudaStream_t stream, int32_t chunk, int32_t per_world) {
   const size_t stack = (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
-  const size_t blk_bytes = (size_t)s.world_block_floats * sizeof(float);
-  auto k_primary = wave_primary_kernel<kMesh>;
-  auto k_surface = wave_surface_kernel<kMesh, kTex>;
+  // world blocks staged in shared memory, or read in place when they do not fit
+  const size_t blk_bytes = kStaged ? (size_t)s.world_block_floats * sizeof(float) : 0;
+  auto k_primary = wave_primary_kernel<kMesh, kStaged>;
+  auto k_surface = wave_surface_kernel<kMesh, kTex, kStaged>;
   auto k_mirror = wave_mirror_kernel<kMesh>;
   auto k_msurface = wave_mirror_surface_kernel<kMesh, kTex>;
   auto k_shadow = wave_shadow_kernel<kMesh>;
-  auto k_resolve = wave_resolve_kernel<kTex>;
+  auto k_resolve = wave_resolve_kernel<kTex, kStaged>;
   int rc = set_smem(k_primary, blk_bytes + stack, "wavefront primary");
   if (!rc) rc = set_smem(k_surface, blk_bytes, "wavefront surface");
   if (!rc) rc = set_smem(k_mirror, stack, "wavefront mirror");
@@ -840,10 +838,17 @@ int render_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) 
   }
   const bool mesh = s.nmesh + s.nhfield > 0 && s.blas_root != nullptr;
   const bool tex = s.settings.textures || s.settings.has_env || s.settings.env_background;
-  if (mesh && tex) return launch_wave<true, true>(s, seed, stream, chunk, per_world);
-  if (mesh) return launch_wave<true, false>(s, seed, stream, chunk, per_world);
-  if (tex) return launch_wave<false, true>(s, seed, stream, chunk, per_world);
-  return launch_wave<false, false>(s, seed, stream, chunk, per_world);
+  const size_t stack = (size_t)kThreads * stack_entries(s.settings.stack_depth) * 8;
+  if (world_block_staged(s.world_block_floats, stack)) {
+    if (mesh && tex) return launch_wave<true, true, true>(s, seed, stream, chunk, per_world);
+    if (mesh) return launch_wave<true, false, true>(s, seed, stream, chunk, per_world);
+    if (tex) return launch_wave<false, true, true>(s, seed, stream, chunk, per_world);
+    return launch_wave<false, false, true>(s, seed, stream, chunk, per_world);
+  }
+  if (mesh && tex) return launch_wave<true, true, false>(s, seed, stream, chunk, per_world);
+  if (mesh) return launch_wave<true, false, false>(s, seed, stream, chunk, per_world);
+  if (tex) return launch_wave<false, true, false>(s, seed, stream, chunk, per_world);
+  return launch_wave<false, false, false>(s, seed, stream, chunk, per_world);
 }
 
 }  // namespace mjpbr

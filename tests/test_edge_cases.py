@@ -128,3 +128,50 @@ def test_more_worlds_than_one_grid_dimension(schedule, tier):
   assert helpers.rgb_diff(gpu["rgb"][w0:w1], ref["rgb"][w0:w1]).max() <= 1
   # every world was rendered (no world left at the cleared value)
   assert np.all(gpu["seg"].reshape(nworld, -1, 2)[:, :, 0].max(axis=1) >= 0)
+
+
+def _crowded_scene(n: int = 2000, nworld: int = 2, res: int = 32):
+  """A ground plane and n small primitives per world: a world block larger than shared memory."""
+  rng = np.random.default_rng(5)
+  b = synthetic.Builder()
+  b.geom(GEOM_PLANE, (8.0, 8.0, 0.1), rgba=(0.6, 0.6, 0.6, 1.0))
+  for i in range(n):
+    kind = (GEOM_SPHERE, GEOM_BOX)[i % 2]
+    pos = (*rng.uniform(-3.0, 3.0, 2), rng.uniform(0.05, 1.5))
+    size = (0.06, 0.0, 0.0) if kind == GEOM_SPHERE else (0.05, 0.04, 0.03)
+    b.geom(kind, size, pos=pos, rgba=(*rng.uniform(0.1, 1.0, 3), 1.0))
+  b.light(LIGHT_DIRECTIONAL, pos=(0, 0, 4), dir=(0.3, 0.2, -1.0), diffuse=(0.7, 0.7, 0.7), castshadow=True)
+  b.light(LIGHT_POINT, pos=(0.5, -0.5, 2.0), diffuse=(0.5, 0.5, 0.5), range=10.0, bulbradius=0.05, castshadow=True)
+  b.camera((0.0, -5.0, 3.0), (0.0, 0.0, 0.3), fovy=50.0, resolution=(res, res))
+  mjm, mjd = b.build()
+  return synthetic.SyntheticScene(
+    name="crowded", mjm=mjm, mjd=mjd, nworld=nworld,
+    options={"cam_res": (res, res), "render_rgb": True, "render_depth": True, "render_seg": True, "shadow_samples": 4},
+    per_world={}, seed=5,
+  )
+
+
+def test_crowded_world_block_exceeds_shared_memory():
+  from mujoco_warp_pbr_gb300 import _lib, context
+
+  sc = _crowded_scene()
+  hc = context.prepare_context(sc.mjm, sc.nworld, data=sc.mjd, **sc.options)
+  assert hc.world_block_floats * 4 > 232448  # more than a GB300 CTA's shared memory
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("schedule", ["grid", "wavefront"])
+@pytest.mark.parametrize("tier", [0, 1])
+def test_crowded_worlds_render_from_global_memory(schedule, tier):
+  """2,001 geoms per world: the kernels that stage a world block in shared memory read it in place
+  instead, with the same images as the oracle."""
+  sc = _crowded_scene()
+  opts = {"tier": tier, "path_samples": 2, "max_depth": 2} if tier else {}
+  m, d, rc = helpers.gpu_scene(sc, schedule=schedule, **opts)
+  gpu = helpers.render_gpu(m, d, rc, seed=3)
+  ref = helpers.oracle_render(sc, seed=3, tables=helpers.gpu_tables(rc), **opts)
+  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
+  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
+  assert helpers.rgb_diff(gpu["rgb"], ref["rgb"]).max() <= 1
+  assert (gpu["seg"][..., 0] > 0).mean() > 0.2  # many primitives in view
