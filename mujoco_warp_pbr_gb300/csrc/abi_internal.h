@@ -26,6 +26,8 @@ int validate_scene(const MjpbrScene* s, bool need_outputs);
 int refit_launch(const MjpbrScene& s, cudaStream_t stream);
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
 int render_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
+bool wave_supported(const MjpbrScene& s);
+bool pt_wave_supported(const MjpbrScene& s);
 int64_t wave_scratch_bytes(const MjpbrScene& s, int32_t worlds);
 int render_pt_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream);
 int64_t pt_wave_scratch_bytes(const MjpbrScene& s, int32_t worlds);

@@ -192,7 +192,7 @@ int render_pt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
   if (s.settings.denoise && (!s.hdr_data || !s.aov_guide || !s.aov_emission || !s.denoise_buffers[0])) {
     return set_error(MJPBR_ERR_ARG, "denoise needs the hdr, guide, emission and denoise buffers");
   }
-  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT) return render_pt_wave_launch(s, seed, stream);
+  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT && pt_wave_supported(s)) return render_pt_wave_launch(s, seed, stream);
   PtTiles tm;
   tm.ncam = s.nrender;
   tm.tile_base[0] = 0;

@@ -705,9 +705,13 @@ int64_t pt_wave_scratch_bytes(const MjpbrScene& s, int32_t worlds) {
   return layout(nullptr, nullptr, (int64_t)worlds * pixels * s.settings.path_samples, slots_of(s));
 }
 
+// The path wavefront's records pack geom slots and triangle BVH ids in 16 bits; larger scenes render
+// with the persistent path kernel (the same images).
+bool pt_wave_supported(const MjpbrScene& s) { return s.nbvh_geom <= 0xffff && s.nmesh + s.nhfield < 0x7fff; }
+
 int render_pt_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
-  if (s.nbvh_geom > 0xffff || s.nmesh + s.nhfield >= 0x7fff) {
-    return set_error(MJPBR_ERR_UNSUPPORTED, "the path wavefront packs slots and triangle BVHs in 16 bits");
+  if (!pt_wave_supported(s)) {
+    return set_error(MJPBR_ERR_UNSUPPORTED, "the path wavefront packs slots and triangle BVHs in 16 bits; use the grid schedule");
   }
   if (!s.wave_scratch || (reinterpret_cast<uintptr_t>(s.wave_scratch) & 255u)) {
     return set_error(MJPBR_ERR_ARG, "the path wavefront needs wave_scratch (256-byte aligned)");

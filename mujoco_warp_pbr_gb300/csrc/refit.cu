@@ -30,6 +30,96 @@ __device__ float4 effective_rgba(const MjpbrScene& s, int32_t w, int32_t g, int3
   return c;
 }
 
+// What a geom's world AABB depends on: its pose, size, type, triangle BVH and flags, as the world
+// block's geom record holds them.
+struct GeomBoxIn {
+  V3 pos;
+  float m[9];
+  V3 size;
+  int32_t type, blas, flags;
+};
+
+__device__ __forceinline__ GeomBoxIn geom_box_in(const float* gr) {
+  GeomBoxIn in;
+  in.pos = V3{gr[0], gr[1], gr[2]};
+  in.type = __float_as_int(gr[3]);
+  in.m[0] = gr[4], in.m[1] = gr[5], in.m[2] = gr[6];
+  in.m[3] = gr[8], in.m[4] = gr[9], in.m[5] = gr[10];
+  in.m[6] = gr[12], in.m[7] = gr[13], in.m[8] = gr[14];
+  in.size = V3{gr[7], gr[11], gr[15]};
+  in.blas = __float_as_int(gr[17]);
+  in.flags = __float_as_int(gr[19]);
+  return in;
+}
+
+// Padded world AABB (lo, hi) of a geom into b[6]; b[0] = FLT_MAX marks a skipped geom.
+__device__ __forceinline__ void geom_box(const MjpbrScene& s, const GeomBoxIn& in, float* b) {
+  const float* m = in.m;
+  const int32_t type = in.type, blas = in.blas;
+  const V3 pos = in.pos, size = in.size;
+  // world AABB: centre c, half extent e per axis
+  V3 c = pos, e;
+  float ax[3];
+  for (int i = 0; i < 3; ++i) {
+    float r0 = fabsf(m[3 * i]), r1 = fabsf(m[3 * i + 1]), r2 = fabsf(m[3 * i + 2]);
+    switch (type) {
+      case MJPBR_GEOM_SPHERE:
+        ax[i] = size.x;
+        break;
+      case MJPBR_GEOM_CAPSULE:
+        ax[i] = r2 * size.y + size.x;
+        break;
+      case MJPBR_GEOM_ELLIPSOID: {
+        float a = m[3 * i] * size.x, bb = m[3 * i + 1] * size.y, cc = m[3 * i + 2] * size.z;
+        ax[i] = sqrtf(a * a + bb * bb + cc * cc);
+        break;
+      }
+      case MJPBR_GEOM_CYLINDER:
+        ax[i] = r2 * size.y + size.x * sqrtf(fmaxf(0.0f, 1.0f - m[3 * i + 2] * m[3 * i + 2]));
+        break;
+      case MJPBR_GEOM_BOX:
+        ax[i] = r0 * size.x + r1 * size.y + r2 * size.z;
+        break;
+      case MJPBR_GEOM_PLANE: {
+        float sx = size.x > 0.0f ? size.x : kBigExtent;
+        float sy = size.y > 0.0f ? size.y : kBigExtent;
+        ax[i] = r0 * sx + r1 * sy;
+        break;
+      }
+      default: {  // mesh or height field: transformed local AABB
+        if (blas >= 0 && s.mesh_bounds) {
+          const float* mb = s.mesh_bounds + blas * 6;
+          float hx = 0.5f * (mb[3] - mb[0]), hy = 0.5f * (mb[4] - mb[1]), hz = 0.5f * (mb[5] - mb[2]);
+          ax[i] = r0 * hx + r1 * hy + r2 * hz;
+        } else {
+          ax[i] = 0.0f;
+        }
+        break;
+      }
+    }
+  }
+  if (blas >= 0 && s.mesh_bounds) {
+    const float* mb = s.mesh_bounds + blas * 6;
+    V3 lc{0.5f * (mb[0] + mb[3]), 0.5f * (mb[1] + mb[4]), 0.5f * (mb[2] + mb[5])};
+    c = pos + V3{m[0] * lc.x + m[1] * lc.y + m[2] * lc.z, m[3] * lc.x + m[4] * lc.y + m[5] * lc.z,
+                 m[6] * lc.x + m[7] * lc.y + m[8] * lc.z};
+  }
+  e = V3{ax[0], ax[1], ax[2]};
+  // Conservative padding: box tests may round differently from the exact primitive tests.
+  float mag = fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z)) + vmax3(e);
+  float pad = 1.0e-5f * (1.0f + mag);
+  b[0] = c.x - e.x - pad;
+  b[1] = c.y - e.y - pad;
+  b[2] = c.z - e.z - pad;
+  b[3] = c.x + e.x + pad;
+  b[4] = c.y + e.y + pad;
+  b[5] = c.z + e.z + pad;
+  if (in.flags & kGeomFlagSkip) b[0] = FLT_MAX;  // marks an empty leaf
+}
+
+// kSmemBoxes: the lanes compute the leaf boxes into shared memory before lane 0's sweep; without
+// (worlds whose boxes do not fit), the sweep computes each leaf's box from its geom record.
+template <bool kSmemBoxes>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_constant__ MjpbrScene s) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31;
@@ -37,7 +127,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
   const int32_t w = blockIdx.x * kWarpsPerCta + warp;
   if (w >= s.nworld) return;
   const int32_t nbvh = s.nbvh_geom;
-  float* box = smem + (int64_t)warp * nbvh * 6;  // leaf AABBs of this world
+  float* box = kSmemBoxes ? smem + (int64_t)warp * nbvh * 6 : nullptr;  // leaf AABBs of this world
   BlockLayout L = block_layout(nbvh, s.nnode, s.nlight, s.nrender);
   float* blk = s.world_blocks + (int64_t)w * s.world_block_floats;
 
@@ -88,65 +178,16 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
     gr[18] = __int_as_float(matid);
     gr[19] = __int_as_float(flags);
 
-    // world AABB: centre c, half extent e per axis
-    V3 c = pos, e;
-    float ax[3];
-    for (int i = 0; i < 3; ++i) {
-      float r0 = fabsf(m[3 * i]), r1 = fabsf(m[3 * i + 1]), r2 = fabsf(m[3 * i + 2]);
-      switch (type) {
-        case MJPBR_GEOM_SPHERE:
-          ax[i] = size.x;
-          break;
-        case MJPBR_GEOM_CAPSULE:
-          ax[i] = r2 * size.y + size.x;
-          break;
-        case MJPBR_GEOM_ELLIPSOID: {
-          float a = m[3 * i] * size.x, b = m[3 * i + 1] * size.y, cc = m[3 * i + 2] * size.z;
-          ax[i] = sqrtf(a * a + b * b + cc * cc);
-          break;
-        }
-        case MJPBR_GEOM_CYLINDER:
-          ax[i] = r2 * size.y + size.x * sqrtf(fmaxf(0.0f, 1.0f - m[3 * i + 2] * m[3 * i + 2]));
-          break;
-        case MJPBR_GEOM_BOX:
-          ax[i] = r0 * size.x + r1 * size.y + r2 * size.z;
-          break;
-        case MJPBR_GEOM_PLANE: {
-          float sx = size.x > 0.0f ? size.x : kBigExtent;
-          float sy = size.y > 0.0f ? size.y : kBigExtent;
-          ax[i] = r0 * sx + r1 * sy;
-          break;
-        }
-        default: {  // mesh or height field: transformed local AABB
-          if (blas >= 0 && s.mesh_bounds) {
-            const float* mb = s.mesh_bounds + blas * 6;
-            float hx = 0.5f * (mb[3] - mb[0]), hy = 0.5f * (mb[4] - mb[1]), hz = 0.5f * (mb[5] - mb[2]);
-            ax[i] = r0 * hx + r1 * hy + r2 * hz;
-          } else {
-            ax[i] = 0.0f;
-          }
-          break;
-        }
-      }
+    if constexpr (kSmemBoxes) {
+      GeomBoxIn in;
+      in.pos = pos;
+      for (int k = 0; k < 9; ++k) in.m[k] = m[k];
+      in.size = size;
+      in.type = type;
+      in.blas = blas;
+      in.flags = flags;
+      geom_box(s, in, box + slot * 6);
     }
-    if (blas >= 0 && s.mesh_bounds) {
-      const float* mb = s.mesh_bounds + blas * 6;
-      V3 lc{0.5f * (mb[0] + mb[3]), 0.5f * (mb[1] + mb[4]), 0.5f * (mb[2] + mb[5])};
-      c = pos + V3{m[0] * lc.x + m[1] * lc.y + m[2] * lc.z, m[3] * lc.x + m[4] * lc.y + m[5] * lc.z,
-                   m[6] * lc.x + m[7] * lc.y + m[8] * lc.z};
-    }
-    e = V3{ax[0], ax[1], ax[2]};
-    // Conservative padding: box tests may round differently from the exact primitive tests.
-    float mag = fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z)) + vmax3(e);
-    float pad = 1.0e-5f * (1.0f + mag);
-    float* b = box + slot * 6;
-    b[0] = c.x - e.x - pad;
-    b[1] = c.y - e.y - pad;
-    b[2] = c.z - e.z - pad;
-    b[3] = c.x + e.x + pad;
-    b[4] = c.y + e.y + pad;
-    b[5] = c.z + e.z + pad;
-    if (flags & kGeomFlagSkip) b[0] = FLT_MAX;  // marks an empty leaf
   }
 
   // ---- lights
@@ -240,7 +281,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
           cnt = -1;
         } else if (c < 0) {
           int32_t slot = ~c;
-          const float* b = box + slot * 6;
+          float tb[6];
+          const float* b = tb;
+          if constexpr (kSmemBoxes) {
+            b = box + slot * 6;
+          } else {
+            geom_box(s, geom_box_in(blk + L.geom_off + slot * kGeomFloats), tb);
+          }
           if (b[0] != FLT_MAX) {
             for (int a = 0; a < 3; ++a) {
               lo[a] = b[a];
@@ -280,15 +327,17 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) refit_kernel(const __grid_c
 }  // namespace
 
 int refit_launch(const MjpbrScene& s, cudaStream_t stream) {
-  size_t smem = (size_t)kWarpsPerCta * s.nbvh_geom * 6 * sizeof(float);
-  if (smem > 200 * 1024) {
-    return set_error(MJPBR_ERR_ARG, "refit: too many enabled geoms per world (%d)", s.nbvh_geom);
+  const size_t smem = (size_t)kWarpsPerCta * s.nbvh_geom * 6 * sizeof(float);
+  const int grid = (s.nworld + kWarpsPerCta - 1) / kWarpsPerCta;
+  if (smem <= 200 * 1024) {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(refit_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "refit: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
+    }
+    refit_kernel<true><<<grid, kWarpsPerCta * 32, smem, stream>>>(s);
+  } else {
+    refit_kernel<false><<<grid, kWarpsPerCta * 32, 0, stream>>>(s);  // leaf boxes computed in the sweep
   }
-  if (smem > 48 * 1024) {
-    cudaFuncSetAttribute(refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  }
-  int grid = (s.nworld + kWarpsPerCta - 1) / kWarpsPerCta;
-  refit_kernel<<<grid, kWarpsPerCta * 32, smem, stream>>>(s);
   return check_launch("refit_kernel");
 }
 

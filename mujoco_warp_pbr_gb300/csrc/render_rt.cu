@@ -482,8 +482,9 @@ bool rt_queue_fits(const MjpbrScene& s) {
 }
 
 int render_rt_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
-  // translucent layers are not staged: such scenes render with the grid schedule (same images)
-  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT && !s.settings.has_transparency) return render_wave_launch(s, seed, stream);
+  // scenes the wavefront does not stage (translucent layers, more than 65535 geoms) render with the
+  // grid schedule (same images)
+  if (s.settings.schedule == MJPBR_SCHEDULE_WAVEFRONT && wave_supported(s)) return render_wave_launch(s, seed, stream);
   if (s.settings.schedule == MJPBR_SCHEDULE_QUEUE) {
     if (!s.work_counter) return set_error(MJPBR_ERR_ARG, "the queue schedule needs the work_counter scratch");
     if (!rt_queue_fits(s)) {

@@ -799,14 +799,16 @@ int64_t wave_scratch_bytes(const MjpbrScene& s, int32_t worlds) {
   return layout(nullptr, nullptr, worlds, per_world, s.nlight);
 }
 
-bool wave_supported(const MjpbrScene& s) { return !s.settings.has_transparency; }
+// The wavefront's records pack geom slots and triangle BVH ids in 16 bits, and its stages do not
+// render translucent layers; other scenes render with the grid schedule (the same images).
+bool wave_supported(const MjpbrScene& s) {
+  return !s.settings.has_transparency && s.nbvh_geom <= 0xffff && s.nmesh + s.nhfield < 0x7fff;
+}
 
 int render_wave_launch(const MjpbrScene& s, uint32_t seed, cudaStream_t stream) {
   if (!wave_supported(s)) {
-    return set_error(MJPBR_ERR_UNSUPPORTED, "the wavefront schedule does not render translucent layers; use the grid schedule");
-  }
-  if (s.nbvh_geom > 0xffff || s.nmesh + s.nhfield >= 0x7fff) {
-    return set_error(MJPBR_ERR_UNSUPPORTED, "the wavefront schedule packs slots and triangle BVHs in 16 bits");
+    return set_error(MJPBR_ERR_UNSUPPORTED, "the wavefront schedule renders neither translucent layers nor more than 65535 geoms "
+                                            "or 32766 triangle BVHs; use the grid schedule");
   }
   const int32_t per_world = samples_per_world(s);
   if (per_world < 0) return set_error(MJPBR_ERR_ARG, "wavefront: too many samples per world");

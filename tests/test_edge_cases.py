@@ -175,3 +175,20 @@ def test_crowded_worlds_render_from_global_memory(schedule, tier):
   np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
   assert helpers.rgb_diff(gpu["rgb"], ref["rgb"]).max() <= 1
   assert (gpu["seg"][..., 0] > 0).mean() > 0.2  # many primitives in view
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not torch.cuda.is_available(), reason="needs a CUDA GPU")
+@pytest.mark.parametrize("tier", [0, 1])
+def test_more_geoms_than_the_wavefront_packs(tier):
+  """65,601 geoms per world: more than the wavefront's 16-bit slot ids, so a context on the
+  wavefront schedule renders with the grid schedule (real-time) or the persistent path kernel, with
+  world blocks read in place; the images match the oracle."""
+  sc = _crowded_scene(n=65600, nworld=2, res=8)
+  opts = {"tier": tier, "path_samples": 2, "max_depth": 2} if tier else {}
+  m, d, rc = helpers.gpu_scene(sc, schedule="wavefront", **opts)
+  gpu = helpers.render_gpu(m, d, rc, seed=4)
+  ref = helpers.oracle_render(sc, seed=4, tables=helpers.gpu_tables(rc), **opts)
+  np.testing.assert_array_equal(gpu["seg"], ref["seg"])
+  np.testing.assert_allclose(gpu["depth"], ref["depth"], rtol=1e-5, atol=1e-6)
+  assert helpers.rgb_diff(gpu["rgb"], ref["rgb"]).max() <= 1
