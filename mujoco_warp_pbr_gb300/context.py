@@ -644,7 +644,9 @@ _SRGB_TABLE = srgb_to_linear(np.arange(256) / 255.0).astype(np.float16)
 
 
 def mip_count(w: int, h: int) -> int:
-  return int(math.floor(math.log2(max(w, h)))) + 1
+  """Levels of a full mip chain, at most the descriptor's MAX_MIPS (textures above 16384 texels per
+  side stop at their 15th level; level-of-detail selection clamps to the last level)."""
+  return min(int(math.floor(math.log2(max(w, h)))) + 1, _lib.MAX_MIPS)
 
 
 @dataclasses.dataclass

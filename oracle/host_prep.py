@@ -28,6 +28,8 @@ from typing import Any
 
 import numpy as np
 
+from oracle import scene_struct as ss
+
 # include/mjpbr.h enums
 GEOM_PLANE, GEOM_HFIELD, GEOM_MESH, GEOM_SDF = 0, 1, 7, 8
 LIGHT_DIRECTIONAL = 1
@@ -488,7 +490,8 @@ def prepare(mjm: Any, mjd: Any, nworld: int, options: dict[str, Any]) -> Prepare
 
 
 def mip_count(w: int, h: int) -> int:
-  return int(math.floor(math.log2(max(w, h)))) + 1
+  """Full mip chain length, at most the texture descriptor's MJPBR_MAX_MIPS levels."""
+  return min(int(math.floor(math.log2(max(w, h)))) + 1, ss.MAX_MIPS)
 
 
 def pack_textures(images: list[tuple[int, np.ndarray]], texture_type: Any) -> tuple[list[Any], np.ndarray]:
