@@ -1,6 +1,9 @@
 // C entry points of libmjpbr (declared in include/mjpbr.h): argument checks, error reporting and
 // dispatch to the kernel launchers. Nothing here synchronises or allocates.
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
@@ -64,6 +67,21 @@ size_t device_max_smem() {
   if (cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || n <= 0) n = 48 * 1024;
   if (dev >= 0 && dev < kMaxSmDevices) g_device_smem[dev].store(n, std::memory_order_relaxed);
   return (size_t)n;
+}
+
+int ensure_smem(const void* kern, size_t bytes, const char* what) {
+  // also below 48 KB: a kernel's static shared memory counts against the default limit too
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "%s: no current device", what);
+  static std::mutex lock;
+  static std::map<std::pair<const void*, int>, size_t> raised;
+  std::lock_guard<std::mutex> guard(lock);
+  size_t& have = raised[{kern, dev}];
+  if (bytes <= have) return MJPBR_OK;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "%s: %zu bytes of shared memory: %s", what, bytes, cudaGetErrorString(e));
+  have = bytes;
+  return MJPBR_OK;
 }
 
 bool world_block_staged(int32_t floats, size_t other) {

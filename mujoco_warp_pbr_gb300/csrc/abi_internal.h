@@ -16,6 +16,10 @@ int check_launch(const char* what);
 int device_sm_count();
 // Largest dynamic shared memory one CTA may opt in to on the current device (bytes).
 size_t device_max_smem();
+// Raises kernel `kern`'s dynamic shared-memory limit to at least `bytes` on the current device
+// (each kernel and device once per larger size, whatever the size: the kernel's static shared
+// memory counts against the default limit too; thread-safe). MJPBR_OK or MJPBR_ERR_CUDA.
+int ensure_smem(const void* kern, size_t bytes, const char* what);
 // Whether a world block of `floats` floats fits in a CTA's shared memory beside `other` bytes
 // (traversal stacks, static arrays); kernels read larger blocks in place from global memory.
 bool world_block_staged(int32_t floats, size_t other);

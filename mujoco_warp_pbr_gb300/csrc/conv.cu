@@ -791,12 +791,7 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     }
     const size_t smem = wg.ring ? (size_t)wg.b_off + wbytes : fixed + (size_t)nst * stage_bytes(G, resident);
     if (smem > kPipeSmemMax) return set_error(MJPBR_ERR_ARG, "conv3x3: %zu bytes of shared memory needed", smem);
-    static bool ws_smem_set = false;
-    if (!ws_smem_set) {
-      cudaError_t e = cudaFuncSetAttribute(conv3x3_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmemMax);
-      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "conv3x3: %zu bytes of shared memory: %s", kPipeSmemMax, cudaGetErrorString(e));
-      ws_smem_set = true;
-    }
+    if (int rc = ensure_smem(reinterpret_cast<const void*>(conv3x3_ws_kernel), kPipeSmemMax, "conv3x3")) return rc;
     CUtensorMap tm_in, tm_in2, tm_w;
     memset(&tm_in2, 0, sizeof(tm_in2));
     if (wg.ring) {
@@ -828,12 +823,7 @@ int conv3x3_launch(const MjpbrConv& c, cudaStream_t stream) {
     return check_launch("conv3x3_ws_kernel");
   }
   const size_t smem = (size_t)6 * (g.rows + 2) * g.pitch * 16 + (size_t)18 * c.c_out * 16;
-  static size_t smem_set = 0;
-  if (smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(conv3x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "conv3x3: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
-    smem_set = smem;
-  }
+  if (int rc = ensure_smem(reinterpret_cast<const void*>(conv3x3_kernel), smem, "conv3x3")) return rc;
   conv3x3_kernel<<<(unsigned)tiles, kConvThreads, smem, stream>>>(c, g);
   return check_launch("conv3x3_kernel");
 }
@@ -1220,12 +1210,7 @@ int wgrad_ws_launch(const MjpbrConvGrad& c, const WgradGeom& gg, cudaStream_t st
   wg.nstage = std::min<int64_t>(kWgMaxStages, (int64_t)kPipeSmemMax / wg.stage_bytes);
   if (wg.nstage < 2) return kWgradWsUnsuitable;
   const size_t smem = (size_t)wg.nstage * wg.stage_bytes;
-  static bool smem_set = false;
-  if (!smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmemMax);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "conv3x3 wgrad: %zu bytes of shared memory: %s", kPipeSmemMax, cudaGetErrorString(e));
-    smem_set = true;
-  }
+  if (int rc = ensure_smem(reinterpret_cast<const void*>(conv3x3_wgrad_ws_kernel), kPipeSmemMax, "conv3x3 wgrad")) return rc;
   CUtensorMap tm_go, tm_in, tm_in2;
   memset(&tm_in2, 0, sizeof(tm_in2));
   if (make_act_map(&tm_go, c.grad_out, c.c_out, c.width, c.height, c.nimg, gg.pitch, gg.rows, c.c_out / 8) != 0) return MJPBR_ERR_CUDA;
@@ -1288,12 +1273,7 @@ int conv3x3_wgrad_launch(const MjpbrConvGrad& c, cudaStream_t stream) {
   const int32_t splits = (g.total + g.per_cta - 1) / g.per_cta;
   if (splits > 65535) return set_error(MJPBR_ERR_ARG, "conv3x3 wgrad: %d tile runs exceed the grid; raise tiles_per_cta", splits);
   const size_t smem = (size_t)16 * 16 * 128 + (size_t)16 * c.c_out * 16;
-  static size_t smem_set = 0;
-  if (smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "conv3x3 wgrad: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
-    smem_set = smem;
-  }
+  if (int rc = ensure_smem(reinterpret_cast<const void*>(conv3x3_wgrad_kernel), smem, "conv3x3 wgrad")) return rc;
   conv3x3_wgrad_kernel<<<dim3(mblocks, splits), kConvThreads, smem, stream>>>(c, g);
   if (int rc = check_launch("conv3x3_wgrad_kernel")) return rc;
   if (c.grad_bias) {

@@ -111,12 +111,7 @@ int gemm_bf16_launch(const uint16_t* a, const uint16_t* b, float* d, int32_t m, 
   // at least 64 KB: every operand read the descriptors can express for these shapes stays inside
   // the allocation
   const size_t smem = std::max<size_t>((size_t)(kChunk / 8) * (kRows + n) * 16, 64 * 1024);
-  static size_t smem_set = 0;
-  if (smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "gemm: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
-    smem_set = smem;
-  }
+  if (int rc = ensure_smem(reinterpret_cast<const void*>(gemm_bf16_kernel), smem, "gemm")) return rc;
   gemm_bf16_kernel<<<m / kRows, kGemmThreads, smem, stream>>>(a, b, d, n, k, error_word);
   return check_launch("gemm_bf16_kernel");
 }

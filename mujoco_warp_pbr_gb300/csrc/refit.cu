@@ -330,10 +330,7 @@ int refit_launch(const MjpbrScene& s, cudaStream_t stream) {
   const size_t smem = (size_t)kWarpsPerCta * s.nbvh_geom * 6 * sizeof(float);
   const int grid = (s.nworld + kWarpsPerCta - 1) / kWarpsPerCta;
   if (smem <= 200 * 1024) {
-    if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(refit_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "refit: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
-    }
+    if (int rc = ensure_smem(reinterpret_cast<const void*>(refit_kernel<true>), smem, "refit")) return rc;
     refit_kernel<true><<<grid, kWarpsPerCta * 32, smem, stream>>>(s);
   } else {
     refit_kernel<false><<<grid, kWarpsPerCta * 32, 0, stream>>>(s);  // leaf boxes computed in the sweep

@@ -413,14 +413,9 @@ size_t stack_bytes(const MjpbrScene& s) { return (size_t)kThreads * stack_entrie
 
 template <bool kMesh, bool kTex, bool kStaged>
 int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaStream_t stream) {
-  static size_t smem_set = 0;
   const size_t smem = (kStaged ? (size_t)s.world_block_floats * sizeof(float) : 0) + stack_bytes(s);
   auto kern = rt_kernel<kMesh, kTex, kStaged>;
-  if (smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render: world block of %zu bytes: %s", smem, cudaGetErrorString(e));
-    smem_set = smem;
-  }
+  if (int rc = ensure_smem(reinterpret_cast<const void*>(kern), smem, "render")) return rc;
   TileMap part = tm;
   for (int32_t w0 = 0; w0 < s.nworld; w0 += kMaxGridWorlds) {
     part.w0 = w0;
@@ -434,14 +429,9 @@ int launch_variant(const MjpbrScene& s, uint32_t seed, const TileMap& tm, cudaSt
 
 template <bool kMesh, bool kTex>
 int launch_queue_variant(const MjpbrScene& s, uint32_t seed, const QueueMap& qm, cudaStream_t stream) {
-  static size_t smem_set = 0;
   const size_t smem = (size_t)(kThreads / 32) * s.world_block_floats * sizeof(float) + stack_bytes(s);
   auto kern = rt_queue_kernel<kMesh, kTex>;
-  if (smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render queue: %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
-    smem_set = smem;
-  }
+  if (int rc = ensure_smem(reinterpret_cast<const void*>(kern), smem, "render queue")) return rc;
   cudaError_t e = cudaMemsetAsync(s.work_counter + 1, 0, sizeof(int32_t), stream);
   if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "render queue: work counter: %s", cudaGetErrorString(e));
   const int grid = std::min(qm.total, device_sm_count() * MJPBR_RT_MIN_BLOCKS);

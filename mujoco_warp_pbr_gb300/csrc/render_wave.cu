@@ -708,10 +708,7 @@ int resident_ctas(K kern, size_t smem) {
 
 template <class K>
 int set_smem(K kern, size_t smem, const char* what) {
-  if (smem <= 48 * 1024) return MJPBR_OK;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return set_error(MJPBR_ERR_CUDA, "%s: %zu bytes of shared memory: %s", what, smem, cudaGetErrorString(e));
-  return MJPBR_OK;
+  return ensure_smem(reinterpret_cast<const void*>(kern), smem, what);
 }
 
 template <bool kMesh, bool kTex, bool kStaged>
